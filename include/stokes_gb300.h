@@ -1,0 +1,231 @@
+/*
+ * stokes_gb300.h - C ABI of the GB300 Brinkman-Stokes topology-optimization hot path.
+ *
+ * One handle owns one problem on one GPU: the multigrid hierarchy, the Krylov
+ * workspace and the design-loop buffers, all resident in device memory. Every call
+ * returns 0 on success and a negative STG_E_* code on failure; stg_last_error()
+ * gives the message of the last failure on the calling thread. A handle is used by
+ * one host thread at a time and issues its work on its own CUDA stream.
+ *
+ * Host arrays use the simplex Field order of the reference
+ * (simplex/src/reservoir/Field.h:67-72): a 3D cell array has N^3 entries with cell
+ * (i,j,k) at (i*N + j)*N + k; face axis d is a separate array with N+1 entries along
+ * d (simplex/src/reservoir/FaceField.h:16), so Field::array.data() plugs in directly.
+ * 2D arrays follow the same rule with (i*N + j).
+ *
+ * "Blocked" device vectors use the reference solver layout
+ * [cells | x-faces | y-faces | z-faces] of common_cpx/grid3D.cu:24-146, so the
+ * device-pointer entry points can sit behind the reference LinearMapping interface
+ * (common_cpx/LinearMapping.h:4-14) unchanged.
+ */
+#ifndef STOKES_GB300_H
+#define STOKES_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define STG_OK 0
+#define STG_E_INVALID (-1)     /* bad argument, size or state */
+#define STG_E_CUDA (-2)        /* a CUDA call failed */
+#define STG_E_NOMEM (-3)       /* device allocation failed */
+#define STG_E_UNSUPPORTED (-4) /* input outside what this build implements */
+#define STG_E_NOT_CONVERGED (-5)
+#define STG_E_NONFINITE (-6) /* NaN/Inf met in a residual */
+
+typedef struct stg_ctx stg_t;
+
+/* Solver method of stg_solve. */
+#define STG_METHOD_PLAIN 0 /* FP32 V-cycle preconditioned FGMRES inside FP64 refinement */
+#define STG_METHOD_MIXED 1 /* as PLAIN with BF16-stored coarse-level corrections */
+
+typedef struct stg_opts {
+    int method;          /* STG_METHOD_* */
+    double tol;          /* FP64 true relative residual ||b-Ax||/||b|| to reach */
+    int max_outer;       /* FP64 refinement steps */
+    int inner_max;       /* FGMRES basis size of one refinement step */
+    double inner_tol;    /* relative reduction asked of one refinement step */
+    int verbose;         /* print per-iteration residuals to stderr */
+} stg_opts;
+
+typedef struct stg_stats {
+    int outer_iters;     /* FP64 refinement steps taken */
+    int inner_iters;     /* total FGMRES iterations (= V-cycles) */
+    double rel_residual; /* final FP64 true relative residual */
+    double abs_residual;
+    double setup_ms;     /* hierarchy + coarsest-inverse set-up time */
+    double solve_ms;     /* device time of the Krylov solve */
+    int status;          /* 0 converged, STG_E_* otherwise */
+} stg_stats;
+
+/* Runs the handle's work on a caller-owned CUDA stream (a cudaStream_t passed as void*);
+ * NULL returns to the handle's own stream. Not part of the reference, which uses the
+ * default stream. */
+int stg_set_stream(stg_t* h, void* cuda_stream);
+
+/* Kernel accounting: total kernels this library has launched in the process, and
+ * per-kernel-class CUDA-event timing on the handle's stream (off by default). */
+#define STG_PROF_NCLASS 10
+int64_t stg_kernel_launches(void);
+int stg_profile(stg_t* h, int enable); /* enabling also clears the counters */
+int stg_profile_read(stg_t* h, int cls, int64_t* launches, double* ms, double* bytes);
+const char* stg_profile_name(int cls);
+
+/* Fills *o with the defaults (PLAIN, tol 1e-8, 20 outer, 30 inner, 1e-4). */
+void stg_default_opts(stg_opts* o);
+
+/* Message of the last failure on this thread ("" if none). */
+const char* stg_last_error(void);
+
+/* Library build string (arch, version). */
+const char* stg_version(void);
+
+/* ----------------------------------------------------------------------------
+ * Solver-class API: FluidSteadyState3D / FluidSteadyState
+ * (stoke/FluidSteadyState3D.h:11-38, stoke/FluidSteadyState.h).
+ * -------------------------------------------------------------------------- */
+
+/* FluidSteadyState3D::init(N) (stoke/FluidSteadyState3D.cpp:12-90): builds the level
+ * hierarchy with levels = log2(lowbit N) - 1. dim must be 3 (dim 2 is rejected with
+ * STG_E_UNSUPPORTED in this build). N must be a multiple of 4 and >= 4. */
+int stg_create(int dim, int n, const stg_opts* opts, stg_t** out);
+int stg_destroy(stg_t* h);
+
+/* Number of levels and cells per axis of a level (level 0 = coarsest, as the reference). */
+int stg_levels(const stg_t* h);
+int stg_level_n(const stg_t* h, int level);
+/* LinearMapping::xDoF()/yDoF() of the reference operator at a level (blocked layout size). */
+int64_t stg_level_dof(const stg_t* h, int level);
+
+/* FluidSteadyState3D::init_boundary(cell_vol, cell_fixed, face_vol, face_fixed, closed)
+ * (stoke/FluidSteadyState3D.cpp:92-114) together with FluidEnergy3D::init_boundary
+ * (fluid_topo/FluidEnergy3D.cpp:33-54). face_* point to dim arrays. Returns
+ * STG_E_UNSUPPORTED when the free faces do not share one vol value or a cell is
+ * fixed (this build implements the uniform-coefficient smoother only). */
+int stg_set_boundary(stg_t* h, const double* cell_vol, const int32_t* cell_fixed, const double* const* face_vol,
+                     const int32_t* const* face_fixed, int closed);
+
+/* FluidSteadyState3D::update_penalty(cell_penalty, face_penalty) (:130-150) and
+ * FluidEnergy3D::update_penalty. cell_penalty may be NULL (zero). */
+int stg_set_penalty(stg_t* h, const double* cell_penalty, const double* const* face_penalty);
+
+/* FluidSteadyState3D::update_b(cell_b, face_b) (:116-127). */
+int stg_set_rhs(stg_t* h, const double* cell_b, const double* const* face_b);
+
+/* FluidSteadyState3D::solve() (:152-170): coarse re-discretisation, smoother and
+ * coarsest set-up, then the Krylov solve from a zero initial guess. The results go to
+ * p_out (cells) and vel_out[dim] (faces), the public members p and vel of the
+ * reference; either may be NULL to keep the solution on the device only. */
+int stg_solve(stg_t* h, double* p_out, double* const* vel_out, stg_stats* stats);
+
+/* Copies the last solution to host Field arrays. */
+int stg_get_solution(stg_t* h, double* p_out, double* const* vel_out);
+
+/* ----------------------------------------------------------------------------
+ * Energy API: FluidEnergy3D (fluid_topo/FluidEnergy3D.h:10-44).
+ * The velocity/pressure arguments are host Field arrays; NULL means "use the last
+ * solution held on the device".
+ * -------------------------------------------------------------------------- */
+
+/* compute_energy(vel, p): J = 1/2 x^T E x (fluid_topo/FluidEnergy3D.cpp:94-109). */
+int stg_energy(stg_t* h, const double* p, const double* const* vel, double* J);
+/* compute_gradient_x(vel, p): p_grad, vel_grad = E x (:71-80). */
+int stg_energy_grad_x(stg_t* h, const double* p, const double* const* vel, double* p_grad, double* const* vel_grad);
+/* compute_gradient_q(vel, p): 1/2 x^2 per DOF (:82-91). */
+int stg_energy_grad_q(stg_t* h, const double* p, const double* const* vel, double* cell_q, double* const* face_q);
+
+/* ----------------------------------------------------------------------------
+ * Design-loop API (FluidTopoOpt3D, fluid_topo/FluidTopoOpt3D.cpp:4-223, plus the
+ * density filter and optimality-criteria update of the target problem).
+ * -------------------------------------------------------------------------- */
+
+#define STG_ALPHA_REF 0 /* alpha_os + (alpha_us - alpha_os) s (1+q)/(s+q), s = rho^3 (FluidTopoOpt3D.cpp:110-123) */
+#define STG_ALPHA_BP 1  /* amax * 0.1 (1 - rho)/(0.1 + rho) on the filtered density */
+
+typedef struct stg_alpha {
+    int law;         /* STG_ALPHA_* */
+    double alpha_os; /* REF: solid value (the reference scales 5e2 by 32/N) */
+    double alpha_us; /* REF: fluid value (1e-3) */
+    double q;        /* REF: 0.01 in 3D, 0.014 in 2D */
+    double amax;     /* BP: 1e4 */
+} stg_alpha;
+
+/* Update_Fluid's penalty assembly (FluidTopoOpt3D.cpp:145-159) on the GPU: face
+ * penalty = sum over the adjacent cells of 1/2 alpha(rho_c); installs it as with
+ * stg_set_penalty (cell penalty zero). rho: host cell array, or NULL to use the
+ * device-resident design of stg_filter. */
+int stg_set_density(stg_t* h, const double* rho, const stg_alpha* law);
+
+/* Adjoint sensitivity (FluidTopoOpt3D::Update_Grad, :170-198): solves A lambda = E x
+ * with the same solver, then dJ/drho_c = 1/2 alpha'(.) (ds/drho) sum_{faces of c}
+ * (-u_f lambda_f + 1/2 u_f^2). Needs a prior stg_solve. dJ (host, N^dim) may be NULL
+ * to keep the result on the device. */
+int stg_adjoint_sensitivity(stg_t* h, const stg_alpha* law, double* dJ, stg_stats* stats);
+
+/* Linear hat density filter of radius rmin cells: rho~ = H rho, weights
+ * max(0, rmin - |c_i - c_j|) normalised per row. in/out are host cell arrays; out NULL
+ * keeps the filtered design on the device for stg_set_density. transpose != 0 applies
+ * H^T (sensitivity chain rule). */
+int stg_filter(stg_t* h, double rmin, const double* in, double* out, int transpose);
+
+/* Optimality-criteria update with a bisection on the volume multiplier:
+ * x_new = clamp(x sqrt(max(0,-dc)/(lambda dv)), max(lo, x - move), min(hi, x + move)),
+ * with the volume of the filtered design equal to frac. x, dc host arrays (NULL:
+ * device-resident design / sensitivity); x_new may alias x. */
+int stg_oc_update(stg_t* h, double rmin, const double* x, const double* dc, double frac, double move, double lo, double hi,
+                  double* x_new, double* lambda_out);
+
+/* ----------------------------------------------------------------------------
+ * LinearMapping plugin API (common_cpx/LinearMapping.h:4-14) on raw device pointers in
+ * the reference blocked layout; issued on the handle's stream and synchronised
+ * before return.
+ * -------------------------------------------------------------------------- */
+
+/* StokeFlowMapping3DFixed::applyMapping(Ap, p) at a level (stoke/StokeFlowMapping3D.cu:218-348), FP64. */
+int stg_apply_A_device(stg_t* h, int level, double* d_Ap, const double* d_p);
+/* FluidEnergyGrad3D::applyMapping(Ap, p) (fluid_topo/FluidEnergyGrad3D.cu:201-308), FP64. */
+int stg_apply_E_device(stg_t* h, double* d_Ap, const double* d_p);
+/* MultigridSolve::update() (common_cpx/MultigridSolve.cpp:116-124) together with the coarse
+ * re-discretisation of FluidSteadyState3D::solve (:155). */
+int stg_update(stg_t* h);
+/* MultigridSolve::applyMapping(Ap, p) (common_cpx/MultigridSolve.cpp:108-114): one V-cycle
+ * from a zero guess, FP32 arithmetic inside, FP64 in and out. */
+int stg_vcycle_device(stg_t* h, double* d_out, const double* d_in);
+
+/* Component entry points behind the same interface (one LinearMapping each):
+ *  STG_OP_RESTRICT   StokeFlowDownSample3D (stoke/StokeFlowSubSystem3D.cu:32-52), level = coarse level
+ *  STG_OP_PROLONG    StokeFlowUpSample3D   (:81-101), level = coarse level
+ *  STG_OP_SMOOTH_PRE / STG_OP_SMOOTH_POST  DescentSmoother of StokeLike::GenerateJacobiPreconditioner
+ *                    (stoke/StokeLike.cu:345-372, common_cpx/DescentSmoother.cu:31-47)
+ *  STG_OP_VANKA_RED / STG_OP_VANKA_BLACK   VelDiagPressureFullSmoothing (stoke/StokeLike.cu:220-278)
+ *  STG_OP_COARSE     DirectSolve3D::applyMapping (stoke/StokeLike.cu:421-425), level 0
+ * The smoothing and coarse operators compute in FP32 (coarse: FP64) with FP64 in/out. */
+#define STG_OP_RESTRICT 1
+#define STG_OP_PROLONG 2
+#define STG_OP_SMOOTH_PRE 3
+#define STG_OP_SMOOTH_POST 4
+#define STG_OP_VANKA_RED 5
+#define STG_OP_VANKA_BLACK 6
+#define STG_OP_COARSE 7
+int stg_apply_op_device(stg_t* h, int op, int level, double* d_out, const double* d_in);
+
+/* Coarse descriptor of a level after stg_update (StokeFlowDescriptor3D d_vol,
+ * d_penalty, d_fixed; stoke/StokeFlowDescriptor3D.h:5-30), blocked layout, device pointers. */
+int stg_level_descr_device(stg_t* h, int level, double* d_vol, double* d_penalty, uint8_t* d_fixed);
+
+/* ----------------------------------------------------------------------------
+ * Input generators used by the benchmarks (not part of the reference).
+ * -------------------------------------------------------------------------- */
+
+/* Seeded density: U[0,1) per cell keyed by (seed, Field index) through a SplitMix64
+ * hash, separable Gaussian blur (sigma cells, truncated at ceil(3 sigma), clamp-to-edge)
+ * along axes 0,1,2, clipped to [0,1]. Computed on the GPU; out is a host cell array,
+ * or NULL to keep it as the handle's device-resident design. */
+int stg_density_noise(stg_t* h, uint64_t seed, double sigma, double* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* STOKES_GB300_H */

@@ -1,0 +1,20 @@
+#!/usr/bin/env bash
+# Builds the checker pieces of the reference from its own sources (where they lie under
+# the reference checkout) into oracle/_ref/. Only host-callable code is used: the
+# reference's CUDA kernels need a GPU and its solver classes need the GPU runtime, so
+# the rest of the reference path is not buildable as a CPU checker.
+#   usage: oracle/ref_build.sh [REFERENCE_ROOT]   (default: /root/reference)
+set -euo pipefail
+REF="${1:-/root/reference}"
+HERE="$(cd "$(dirname "$0")" && pwd)"
+OUT="$HERE/_ref"
+CC_DIR="$REF/simplex/src/common_cpx"
+if [ ! -f "$CC_DIR/grid3D.cu" ]; then
+  echo "reference sources not found under $REF; skipping oracle/_ref" >&2
+  exit 0
+fi
+mkdir -p "$OUT"
+NVCC="${NVCC:-nvcc}"
+"$NVCC" -std=c++14 -O2 -Xcompiler -fPIC -shared -gencode arch=compute_103a,code=sm_103a \
+  -I "$CC_DIR" "$HERE/ref_grid3d_wrap.cu" "$CC_DIR/grid3D.cu" -o "$OUT/libref_grid3d.so"
+echo "built $OUT/libref_grid3d.so"

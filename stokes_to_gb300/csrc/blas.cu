@@ -1,0 +1,281 @@
+// Vector kernels of the device-resident Krylov solver: precision conversion, batched
+// dot products and updates for the Arnoldi step, and deterministic reductions (fixed
+// grid, partials summed in a fixed order, so repeated runs are bitwise identical).
+#include "kernels.h"
+
+namespace stg {
+
+namespace {
+
+constexpr int TPB = 256;
+constexpr int RGRID = 1216;  // 8 x 152 SMs: reduction grid
+constexpr int MAXV = 8;      // vectors per multi-dot / multi-axpy pass
+
+__device__ __forceinline__ double warp_sum(double v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+template <int NV>
+__device__ __forceinline__ void block_sums(double (&v)[NV], double* out) {
+    __shared__ double sh[NV][TPB / 32];
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < NV; q++) {
+        double s = warp_sum(v[q]);
+        if (lane == 0) sh[q][wid] = s;
+    }
+    __syncthreads();
+    if (threadIdx.x < NV) {
+        double s = 0;
+        for (int w = 0; w < TPB / 32; w++) s += sh[threadIdx.x][w];
+        out[threadIdx.x] = s;
+    }
+}
+
+__global__ void k_f64_to_f32(long long n4, const double* __restrict__ a, double scale, float* __restrict__ out) {
+    for (long long t = (long long)blockIdx.x * TPB + threadIdx.x; t < 4 * n4; t += (long long)gridDim.x * TPB)
+        out[t] = (float)(a[t] * scale);
+}
+__global__ void k_f32_to_f64(long long n4, const float* __restrict__ a, double* __restrict__ out) {
+    for (long long t = (long long)blockIdx.x * TPB + threadIdx.x; t < 4 * n4; t += (long long)gridDim.x * TPB)
+        out[t] = (double)a[t];
+}
+
+struct Tab {
+    const float4* p[MAXV];
+};
+
+template <int NV>
+__global__ void __launch_bounds__(TPB) k_axpy_multi_32to64(long long n4, Tab z, const double* __restrict__ y, double alpha,
+                                                           d4* __restrict__ x) {
+    double c[NV];
+#pragma unroll
+    for (int q = 0; q < NV; q++) c[q] = alpha * y[q];
+    for (long long t = (long long)blockIdx.x * TPB + threadIdx.x; t < n4; t += (long long)gridDim.x * TPB) {
+        double2* xp = reinterpret_cast<double2*>(x + t);
+        double2 a = xp[0], b = xp[1];
+#pragma unroll
+        for (int q = 0; q < NV; q++) {
+            float4 v = __ldg(z.p[q] + t);
+            a.x += c[q] * v.x;
+            a.y += c[q] * v.y;
+            b.x += c[q] * v.z;
+            b.y += c[q] * v.w;
+        }
+        xp[0] = a;
+        xp[1] = b;
+    }
+}
+
+template <int NV>
+__global__ void __launch_bounds__(TPB) k_multidot32(long long n4, Tab v, const float4* __restrict__ w, double* __restrict__ part) {
+    double acc[NV];
+#pragma unroll
+    for (int q = 0; q < NV; q++) acc[q] = 0;
+    for (long long t = (long long)blockIdx.x * TPB + threadIdx.x; t < n4; t += (long long)gridDim.x * TPB) {
+        float4 a = __ldg(w + t);
+#pragma unroll
+        for (int q = 0; q < NV; q++) {
+            float4 b = __ldg(v.p[q] + t);
+            acc[q] += (double)a.x * b.x + (double)a.y * b.y + (double)a.z * b.z + (double)a.w * b.w;
+        }
+    }
+    block_sums<NV>(acc, part + (long long)blockIdx.x * MAXV);
+}
+
+// w -= sum_q h[q] v_q ; partial ||w||^2 per block (computed after the update)
+template <int NV>
+__global__ void __launch_bounds__(TPB) k_multiaxpy32(long long n4, Tab v, const double* __restrict__ h, float4* __restrict__ w,
+                                                     double* __restrict__ part, int want_norm) {
+    float c[NV];
+#pragma unroll
+    for (int q = 0; q < NV; q++) c[q] = (float)h[q];
+    double acc[1] = {0.0};
+    for (long long t = (long long)blockIdx.x * TPB + threadIdx.x; t < n4; t += (long long)gridDim.x * TPB) {
+        float4 a = w[t];
+#pragma unroll
+        for (int q = 0; q < NV; q++) {
+            float4 b = __ldg(v.p[q] + t);
+            a.x -= c[q] * b.x;
+            a.y -= c[q] * b.y;
+            a.z -= c[q] * b.z;
+            a.w -= c[q] * b.w;
+        }
+        w[t] = a;
+        if (want_norm) acc[0] += (double)a.x * a.x + (double)a.y * a.y + (double)a.z * a.z + (double)a.w * a.w;
+    }
+    if (want_norm) block_sums<1>(acc, part + blockIdx.x);
+}
+
+__global__ void k_scale32(long long n4, const float4* __restrict__ x, const double* __restrict__ nrm2, float4* __restrict__ out) {
+    double s0 = *nrm2;
+    float s = s0 > 0 ? (float)(1.0 / sqrt(s0)) : 0.f;
+    for (long long t = (long long)blockIdx.x * TPB + threadIdx.x; t < n4; t += (long long)gridDim.x * TPB) {
+        float4 a = __ldg(x + t);
+        out[t] = make_float4(a.x * s, a.y * s, a.z * s, a.w * s);
+    }
+}
+
+// Sums column q of a [nparts][stride] partial table in a fixed order.
+__global__ void k_reduce_cols(const double* __restrict__ part, int nparts, int stride, int ncols, double* __restrict__ out) {
+    __shared__ double sh[TPB / 32];
+    for (int q = 0; q < ncols; q++) {
+        double s = 0;
+        for (int p = threadIdx.x; p < nparts; p += TPB) s += part[(long long)p * stride + q];
+        s = warp_sum(s);
+        int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+        if (lane == 0) sh[wid] = s;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double r = 0;
+            for (int w = 0; w < TPB / 32; w++) r += sh[w];
+            out[q] = r;
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(TPB) k_dot64(long long n4, const d4* __restrict__ a, const d4* __restrict__ b,
+                                               double* __restrict__ part) {
+    double acc[1] = {0.0};
+    const double* x = reinterpret_cast<const double*>(a);
+    const double* y = reinterpret_cast<const double*>(b);
+    for (long long t = (long long)blockIdx.x * TPB + threadIdx.x; t < 4 * n4; t += (long long)gridDim.x * TPB)
+        acc[0] += x[t] * y[t];
+    block_sums<1>(acc, part + blockIdx.x);
+}
+
+unsigned rgrid(long long work) {
+    long long g = (work + TPB - 1) / TPB;
+    return (unsigned)(g < 1 ? 1 : (g > RGRID ? RGRID : g));
+}
+
+}  // namespace
+
+int fill_bytes(cudaStream_t st, void* p, size_t bytes) {
+    STG_CK(cudaMemsetAsync(p, 0, bytes, st));
+    return STG_OK;
+}
+
+int f64_to_f32(cudaStream_t st, long long n4, const d4* a, double scale, float4* out) {
+    k_f64_to_f32<<<rgrid(4 * n4), TPB, 0, st>>>(n4, reinterpret_cast<const double*>(a), scale, reinterpret_cast<float*>(out));
+    STG_LAUNCH_CK();
+    return STG_OK;
+}
+
+int f32_to_f64(cudaStream_t st, long long n4, const float4* a, d4* out) {
+    k_f32_to_f64<<<rgrid(4 * n4), TPB, 0, st>>>(n4, reinterpret_cast<const float*>(a), reinterpret_cast<double*>(out));
+    STG_LAUNCH_CK();
+    return STG_OK;
+}
+
+int reduce_parts(cudaStream_t st, const double* parts, int nparts, double* out) {
+    k_reduce_cols<<<1, TPB, 0, st>>>(parts, nparts, 1, 1, out);
+    STG_LAUNCH_CK();
+    return STG_OK;
+}
+
+template <int NV>
+static void launch_axpy(cudaStream_t st, long long n4, const Tab& t, const double* y, double alpha, d4* x) {
+    k_axpy_multi_32to64<NV><<<rgrid(n4), TPB, 0, st>>>(n4, t, y, alpha, x);
+}
+
+int axpy_multi_32to64(cudaStream_t st, long long n4, const float4* const* z, const double* y, int nz, double alpha, d4* x) {
+    for (int j0 = 0; j0 < nz; j0 += MAXV) {
+        int nb = nz - j0 < MAXV ? nz - j0 : MAXV;
+        Tab t{};
+        for (int q = 0; q < nb; q++) t.p[q] = z[j0 + q];
+        switch (nb) {
+            case 1: launch_axpy<1>(st, n4, t, y + j0, alpha, x); break;
+            case 2: launch_axpy<2>(st, n4, t, y + j0, alpha, x); break;
+            case 3: launch_axpy<3>(st, n4, t, y + j0, alpha, x); break;
+            case 4: launch_axpy<4>(st, n4, t, y + j0, alpha, x); break;
+            case 5: launch_axpy<5>(st, n4, t, y + j0, alpha, x); break;
+            case 6: launch_axpy<6>(st, n4, t, y + j0, alpha, x); break;
+            case 7: launch_axpy<7>(st, n4, t, y + j0, alpha, x); break;
+            default: launch_axpy<8>(st, n4, t, y + j0, alpha, x); break;
+        }
+        STG_LAUNCH_CK();
+    }
+    return STG_OK;
+}
+
+template <int NV>
+static void launch_dot(cudaStream_t st, long long n4, const Tab& t, const float4* w, double* part) {
+    k_multidot32<NV><<<rgrid(n4), TPB, 0, st>>>(n4, t, w, part);
+}
+
+int multidot32(cudaStream_t st, long long n4, const float4* const* v, int nv, const float4* w, double* h, double* scratch) {
+    unsigned g = rgrid(n4);
+    for (int j0 = 0; j0 < nv; j0 += MAXV) {
+        int nb = nv - j0 < MAXV ? nv - j0 : MAXV;
+        Tab t{};
+        for (int q = 0; q < nb; q++) t.p[q] = v[j0 + q];
+        switch (nb) {
+            case 1: launch_dot<1>(st, n4, t, w, scratch); break;
+            case 2: launch_dot<2>(st, n4, t, w, scratch); break;
+            case 3: launch_dot<3>(st, n4, t, w, scratch); break;
+            case 4: launch_dot<4>(st, n4, t, w, scratch); break;
+            case 5: launch_dot<5>(st, n4, t, w, scratch); break;
+            case 6: launch_dot<6>(st, n4, t, w, scratch); break;
+            case 7: launch_dot<7>(st, n4, t, w, scratch); break;
+            default: launch_dot<8>(st, n4, t, w, scratch); break;
+        }
+        STG_LAUNCH_CK();
+        k_reduce_cols<<<1, TPB, 0, st>>>(scratch, (int)g, MAXV, nb, h + j0);
+        STG_LAUNCH_CK();
+    }
+    return STG_OK;
+}
+
+template <int NV>
+static void launch_maxpy(cudaStream_t st, long long n4, const Tab& t, const double* h, float4* w, double* part, int want) {
+    k_multiaxpy32<NV><<<rgrid(n4), TPB, 0, st>>>(n4, t, h, w, part, want);
+}
+
+int multiaxpy32_norm(cudaStream_t st, long long n4, const float4* const* v, int nv, const double* h, float4* w, double* nrm2,
+                     double* scratch) {
+    if (nv < 1) {
+        set_error("multiaxpy32_norm: empty basis");
+        return STG_E_INVALID;
+    }
+    unsigned g = rgrid(n4);
+    for (int j0 = 0; j0 < nv; j0 += MAXV) {
+        int nb = nv - j0 < MAXV ? nv - j0 : MAXV;
+        int last = j0 + nb >= nv;
+        Tab t{};
+        for (int q = 0; q < nb; q++) t.p[q] = v[j0 + q];
+        switch (nb) {
+            case 1: launch_maxpy<1>(st, n4, t, h + j0, w, scratch, last); break;
+            case 2: launch_maxpy<2>(st, n4, t, h + j0, w, scratch, last); break;
+            case 3: launch_maxpy<3>(st, n4, t, h + j0, w, scratch, last); break;
+            case 4: launch_maxpy<4>(st, n4, t, h + j0, w, scratch, last); break;
+            case 5: launch_maxpy<5>(st, n4, t, h + j0, w, scratch, last); break;
+            case 6: launch_maxpy<6>(st, n4, t, h + j0, w, scratch, last); break;
+            case 7: launch_maxpy<7>(st, n4, t, h + j0, w, scratch, last); break;
+            default: launch_maxpy<8>(st, n4, t, h + j0, w, scratch, last); break;
+        }
+        STG_LAUNCH_CK();
+    }
+    k_reduce_cols<<<1, TPB, 0, st>>>(scratch, (int)g, 1, 1, nrm2);
+    STG_LAUNCH_CK();
+    return STG_OK;
+}
+
+int scale32(cudaStream_t st, long long n4, float4* x, const double* nrm2, float4* out) {
+    k_scale32<<<rgrid(n4), TPB, 0, st>>>(n4, x, nrm2, out);
+    STG_LAUNCH_CK();
+    return STG_OK;
+}
+
+int dot64(cudaStream_t st, long long n4, const d4* a, const d4* b, double* out, double* scratch) {
+    unsigned g = rgrid(4 * n4);
+    k_dot64<<<g, TPB, 0, st>>>(n4, a, b, scratch);
+    STG_LAUNCH_CK();
+    k_reduce_cols<<<1, TPB, 0, st>>>(scratch, (int)g, 1, 1, out);
+    STG_LAUNCH_CK();
+    return STG_OK;
+}
+
+}  // namespace stg

@@ -1,0 +1,335 @@
+// Coarsest-level direct solve (DirectSolve3D, stoke/StokeLike.cu:374-648) on the GPU.
+//
+// The dense matrix is read off the same nine probes as the reference: two cell probes
+// coloured by (x+y+z+flag) mod 2 and seven face probes coloured by
+// (x + 2y + 3z + magic[d] + flag) mod 7, magic = {2,4,5}; each probe image entry is
+// stored at the column the colouring rule assigns to its row (:431-603). Cell-cell
+// entries are never recorded (as in the reference); with `closed` the pressure block
+// gets +1 everywhere (:605-608). Unknowns that exist only as padding in the reference
+// layout are identity rows decoupled from the rest, so the dense system here keeps the
+// unknowns that exist. It is LU-factorised with partial pivoting (getrf semantics),
+// inverted once per set-up, and applied as a GEMV inside each V-cycle.
+#include <vector>
+
+#include "kernels.h"
+#include "stencil.cuh"
+
+namespace stg {
+
+namespace {
+
+constexpr int TPB = 256;
+
+__global__ void k_probe(Geom g, int kind, int flag, d4* __restrict__ probe) {
+    long long t = (long long)blockIdx.x * TPB + threadIdx.x;
+    if (t >= g.box()) return;
+    int i, j, k;
+    g.box_ijk(t, i, j, k);
+    const int n = g.n;
+    const int magic[3] = {2, 4, 5};
+    double v[4] = {0, 0, 0, 0};
+    if (kind == 0) {
+        if (cell_ok(n, i, j, k)) v[0] = ((i + j + k + flag) % 2 == 0) ? 1.0 : 0.0;
+    } else {
+        for (int d = 0; d < 3; d++)
+            if (face_ok(n, d, i, j, k)) v[d + 1] = ((i + 2 * j + 3 * k + magic[d] + flag) % 7 == 0) ? 1.0 : 0.0;
+    }
+    store4(probe, g.slot(i, j, k), v[0], v[1], v[2], v[3]);
+}
+
+// Scatter one probe image into the dense matrix (column-major, nd x nd).
+__global__ void k_scatter(Geom g, int kind, int flag, int nd, const int* __restrict__ slot_of, const int* __restrict__ comp_of,
+                          const int* __restrict__ dense_of, const d4* __restrict__ image, double* __restrict__ A) {
+    int row = blockIdx.x * TPB + threadIdx.x;
+    if (row >= nd) return;
+    const int n = g.n;
+    int s = slot_of[row], c = comp_of[row];
+    // logical coordinates of the slot
+    int k = s % g.sz - 1, r = s / g.sz;
+    int j = r % g.sy - 1, i = r / g.sy - 1;
+    double val = reinterpret_cast<const double*>(image)[4ll * s + c];
+    int ci = -1, cj = 0, ck = 0, cc = 0;
+    if (kind == 0) {
+        if (c == 0) return;  // cell rows are not read from the cell probes
+        int d = c - 1;
+        ci = i;
+        cj = j;
+        ck = k;
+        if ((i + j + k + flag) % 2 == 1) {
+            if (d == 0) ci--;
+            if (d == 1) cj--;
+            if (d == 2) ck--;
+        }
+        if (!(ci >= 0 && cj >= 0 && ck >= 0 && cell_ok(n, ci, cj, ck))) return;
+        cc = 0;
+    } else {
+        const int magic[3] = {2, 4, 5};
+        ci = i;
+        cj = j;
+        ck = k;
+        if (c == 0) {
+            switch ((i + 2 * j + 3 * k + flag) % 7) {
+                case 1: cc = 2; cj++; break;
+                case 2: cc = 3; break;
+                case 3: cc = 2; break;
+                case 4: cc = 1; ci++; break;
+                case 5: cc = 1; break;
+                case 6: cc = 3; ck++; break;
+                default: return;
+            }
+        } else {
+            int d = c - 1;
+            cc = c;
+            switch ((i + 2 * j + 3 * k + magic[d] + flag) % 7) {
+                case 1: ci--; break;
+                case 2: cj--; break;
+                case 3: ck--; break;
+                case 4: ck++; break;
+                case 5: cj++; break;
+                case 6: ci++; break;
+                default: break;
+            }
+        }
+        // a column outside the existing unknowns is a padding column of the reference layout
+        if (ci < 0 || cj < 0 || ck < 0 || !face_ok(n, cc - 1, ci, cj, ck)) return;
+    }
+    int col = dense_of[4 * g.slot(ci, cj, ck) + cc];
+    if (col < 0) return;
+    A[row + (long long)col * nd] = val;
+}
+
+__global__ void k_closed(int nd, const int* __restrict__ comp_of, double* __restrict__ A) {
+    long long t = (long long)blockIdx.x * TPB + threadIdx.x;
+    if (t >= (long long)nd * nd) return;
+    int row = (int)(t % nd), col = (int)(t / nd);
+    if (comp_of[row] == 0 && comp_of[col] == 0) A[t] += 1.0;
+}
+
+// Single-CTA right-looking LU with partial pivoting (first maximal |a| wins, as idamax).
+constexpr int LU_T = 1024;
+__global__ void __launch_bounds__(LU_T) k_lu(int nd, double* __restrict__ A, int* __restrict__ piv, int* __restrict__ info) {
+    __shared__ double sv[LU_T / 32];
+    __shared__ int si[LU_T / 32];
+    __shared__ int sp;
+    if (threadIdx.x == 0) *info = 0;
+    for (int jc = 0; jc < nd; jc++) {
+        double best = -1.0;
+        int bi = nd;
+        for (int r = jc + threadIdx.x; r < nd; r += LU_T) {
+            double a = fabs(A[r + (long long)jc * nd]);
+            if (a > best || (a == best && r < bi)) {
+                best = a;
+                bi = r;
+            }
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            double ob = __shfl_xor_sync(0xffffffffu, best, o);
+            int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+            if (ob > best || (ob == best && oi < bi)) {
+                best = ob;
+                bi = oi;
+            }
+        }
+        if ((threadIdx.x & 31) == 0) {
+            sv[threadIdx.x >> 5] = best;
+            si[threadIdx.x >> 5] = bi;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double b = -1.0;
+            int ii = nd;
+            for (int w = 0; w < LU_T / 32; w++)
+                if (sv[w] > b || (sv[w] == b && si[w] < ii)) {
+                    b = sv[w];
+                    ii = si[w];
+                }
+            sp = ii;
+            piv[jc] = ii;
+            if (A[ii + (long long)jc * nd] == 0.0 && *info == 0) *info = jc + 1;
+        }
+        __syncthreads();
+        int p = sp;
+        if (p != jc)
+            for (int c = threadIdx.x; c < nd; c += LU_T) {
+                double t0 = A[jc + (long long)c * nd];
+                A[jc + (long long)c * nd] = A[p + (long long)c * nd];
+                A[p + (long long)c * nd] = t0;
+            }
+        __syncthreads();
+        double d = A[jc + (long long)jc * nd];
+        if (d != 0.0) {
+            double inv = 1.0 / d;
+            for (int r = jc + 1 + threadIdx.x; r < nd; r += LU_T) A[r + (long long)jc * nd] *= inv;
+        }
+        __syncthreads();
+        int m = nd - jc - 1;
+        if (d != 0.0)
+            for (long long e = threadIdx.x; e < (long long)m * m; e += LU_T) {
+                int r = jc + 1 + (int)(e % m), c = jc + 1 + (int)(e / m);
+                A[r + (long long)c * nd] -= A[r + (long long)jc * nd] * A[jc + (long long)c * nd];
+            }
+        __syncthreads();
+    }
+}
+
+// Column c of the inverse from the LU factors; written row-major (Ainv[row*nd + c]).
+__global__ void k_inverse(int nd, const double* __restrict__ LU, const int* __restrict__ piv, double* __restrict__ Ainv,
+                          double* __restrict__ work) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nd) return;
+    // x[r] lives at work[r*nd + c]: consecutive threads touch consecutive addresses
+#define XR(r) work[(long long)(r) * nd + c]
+    for (int r = 0; r < nd; r++) XR(r) = (r == c) ? 1.0 : 0.0;
+    for (int r = 0; r < nd; r++)
+        if (piv[r] != r) {
+            double t = XR(r);
+            XR(r) = XR(piv[r]);
+            XR(piv[r]) = t;
+        }
+    for (int q = 0; q < nd; q++) {
+        double xq = XR(q);
+        if (xq != 0.0)
+            for (int r = q + 1; r < nd; r++) XR(r) -= LU[r + (long long)q * nd] * xq;
+    }
+    for (int q = nd - 1; q >= 0; q--) {
+        double dq = LU[q + (long long)q * nd];
+        double xq = dq != 0.0 ? XR(q) / dq : 0.0;
+        XR(q) = xq;
+        if (xq != 0.0)
+            for (int r = 0; r < q; r++) XR(r) -= LU[r + (long long)q * nd] * xq;
+    }
+    for (int r = 0; r < nd; r++) Ainv[(long long)r * nd + c] = XR(r);
+#undef XR
+}
+
+template <class V>
+__device__ __forceinline__ double comp_value(const V* r, int s, int c);
+template <>
+__device__ __forceinline__ double comp_value<float4>(const float4* r, int s, int c) {
+    return (double)reinterpret_cast<const float*>(r)[4ll * s + c];
+}
+template <>
+__device__ __forceinline__ double comp_value<d4>(const d4* r, int s, int c) {
+    return reinterpret_cast<const double*>(r)[4ll * s + c];
+}
+
+template <class V>
+__global__ void k_gather(int nd, const int* __restrict__ slot_of, const int* __restrict__ comp_of, const V* __restrict__ r,
+                         double* __restrict__ rd) {
+    int q = blockIdx.x * TPB + threadIdx.x;
+    if (q < nd) rd[q] = comp_value<V>(r, slot_of[q], comp_of[q]);
+}
+
+// one warp per row: x[row] = sum_c Ainv[row, c] rd[c], scattered into the slot vector
+template <class T>
+__global__ void k_gemv(int nd, const double* __restrict__ Ainv, const double* __restrict__ rd, const int* __restrict__ slot_of,
+                       const int* __restrict__ comp_of, T* __restrict__ x) {
+    int row = (blockIdx.x * TPB + threadIdx.x) >> 5;
+    int lane = threadIdx.x & 31;
+    if (row >= nd) return;
+    double s = 0;
+    for (int c = lane; c < nd; c += 32) s += Ainv[(long long)row * nd + c] * rd[c];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) x[4ll * slot_of[row] + comp_of[row]] = (T)s;
+}
+
+}  // namespace
+
+int dense_init(DenseCoarse& D, const Geom& g) {
+    std::vector<int> slot_of, comp_of, dense_of((size_t)g.nslot * 4, -1);
+    const int n = g.n;
+    for (int i = 0; i <= n; i++)
+        for (int j = 0; j <= n; j++)
+            for (int k = 0; k <= n; k++) {
+                int s = g.slot(i, j, k);
+                for (int c = 0; c < 4; c++) {
+                    bool ok = c == 0 ? cell_ok(n, i, j, k) : face_ok(n, c - 1, i, j, k);
+                    if (!ok) continue;
+                    dense_of[4 * (size_t)s + c] = (int)slot_of.size();
+                    slot_of.push_back(s);
+                    comp_of.push_back(c);
+                }
+            }
+    D.nd = (int)slot_of.size();
+    size_t nd = D.nd;
+    STG_CK(cudaMalloc(&D.slot_of, sizeof(int) * nd));
+    STG_CK(cudaMalloc(&D.comp_of, sizeof(int) * nd));
+    STG_CK(cudaMalloc(&D.dense_of, sizeof(int) * dense_of.size()));
+    STG_CK(cudaMalloc(&D.A, sizeof(double) * nd * nd));
+    STG_CK(cudaMalloc(&D.Ainv, sizeof(double) * nd * nd));
+    STG_CK(cudaMalloc(&D.piv, sizeof(int) * nd));
+    STG_CK(cudaMalloc(&D.info, sizeof(int)));
+    STG_CK(cudaMalloc(&D.probe, sizeof(d4) * g.nslot));
+    STG_CK(cudaMalloc(&D.image, sizeof(d4) * g.nslot));
+    STG_CK(cudaMalloc(&D.work, sizeof(double) * nd * nd));
+    STG_CK(cudaMalloc(&D.rd, sizeof(double) * nd));
+    STG_CK(cudaMemcpy(D.slot_of, slot_of.data(), sizeof(int) * nd, cudaMemcpyHostToDevice));
+    STG_CK(cudaMemcpy(D.comp_of, comp_of.data(), sizeof(int) * nd, cudaMemcpyHostToDevice));
+    STG_CK(cudaMemcpy(D.dense_of, dense_of.data(), sizeof(int) * dense_of.size(), cudaMemcpyHostToDevice));
+    STG_CK(cudaMemset(D.probe, 0, sizeof(d4) * g.nslot));
+    STG_CK(cudaMemset(D.image, 0, sizeof(d4) * g.nslot));
+    return STG_OK;
+}
+
+void dense_free(DenseCoarse& D) {
+    cudaFree(D.slot_of);
+    cudaFree(D.comp_of);
+    cudaFree(D.dense_of);
+    cudaFree(D.A);
+    cudaFree(D.Ainv);
+    cudaFree(D.piv);
+    cudaFree(D.info);
+    cudaFree(D.probe);
+    cudaFree(D.image);
+    cudaFree(D.work);
+    cudaFree(D.rd);
+    D = DenseCoarse();
+}
+
+int dense_setup(cudaStream_t st, DenseCoarse& D, const Geom& g, double vol, const uint8_t* m, const d4* P64, int closed) {
+    const int nd = D.nd;
+    STG_CK(cudaMemsetAsync(D.A, 0, sizeof(double) * nd * nd, st));
+    for (int kind = 0; kind < 2; kind++) {
+        int nflags = kind == 0 ? 2 : 7;
+        for (int f = 0; f < nflags; f++) {
+            k_probe<<<grid_for(g.box(), TPB), TPB, 0, st>>>(g, kind, f, D.probe);
+            STG_LAUNCH_CK();
+            STG_TRY(op64(st, g, vol, D.probe, m, P64, nullptr, D.image, 0, nullptr, nullptr));
+            k_scatter<<<grid_for(nd, TPB), TPB, 0, st>>>(g, kind, f, nd, D.slot_of, D.comp_of, D.dense_of, D.image, D.A);
+            STG_LAUNCH_CK();
+        }
+    }
+    if (closed) {
+        k_closed<<<grid_for((long long)nd * nd, TPB), TPB, 0, st>>>(nd, D.comp_of, D.A);
+        STG_LAUNCH_CK();
+    }
+    k_lu<<<1, LU_T, 0, st>>>(nd, D.A, D.piv, D.info);
+    STG_LAUNCH_CK();
+    k_inverse<<<grid_for(nd, 64), 64, 0, st>>>(nd, D.A, D.piv, D.Ainv, D.work);
+    STG_LAUNCH_CK();
+    return STG_OK;
+}
+
+int dense_apply32(cudaStream_t st, const DenseCoarse& D, const Geom& g, const float4* r, float4* x) {
+    double* rd = D.rd;
+    k_gather<float4><<<grid_for(D.nd, TPB), TPB, 0, st>>>(D.nd, D.slot_of, D.comp_of, r, rd);
+    STG_LAUNCH_CK();
+    STG_CK(cudaMemsetAsync(x, 0, sizeof(float4) * g.nslot, st));
+    k_gemv<float><<<grid_for(32ll * D.nd, TPB), TPB, 0, st>>>(D.nd, D.Ainv, rd, D.slot_of, D.comp_of,
+                                                              reinterpret_cast<float*>(x));
+    STG_LAUNCH_CK();
+    return STG_OK;
+}
+
+int dense_apply64(cudaStream_t st, const DenseCoarse& D, const Geom& g, const d4* r, d4* x) {
+    double* rd = D.rd;
+    k_gather<d4><<<grid_for(D.nd, TPB), TPB, 0, st>>>(D.nd, D.slot_of, D.comp_of, r, rd);
+    STG_LAUNCH_CK();
+    STG_CK(cudaMemsetAsync(x, 0, sizeof(d4) * g.nslot, st));
+    k_gemv<double><<<grid_for(32ll * D.nd, TPB), TPB, 0, st>>>(D.nd, D.Ainv, rd, D.slot_of, D.comp_of,
+                                                                reinterpret_cast<double*>(x));
+    STG_LAUNCH_CK();
+    return STG_OK;
+}
+
+}  // namespace stg

@@ -1,0 +1,109 @@
+// Host-side launchers of the grid kernels (kernels.cu, dense.cu, blas.cu, topo.cu).
+#pragma once
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include "internal.cuh"
+
+namespace stg {
+
+// ---------------------------------------------------------------- operators (kernels.cu)
+// mode: 0 out = A x, 1 out = b - A x, 2 out = E x. If part != nullptr, each block writes
+// its partial sum of out.out (mode 1) or x.out (mode 2) to part[blockIdx.x] (FP64).
+int op64(cudaStream_t st, const Geom& g, double vol, const d4* x, const uint8_t* m, const d4* P, const d4* b, d4* out,
+         int mode, double* part, int* nblocks_out);
+// rr = r - A x in FP32 (x == nullptr means x = 0, so rr = r)
+int resid32(cudaStream_t st, const Geom& g, float vol, const float4* r, const float4* x, const uint8_t* m, const float4* P,
+            float4* rr);
+// y = A x in FP32
+int apply32(cudaStream_t st, const Geom& g, float vol, const float4* x, const uint8_t* m, const float4* P, float4* y);
+// One colour of the box-Vanka block-Jacobi step: xout = xin + SHATTER(B^-1 GATHER(rr)).
+// xin == nullptr means xin = 0.
+int vanka32(cudaStream_t st, const Geom& g, float vol, const float4* rr, const float4* xin, float4* xout, const uint8_t* m,
+            const float4* P, int flag);
+// rc = R (rf - A xf) with R the 8-child sum masked by the coarse mask (xf == nullptr: rc = R rf).
+int restrict_resid32(cudaStream_t st, const Geom& gc, const Geom& gf, float volf, const float4* rf, const float4* xf,
+                     const uint8_t* mf, const float4* Pf, const uint8_t* mc, float4* rc);
+// xf += fix_f (injection of xc)
+int prolong_add32(cudaStream_t st, const Geom& gf, const Geom& gc, const float4* xc, const uint8_t* mf, float4* xf);
+// same with BF16-stored coarse correction
+int prolong_add_bf16(cudaStream_t st, const Geom& gf, const Geom& gc, const __nv_bfloat16* xc, const uint8_t* mf, float4* xf);
+int to_bf16(cudaStream_t st, const Geom& g, const float4* x, __nv_bfloat16* y);
+// coarse descriptor from the fine one (updateSubSystem + finish)
+int coarsen(cudaStream_t st, const Geom& gc, const Geom& gf, const uint8_t* mf, const d4* Pf, uint8_t* mc, d4* Pc64,
+            float4* Pc32);
+// FP64 restriction / prolongation (component adapters): rc = fix_c R rf ; xf = fix_f P xc
+int restrict64(cudaStream_t st, const Geom& gc, const Geom& gf, const d4* rf, const uint8_t* mc, d4* rc);
+int prolong64(cudaStream_t st, const Geom& gf, const Geom& gc, const d4* xc, const uint8_t* mf, d4* xf);
+
+// ---------------------------------------------------------------- layout (kernels.cu)
+// Field-order device arrays (cell, face0..2) <-> slots. Any pointer may be null (zeros).
+int field_to_slots64(cudaStream_t st, const Geom& g, const double* cell, const double* f0, const double* f1, const double* f2,
+                     d4* out);
+int slots_to_field64(cudaStream_t st, const Geom& g, const d4* in, double* cell, double* f0, double* f1, double* f2);
+// mask = fixed flags (Field order int32, null = free) | not-present bits
+int mask_from_field(cudaStream_t st, const Geom& g, const int* cell, const int* f0, const int* f1, const int* f2, uint8_t* m);
+// penalty: P64 = fields zeroed on fixed; P32 = float(P64)
+int penalty_from_field(cudaStream_t st, const Geom& g, const double* cell, const double* f0, const double* f1, const double* f2,
+                       const uint8_t* m, d4* P64, float4* P32);
+// reference blocked layout <-> slots. pad_identity: blocked padding entries copy in->out.
+int blocked_to_slots64(cudaStream_t st, const Geom& g, const double* in, d4* out);
+int slots_to_blocked64(cudaStream_t st, const Geom& g, const d4* in, double* out, const double* pad_src);
+int mask_to_blocked(cudaStream_t st, const Geom& g, const uint8_t* m, uint8_t* out);
+// descriptor vol per unknown: cell_vol on free cells, vol on free faces, 0 on fixed / absent
+int vol_slots(cudaStream_t st, const Geom& g, const uint8_t* m, double cell_vol, double vol, d4* out);
+// out = 1/2 x^2 per unknown
+int half_square64(cudaStream_t st, long long n4, const d4* x, d4* out);
+
+// ---------------------------------------------------------------- vectors (blas.cu)
+int fill_bytes(cudaStream_t st, void* p, size_t bytes);
+int f64_to_f32(cudaStream_t st, long long n4, const d4* a, double scale, float4* out);
+int f32_to_f64(cudaStream_t st, long long n4, const float4* a, d4* out);
+// x64 += alpha * sum_j y[j] z[j]  (z FP32 vectors), y on device (nz entries)
+int axpy_multi_32to64(cudaStream_t st, long long n4, const float4* const* z, const double* y, int nz, double alpha, d4* x);
+// h[j] = <v_j, w> for j < nv  (FP64 accumulation), written to hpart then reduced into h
+int multidot32(cudaStream_t st, long long n4, const float4* const* v, int nv, const float4* w, double* h, double* scratch);
+// w -= sum_j h[j] v_j ; then returns ||w||^2 into nrm2 (device)
+int multiaxpy32_norm(cudaStream_t st, long long n4, const float4* const* v, int nv, const double* h, float4* w, double* nrm2,
+                     double* scratch);
+// x *= s (s on device, s = 1/sqrt(*nrm2) if invsqrt)
+int scale32(cudaStream_t st, long long n4, float4* x, const double* nrm2, float4* out);
+// deterministic sum of nparts partials -> *out
+int reduce_parts(cudaStream_t st, const double* parts, int nparts, double* out);
+int dot64(cudaStream_t st, long long n4, const d4* a, const d4* b, double* out, double* scratch);
+
+// ---------------------------------------------------------------- coarsest dense solve (dense.cu)
+struct DenseCoarse {
+    int nd = 0;                // number of unknowns present at the coarsest level
+    int* slot_of = nullptr;    // dense index -> slot
+    int* comp_of = nullptr;    // dense index -> 0 p, 1 u, 2 v, 3 w
+    int* dense_of = nullptr;   // slot*4+comp -> dense index or -1
+    double* A = nullptr;       // nd x nd column-major; LU then inverse
+    double* Ainv = nullptr;
+    int* piv = nullptr;
+    int* info = nullptr;
+    d4* probe = nullptr;       // probe vector and its image (slots)
+    d4* image = nullptr;
+    double* work = nullptr;    // nd x nd inversion work area
+    double* rd = nullptr;      // gathered right-hand side (nd)
+};
+int dense_init(DenseCoarse& D, const Geom& g);
+void dense_free(DenseCoarse& D);
+// DirectSolve3D::update: probe assembly + (closed) all-ones p-block + inversion
+int dense_setup(cudaStream_t st, DenseCoarse& D, const Geom& g, double vol, const uint8_t* m, const d4* P64, int closed);
+// x = A^-1 r on the slots (FP32 in/out, FP64 inside)
+int dense_apply32(cudaStream_t st, const DenseCoarse& D, const Geom& g, const float4* r, float4* x);
+int dense_apply64(cudaStream_t st, const DenseCoarse& D, const Geom& g, const d4* r, d4* x);
+
+// ---------------------------------------------------------------- design loop (topo.cu)
+int face_penalty_from_density(cudaStream_t st, const Geom& g, const double* rho, const stg_alpha& law, const uint8_t* m,
+                              d4* P64, float4* P32);
+int sensitivity(cudaStream_t st, const Geom& g, const double* rho, const stg_alpha& law, const d4* x, const d4* lam,
+                double* grad);
+int density_filter(cudaStream_t st, int n, double rmin, const double* in, double* out, int transpose);
+int filter_volume_weights(cudaStream_t st, int n, double rmin, double* vw);
+int oc_volume(cudaStream_t st, int ncell, const double* x, const double* dc, const double* vw, double lam, double move,
+              double lo, double hi, double* xnew, double* parts, int* nparts);
+int density_noise(cudaStream_t st, int n, uint64_t seed, const double* w, int R, double* out, double* tmp);
+
+}  // namespace stg

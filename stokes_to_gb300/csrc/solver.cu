@@ -1,0 +1,990 @@
+// Host orchestration of libstokes_gb300 and its C ABI (include/stokes_gb300.h).
+//
+// Solve = FluidSteadyState3D::solve (stoke/FluidSteadyState3D.cpp:152-170) re-designed
+// for one GB300: the coarse re-discretisation, the smoother blocks and the coarsest
+// inverse are rebuilt on the device; the reference's host GMRES with the V-cycle as
+// left preconditioner (common_cpx/GMRES.cpp:20-110) becomes a device-resident FP64
+// defect-correction loop whose correction equations are solved by right-preconditioned
+// FGMRES in FP32 with the same V-cycle (common_cpx/MultigridSolve.cpp:73-114) as
+// preconditioner. Every vector stays in HBM; the host only sees the Hessenberg scalars.
+#include <cuda_bf16.h>
+
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "kernels.h"
+
+namespace stg {
+
+static thread_local char g_err[512] = "";
+static std::atomic<long long> g_launches{0};
+
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+void set_error(const char* fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+}
+
+int cuda_fail(cudaError_t e, const char* what, const char* file, int line) {
+    const char* base = strrchr(file, '/');
+    set_error("%s:%d %s: %s", base ? base + 1 : file, line, what, cudaGetErrorString(e));
+    return e == cudaErrorMemoryAllocation ? STG_E_NOMEM : STG_E_CUDA;
+}
+
+struct Level {
+    Geom g;
+    double vol = 1.0;       // vol of the free faces
+    double cell_vol = 1.0;  // cell vol (reported by the descriptor adapter only)
+    uint8_t* m = nullptr;
+    d4* P64 = nullptr;
+    float4* P32 = nullptr;
+    float4 *r = nullptr, *xa = nullptr, *xb = nullptr, *rr = nullptr;
+    int cur = 0;  // which of xa/xb holds the current correction
+    __nv_bfloat16* xbf = nullptr;
+    d4 *t0 = nullptr, *t1 = nullptr;  // FP64 adapter buffers (allocated on first use)
+    float4* x() { return cur ? xb : xa; }
+    float4* other() { return cur ? xa : xb; }
+};
+
+}  // namespace stg
+
+using namespace stg;
+
+// Per-kernel-class CUDA-event timing on the handle's stream.
+struct Prof {
+    bool on = false;
+    std::vector<cudaEvent_t> pool;
+    size_t used = 0;
+    struct Pending {
+        int cls;
+        size_t ev;
+        double bytes;
+    };
+    std::vector<Pending> pend;
+    long long launches[STG_PROF_NCLASS] = {};
+    double ms[STG_PROF_NCLASS] = {};
+    double bytes[STG_PROF_NCLASS] = {};
+};
+
+struct stg_ctx {
+    int dim = 3, n = 0, L = 0;
+    Prof prof;
+    cudaStream_t own_st = nullptr;
+    stg_opts opts{};
+    cudaStream_t st = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    std::vector<Level> lv;  // lv[0] coarsest ... lv[L-1] finest (reference order)
+    DenseCoarse dense;
+    bool closed = true, have_boundary = false, have_penalty = false, have_rhs = false, updated = false, have_solution = false;
+    // fine-level FP64
+    d4 *b64 = nullptr, *x64 = nullptr, *r64 = nullptr, *t64 = nullptr, *lam64 = nullptr;
+    // Krylov (FP32)
+    int m = 0;
+    std::vector<float4*> V, Z;
+    float4* w = nullptr;
+    double *dscr = nullptr, *dh = nullptr, *dnrm = nullptr, *dy = nullptr;
+    // host-order staging (cells + 3 face arrays)
+    double* stage = nullptr;
+    int* istage = nullptr;
+    size_t ncell = 0, nface = 0;
+    // design loop
+    double *d_design = nullptr, *d_phys = nullptr, *d_sens = nullptr, *d_sens_design = nullptr, *d_vw = nullptr,
+           *d_tmp = nullptr, *d_gauss = nullptr, *d_parts = nullptr;
+    double vw_rmin = -1.0;
+    const double* phys_used = nullptr;
+};
+
+namespace {
+
+Level& fine(stg_t* h) { return h->lv[h->L - 1]; }
+
+int prof_flush(stg_t* h) {
+    Prof& P = h->prof;
+    if (P.pend.empty()) return STG_OK;
+    STG_CK(cudaEventSynchronize(P.pool[P.used - 1]));
+    for (auto& q : P.pend) {
+        float ms = 0;
+        STG_CK(cudaEventElapsedTime(&ms, P.pool[q.ev], P.pool[q.ev + 1]));
+        P.ms[q.cls] += ms;
+        P.bytes[q.cls] += q.bytes;
+        P.launches[q.cls]++;
+    }
+    P.pend.clear();
+    P.used = 0;
+    return STG_OK;
+}
+
+int prof_begin(stg_t* h, size_t* ev) {
+    Prof& P = h->prof;
+    if (!P.on) return STG_OK;
+    if (P.used + 2 > P.pool.size()) STG_TRY(prof_flush(h));
+    while (P.pool.size() < P.used + 2) {
+        cudaEvent_t e;
+        STG_CK(cudaEventCreate(&e));
+        P.pool.push_back(e);
+    }
+    *ev = P.used;
+    STG_CK(cudaEventRecord(P.pool[P.used++], h->st));
+    return STG_OK;
+}
+
+int prof_end(stg_t* h, int cls, double bytes, size_t ev) {
+    Prof& P = h->prof;
+    if (!P.on) return STG_OK;
+    STG_CK(cudaEventRecord(P.pool[P.used++], h->st));
+    P.pend.push_back({cls, ev, bytes});
+    if (P.used >= 8192) STG_TRY(prof_flush(h));
+    return STG_OK;
+}
+
+#define PROF(h, cls, bytes, expr)                     \
+    do {                                              \
+        size_t ev_ = 0;                               \
+        STG_TRY(prof_begin((h), &ev_));               \
+        STG_TRY(expr);                                \
+        STG_TRY(prof_end((h), (cls), (bytes), ev_));  \
+    } while (0)
+
+int level_count(int n) {
+    int low = n & -n;
+    int l = (int)std::lround(std::log2((double)low)) - 1;
+    return l < 1 ? 1 : l;
+}
+
+template <class T>
+int dalloc(T** p, size_t count) {
+    cudaError_t e = cudaMalloc((void**)p, sizeof(T) * (count ? count : 1));
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc", __FILE__, __LINE__);
+    e = cudaMemset(*p, 0, sizeof(T) * (count ? count : 1));
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemset", __FILE__, __LINE__);
+    return STG_OK;
+}
+
+double* stage_cell(stg_t* h) { return h->stage; }
+double* stage_face(stg_t* h, int d) { return h->stage + h->ncell + (size_t)d * h->nface; }
+
+int upload_fields(stg_t* h, const double* cell, const double* const* faces, const double** dc, const double** df) {
+    if (cell) STG_CK(cudaMemcpyAsync(stage_cell(h), cell, sizeof(double) * h->ncell, cudaMemcpyHostToDevice, h->st));
+    *dc = cell ? stage_cell(h) : nullptr;
+    for (int d = 0; d < 3; d++) {
+        const double* f = faces ? faces[d] : nullptr;
+        if (f) STG_CK(cudaMemcpyAsync(stage_face(h, d), f, sizeof(double) * h->nface, cudaMemcpyHostToDevice, h->st));
+        df[d] = f ? stage_face(h, d) : nullptr;
+    }
+    return STG_OK;
+}
+
+int download_fields(stg_t* h, const d4* src, double* cell, double* const* faces) {
+    STG_TRY(slots_to_field64(h->st, fine(h).g, src, stage_cell(h), stage_face(h, 0), stage_face(h, 1), stage_face(h, 2)));
+    if (cell) STG_CK(cudaMemcpyAsync(cell, stage_cell(h), sizeof(double) * h->ncell, cudaMemcpyDeviceToHost, h->st));
+    for (int d = 0; d < 3; d++)
+        if (faces && faces[d])
+            STG_CK(cudaMemcpyAsync(faces[d], stage_face(h, d), sizeof(double) * h->nface, cudaMemcpyDeviceToHost, h->st));
+    STG_CK(cudaStreamSynchronize(h->st));
+    return STG_OK;
+}
+
+// ---------------------------------------------------------------- hierarchy set-up
+// FluidSteadyState3D::solve set-up (stoke/FluidSteadyState3D.cpp:155-156): coarse
+// descriptors (updateSubSystem) and the coarsest inverse (DirectSolve3D::update). The
+// smoother blocks need no set-up: the kernels form them from the level coefficients.
+int update(stg_t* h) {
+    if (!h->have_boundary || !h->have_penalty) {
+        set_error("boundary and penalty must be set before the solver set-up");
+        return STG_E_INVALID;
+    }
+    for (int i = h->L - 2; i >= 0; i--) {
+        Level &c = h->lv[i], &f = h->lv[i + 1];
+        PROF(h, 8, 0.0, coarsen(h->st, c.g, f.g, f.m, f.P64, c.m, c.P64, c.P32));
+        c.vol = 4.0 * f.vol;
+        c.cell_vol = 8.0 * f.cell_vol;
+    }
+    PROF(h, 8, 0.0, dense_setup(h->st, h->dense, h->lv[0].g, h->lv[0].vol, h->lv[0].m, h->lv[0].P64, h->closed ? 1 : 0));
+    h->updated = true;
+    return STG_OK;
+}
+
+// ---------------------------------------------------------------- V-cycle (FP32)
+// Smoother of StokeLike::GenerateJacobiPreconditioner(grid, A, 2) (stoke/StokeLike.cu:345-372):
+// DescentSmoother({red, black}, {2, 2}) before the coarse correction and {black, red} after
+// (common_cpx/DescentSmoother.cu:31-47), written in correction form x <- x + P_c(r - A x).
+int sweep(stg_t* h, Level& L, const float4* r, int flag, bool first) {
+    float vol = (float)L.vol;
+    if (first) {
+        // x = 0: the residual is r itself
+        PROF(h, 1, 49.0 * L.g.box(), vanka32(h->st, L.g, vol, r, nullptr, L.x(), L.m, L.P32, flag));
+        return STG_OK;
+    }
+    PROF(h, 0, 65.0 * L.g.box(), resid32(h->st, L.g, vol, r, L.x(), L.m, L.P32, L.rr));
+    PROF(h, 1, 65.0 * L.g.box(), vanka32(h->st, L.g, vol, L.rr, L.x(), L.other(), L.m, L.P32, flag));
+    L.cur ^= 1;
+    return STG_OK;
+}
+
+int smooth(stg_t* h, Level& L, const float4* r, bool post, bool x_is_zero) {
+    const int flags_pre[4] = {0, 0, 1, 1}, flags_post[4] = {1, 1, 0, 0};
+    const int* f = post ? flags_post : flags_pre;
+    for (int s = 0; s < 4; s++) STG_TRY(sweep(h, L, r, f[s], s == 0 && x_is_zero));
+    return STG_OK;
+}
+
+// MultigridSolve::Vcycle (common_cpx/MultigridSolve.cpp:73-106) from a zero guess; the
+// finest right-hand side is `rhs`, the result is left in fine(h).x().
+int vcycle(stg_t* h, const float4* rhs) {
+    const bool mixed = h->opts.method == STG_METHOD_MIXED;
+    const int L = h->L;
+    for (int i = L - 1; i >= 1; i--) {
+        Level& F = h->lv[i];
+        const float4* r = (i == L - 1) ? rhs : F.r;
+        F.cur = 0;
+        STG_TRY(smooth(h, F, r, false, true));
+        Level& C = h->lv[i - 1];
+        PROF(h, 2, 49.0 * F.g.box() + 17.0 * C.g.box(), restrict_resid32(h->st, C.g, F.g, (float)F.vol, r, F.x(), F.m, F.P32, C.m, C.r));
+    }
+    Level& C0 = h->lv[0];
+    C0.cur = 0;
+    PROF(h, 7, 0.0, dense_apply32(h->st, h->dense, C0.g, L == 1 ? rhs : C0.r, C0.x()));
+    for (int i = 1; i < L; i++) {
+        Level& F = h->lv[i];
+        Level& C = h->lv[i - 1];
+        const float4* r = (i == L - 1) ? rhs : F.r;
+        if (mixed) {
+            PROF(h, 3, 24.0 * C.g.box(), to_bf16(h->st, C.g, C.x(), C.xbf));
+            PROF(h, 3, 8.0 * C.g.box() + 33.0 * F.g.box(), prolong_add_bf16(h->st, F.g, C.g, C.xbf, F.m, F.x()));
+        } else {
+            PROF(h, 3, 16.0 * C.g.box() + 33.0 * F.g.box(), prolong_add32(h->st, F.g, C.g, C.x(), F.m, F.x()));
+        }
+        STG_TRY(smooth(h, F, r, true, false));
+    }
+    return STG_OK;
+}
+
+// ---------------------------------------------------------------- FP64 refinement + FGMRES
+int residual64(stg_t* h, const d4* b, const d4* x, d4* r, double* nrm2_host) {
+    Level& F = fine(h);
+    int nb = 0;
+    PROF(h, 5, 129.0 * F.g.box(), op64(h->st, F.g, F.vol, x, F.m, F.P64, b, r, 1, h->d_parts, &nb));
+    STG_TRY(reduce_parts(h->st, h->d_parts, nb, h->dnrm));
+    STG_CK(cudaMemcpyAsync(nrm2_host, h->dnrm, sizeof(double), cudaMemcpyDeviceToHost, h->st));
+    STG_CK(cudaStreamSynchronize(h->st));
+    return STG_OK;
+}
+
+int solve_core(stg_t* h, const d4* b, d4* x, stg_stats* stats) {
+    Level& F = fine(h);
+    const long long n4 = F.g.nslot;
+    stg_stats S{};
+    if (!h->updated) {
+        auto t0 = std::chrono::steady_clock::now();
+        STG_TRY(update(h));
+        STG_CK(cudaStreamSynchronize(h->st));
+        S.setup_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    }
+    STG_CK(cudaEventRecord(h->e0, h->st));
+    STG_CK(cudaMemsetAsync(x, 0, sizeof(d4) * n4, h->st));
+    double bn2 = 0;
+    STG_TRY(dot64(h->st, n4, b, b, h->dnrm, h->dscr));
+    STG_CK(cudaMemcpyAsync(&bn2, h->dnrm, sizeof(double), cudaMemcpyDeviceToHost, h->st));
+    STG_CK(cudaStreamSynchronize(h->st));
+    const double bn = std::sqrt(bn2);
+    const int m = h->m;
+    std::vector<double> H((size_t)(m + 1) * m), cs(m), sn(m), g(m + 1), y(m), hcol(m + 2);
+    double rel = 0, rn = 0;
+    int status = STG_E_NOT_CONVERGED;
+    for (int outer = 0; outer <= h->opts.max_outer; outer++) {
+        double rn2 = 0;
+        STG_TRY(residual64(h, b, x, h->r64, &rn2));
+        rn = std::sqrt(rn2);
+        rel = bn > 0 ? rn / bn : 0.0;
+        if (!std::isfinite(rn)) {
+            status = STG_E_NONFINITE;
+            set_error("non-finite FP64 residual at refinement step %d", outer);
+            break;
+        }
+        if (h->opts.verbose) fprintf(stderr, "[stg] outer %d  ||b-Ax||/||b|| = %.3e\n", outer, rel);
+        if (rel <= h->opts.tol || rn == 0.0) {
+            status = STG_OK;
+            break;
+        }
+        if (outer == h->opts.max_outer) break;
+        S.outer_iters++;
+        // v0 = r / ||r|| in FP32
+        PROF(h, 6, 48.0 * n4, f64_to_f32(h->st, n4, h->r64, 1.0 / rn, h->V[0]));
+        double beta = 1.0;
+        std::fill(g.begin(), g.end(), 0.0);
+        g[0] = beta;
+        int k = 0;
+        for (int j = 0; j < m; j++) {
+            STG_TRY(vcycle(h, h->V[j]));
+            STG_CK(cudaMemcpyAsync(h->Z[j], F.x(), sizeof(float4) * n4, cudaMemcpyDeviceToDevice, h->st));
+            PROF(h, 4, 49.0 * F.g.box(), apply32(h->st, F.g, (float)F.vol, h->Z[j], F.m, F.P32, h->w));
+            PROF(h, 6, 16.0 * (j + 2) * n4, multidot32(h->st, n4, h->V.data(), j + 1, h->w, h->dh, h->dscr));
+            PROF(h, 6, 16.0 * (j + 3) * n4, multiaxpy32_norm(h->st, n4, h->V.data(), j + 1, h->dh, h->w, h->dnrm, h->dscr));
+            // second classical Gram-Schmidt pass (CGS2): keeps the FP32 basis orthogonal
+            PROF(h, 6, 16.0 * (j + 2) * n4, multidot32(h->st, n4, h->V.data(), j + 1, h->w, h->dh + m + 2, h->dscr));
+            PROF(h, 6, 16.0 * (j + 3) * n4, multiaxpy32_norm(h->st, n4, h->V.data(), j + 1, h->dh + m + 2, h->w, h->dnrm, h->dscr));
+            std::vector<double> h1(j + 1), h2(j + 1);
+            double nw2 = 0;
+            STG_CK(cudaMemcpyAsync(h1.data(), h->dh, sizeof(double) * (j + 1), cudaMemcpyDeviceToHost, h->st));
+            STG_CK(cudaMemcpyAsync(h2.data(), h->dh + m + 2, sizeof(double) * (j + 1), cudaMemcpyDeviceToHost, h->st));
+            STG_CK(cudaMemcpyAsync(&nw2, h->dnrm, sizeof(double), cudaMemcpyDeviceToHost, h->st));
+            STG_CK(cudaStreamSynchronize(h->st));
+            S.inner_iters++;
+            double hn = std::sqrt(nw2);
+            for (int q = 0; q <= j; q++) hcol[q] = h1[q] + h2[q];
+            hcol[j + 1] = hn;
+            if (!std::isfinite(hn)) {
+                status = STG_E_NONFINITE;
+                set_error("non-finite Arnoldi norm");
+                break;
+            }
+            if (hn > 0) PROF(h, 6, 32.0 * n4, scale32(h->st, n4, h->w, h->dnrm, h->V[j + 1]));
+            // Givens rotations on the new Hessenberg column
+            for (int q = 0; q < j; q++) {
+                double a = hcol[q], c = hcol[q + 1];
+                hcol[q] = cs[q] * a + sn[q] * c;
+                hcol[q + 1] = -sn[q] * a + cs[q] * c;
+            }
+            double a = hcol[j], c = hcol[j + 1];
+            double den = std::hypot(a, c);
+            cs[j] = den > 0 ? a / den : 1.0;
+            sn[j] = den > 0 ? c / den : 0.0;
+            hcol[j] = den;
+            hcol[j + 1] = 0.0;
+            for (int q = 0; q <= j; q++) H[q + (size_t)j * (m + 1)] = hcol[q];
+            g[j + 1] = -sn[j] * g[j];
+            g[j] = cs[j] * g[j];
+            k = j + 1;
+            double est = std::fabs(g[j + 1]);
+            if (h->opts.verbose > 1) fprintf(stderr, "[stg]   inner %d  est %.3e\n", j, est);
+            if (est <= h->opts.inner_tol * beta || hn == 0.0) break;
+        }
+        if (status == STG_E_NONFINITE) break;
+        for (int q = k - 1; q >= 0; q--) {
+            double s = g[q];
+            for (int c = q + 1; c < k; c++) s -= H[q + (size_t)c * (m + 1)] * y[c];
+            double d = H[q + (size_t)q * (m + 1)];
+            y[q] = d != 0 ? s / d : 0.0;
+        }
+        STG_CK(cudaMemcpyAsync(h->dy, y.data(), sizeof(double) * k, cudaMemcpyHostToDevice, h->st));
+        PROF(h, 6, (16.0 * k + 64.0) * n4, axpy_multi_32to64(h->st, n4, h->Z.data(), h->dy, k, rn, x));
+    }
+    STG_CK(cudaEventRecord(h->e1, h->st));
+    STG_CK(cudaEventSynchronize(h->e1));
+    float ms = 0;
+    STG_CK(cudaEventElapsedTime(&ms, h->e0, h->e1));
+    S.solve_ms = ms;
+    STG_TRY(prof_flush(h));
+    S.rel_residual = rel;
+    S.abs_residual = rn;
+    S.status = status;
+    if (stats) *stats = S;
+    if (status == STG_E_NOT_CONVERGED) set_error("tolerance %.1e not reached (%.3e after %d steps)", h->opts.tol, rel, S.outer_iters);
+    return status;
+}
+
+int ensure_adapter(Level& L) {
+    if (!L.t0) STG_TRY(dalloc(&L.t0, L.g.nslot));
+    if (!L.t1) STG_TRY(dalloc(&L.t1, L.g.nslot));
+    return STG_OK;
+}
+
+int check_handle(const stg_t* h) {
+    if (!h) {
+        set_error("null handle");
+        return STG_E_INVALID;
+    }
+    return STG_OK;
+}
+
+}  // namespace
+
+// ====================================================================== C ABI
+extern "C" {
+
+void stg_default_opts(stg_opts* o) {
+    if (!o) return;
+    o->method = STG_METHOD_PLAIN;
+    o->tol = 1e-8;
+    o->max_outer = 20;
+    o->inner_max = 30;
+    o->inner_tol = 1e-4;
+    o->verbose = 0;
+}
+
+const char* stg_last_error(void) { return g_err; }
+
+int stg_set_stream(stg_t* h, void* cuda_stream) {
+    STG_TRY(check_handle(h));
+    STG_CK(cudaStreamSynchronize(h->st));
+    h->st = cuda_stream ? (cudaStream_t)cuda_stream : h->own_st;
+    return STG_OK;
+}
+
+int64_t stg_kernel_launches(void) { return g_launches.load(); }
+
+int stg_profile(stg_t* h, int enable) {
+    STG_TRY(check_handle(h));
+    STG_TRY(prof_flush(h));
+    Prof& P = h->prof;
+    P.on = enable != 0;
+    for (int c = 0; c < STG_PROF_NCLASS; c++) {
+        P.launches[c] = 0;
+        P.ms[c] = 0;
+        P.bytes[c] = 0;
+    }
+    return STG_OK;
+}
+
+int stg_profile_read(stg_t* h, int cls, int64_t* launches, double* ms, double* bytes) {
+    STG_TRY(check_handle(h));
+    if (cls < 0 || cls >= STG_PROF_NCLASS) {
+        set_error("bad profile class %d", cls);
+        return STG_E_INVALID;
+    }
+    STG_TRY(prof_flush(h));
+    if (launches) *launches = h->prof.launches[cls];
+    if (ms) *ms = h->prof.ms[cls];
+    if (bytes) *bytes = h->prof.bytes[cls];
+    return STG_OK;
+}
+
+const char* stg_profile_name(int cls) {
+    static const char* names[STG_PROF_NCLASS] = {"resid32",  "vanka32", "restrict32", "prolong32", "apply32",
+                                                 "resid64",  "krylov",  "coarse",     "setup",     "other"};
+    return (cls >= 0 && cls < STG_PROF_NCLASS) ? names[cls] : "";
+}
+
+const char* stg_version(void) { return "stokes_gb300 0.1 (sm_103a)"; }
+
+int stg_create(int dim, int n, const stg_opts* opts, stg_t** out) {
+    if (!out) {
+        set_error("null output handle");
+        return STG_E_INVALID;
+    }
+    *out = nullptr;
+    if (dim != 3) {
+        set_error("dim %d: this build implements the 3D path", dim);
+        return STG_E_UNSUPPORTED;
+    }
+    if (n < 4 || n % 4 != 0) {
+        set_error("N = %d must be a positive multiple of 4", n);
+        return STG_E_INVALID;
+    }
+    if (n > 1024) {
+        set_error("N = %d exceeds the 32-bit slot indexing limit of 1024", n);
+        return STG_E_UNSUPPORTED;
+    }
+    stg_t* h = new stg_t();
+    h->dim = dim;
+    h->n = n;
+    if (opts)
+        h->opts = *opts;
+    else
+        stg_default_opts(&h->opts);
+    if (h->opts.inner_max < 1) h->opts.inner_max = 1;
+    h->m = h->opts.inner_max;
+    h->L = level_count(n);
+    int rc = STG_OK;
+    auto fail = [&](int r) {
+        stg_destroy(h);
+        return r;
+    };
+    if (cudaStreamCreateWithFlags(&h->own_st, cudaStreamNonBlocking) != cudaSuccess) {
+        set_error("cudaStreamCreate failed");
+        delete h;
+        return STG_E_CUDA;
+    }
+    h->st = h->own_st;
+    cudaEventCreate(&h->e0);
+    cudaEventCreate(&h->e1);
+    h->lv.resize(h->L);
+    for (int i = h->L - 1, nn = n; i >= 0; i--, nn /= 2) {
+        Level& L = h->lv[i];
+        L.g = Geom::make(nn);
+        size_t ns = L.g.nslot;
+        if ((rc = dalloc(&L.m, ns)) || (rc = dalloc(&L.P64, ns)) || (rc = dalloc(&L.P32, ns)) || (rc = dalloc(&L.r, ns)) ||
+            (rc = dalloc(&L.xa, ns)) || (rc = dalloc(&L.xb, ns)) || (rc = dalloc(&L.rr, ns)) ||
+            (rc = dalloc(&L.xbf, 4 * ns)))
+            return fail(rc);
+        // halo and absent unknowns fixed; the box is rewritten by set_boundary / coarsen
+        if ((rc = mask_from_field(h->st, L.g, nullptr, nullptr, nullptr, nullptr, L.m))) return fail(rc);
+    }
+    if ((rc = dense_init(h->dense, h->lv[0].g))) return fail(rc);
+    Level& F = fine(h);
+    size_t ns = F.g.nslot;
+    if ((rc = dalloc(&h->b64, ns)) || (rc = dalloc(&h->x64, ns)) || (rc = dalloc(&h->r64, ns)) || (rc = dalloc(&h->t64, ns)) ||
+        (rc = dalloc(&h->lam64, ns)) || (rc = dalloc(&h->w, ns)))
+        return fail(rc);
+    h->V.assign(h->m + 1, nullptr);
+    h->Z.assign(h->m, nullptr);
+    for (auto& p : h->V)
+        if ((rc = dalloc(&p, ns))) return fail(rc);
+    for (auto& p : h->Z)
+        if ((rc = dalloc(&p, ns))) return fail(rc);
+    if ((rc = dalloc(&h->dscr, 1216 * 8)) || (rc = dalloc(&h->dh, 2 * (h->m + 2))) || (rc = dalloc(&h->dnrm, 4)) ||
+        (rc = dalloc(&h->dy, h->m + 1)) || (rc = dalloc(&h->d_parts, (size_t)grid_for(F.g.box(), 256) + 1216)))
+        return fail(rc);
+    h->ncell = (size_t)n * n * n;
+    h->nface = (size_t)n * n * (n + 1);
+    if ((rc = dalloc(&h->stage, h->ncell + 3 * h->nface)) || (rc = dalloc(&h->istage, h->ncell + 3 * h->nface))) return fail(rc);
+    if ((rc = dalloc(&h->d_design, h->ncell)) || (rc = dalloc(&h->d_phys, h->ncell)) || (rc = dalloc(&h->d_sens, h->ncell)) ||
+        (rc = dalloc(&h->d_sens_design, h->ncell)) || (rc = dalloc(&h->d_vw, h->ncell)) || (rc = dalloc(&h->d_tmp, h->ncell)) ||
+        (rc = dalloc(&h->d_gauss, 512)))
+        return fail(rc);
+    if (cudaStreamSynchronize(h->st) != cudaSuccess) return fail(cuda_fail(cudaGetLastError(), "create", __FILE__, __LINE__));
+    *out = h;
+    return STG_OK;
+}
+
+int stg_destroy(stg_t* h) {
+    if (!h) return STG_OK;
+    if (h->st) cudaStreamSynchronize(h->st);
+    for (auto& L : h->lv) {
+        cudaFree(L.m);
+        cudaFree(L.P64);
+        cudaFree(L.P32);
+        cudaFree(L.r);
+        cudaFree(L.xa);
+        cudaFree(L.xb);
+        cudaFree(L.rr);
+        cudaFree(L.xbf);
+        cudaFree(L.t0);
+        cudaFree(L.t1);
+    }
+    dense_free(h->dense);
+    for (d4* p : {h->b64, h->x64, h->r64, h->t64, h->lam64}) cudaFree(p);
+    cudaFree(h->w);
+    for (auto p : h->V) cudaFree(p);
+    for (auto p : h->Z) cudaFree(p);
+    for (double* p : {h->dscr, h->dh, h->dnrm, h->dy, h->stage, h->d_design, h->d_phys, h->d_sens, h->d_sens_design, h->d_vw,
+                      h->d_tmp, h->d_gauss, h->d_parts})
+        cudaFree(p);
+    cudaFree(h->istage);
+    if (h->e0) cudaEventDestroy(h->e0);
+    if (h->e1) cudaEventDestroy(h->e1);
+    for (auto e : h->prof.pool) cudaEventDestroy(e);
+    if (h->own_st) cudaStreamDestroy(h->own_st);
+    delete h;
+    return STG_OK;
+}
+
+int stg_levels(const stg_t* h) { return h ? h->L : 0; }
+int stg_level_n(const stg_t* h, int level) { return (h && level >= 0 && level < h->L) ? h->lv[level].g.n : 0; }
+int64_t stg_level_dof(const stg_t* h, int level) {
+    if (!h || level < 0 || level >= h->L) return 0;
+    Blocked B{h->lv[level].g.n};
+    return B.size();
+}
+
+int stg_set_boundary(stg_t* h, const double* cell_vol, const int32_t* cell_fixed, const double* const* face_vol,
+                     const int32_t* const* face_fixed, int closed) {
+    STG_TRY(check_handle(h));
+    if (!face_vol || !face_fixed) {
+        set_error("face_vol and face_fixed are required");
+        return STG_E_INVALID;
+    }
+    const int n = h->n;
+    // the uniform-coefficient smoother needs one vol value on the free faces and no fixed cell
+    double v = NAN;
+    for (int d = 0; d < 3; d++) {
+        if (!face_vol[d] || !face_fixed[d]) {
+            set_error("face arrays of axis %d missing", d);
+            return STG_E_INVALID;
+        }
+        for (size_t q = 0; q < h->nface; q++) {
+            if (face_fixed[d][q]) continue;
+            if (std::isnan(v)) v = face_vol[d][q];
+            if (face_vol[d][q] != v) {
+                set_error("free faces carry different vol values; this build implements uniform vol only");
+                return STG_E_UNSUPPORTED;
+            }
+        }
+    }
+    if (cell_fixed)
+        for (size_t q = 0; q < h->ncell; q++)
+            if (cell_fixed[q]) {
+                set_error("fixed cells are not supported by this build");
+                return STG_E_UNSUPPORTED;
+            }
+    double cv = cell_vol ? cell_vol[0] : 1.0;
+    Level& F = fine(h);
+    F.vol = std::isnan(v) ? 0.0 : v;
+    F.cell_vol = cv;
+    int* ist = h->istage;
+    const int* fi[3];
+    for (int d = 0; d < 3; d++) {
+        STG_CK(cudaMemcpyAsync(ist + h->ncell + d * h->nface, face_fixed[d], sizeof(int) * h->nface, cudaMemcpyHostToDevice,
+                               h->st));
+        fi[d] = ist + h->ncell + d * h->nface;
+    }
+    STG_TRY(mask_from_field(h->st, F.g, nullptr, fi[0], fi[1], fi[2], F.m));
+    h->closed = closed != 0;
+    h->have_boundary = true;
+    h->updated = false;
+    (void)n;
+    STG_CK(cudaStreamSynchronize(h->st));
+    return STG_OK;
+}
+
+int stg_set_penalty(stg_t* h, const double* cell_penalty, const double* const* face_penalty) {
+    STG_TRY(check_handle(h));
+    if (!h->have_boundary) {
+        set_error("stg_set_boundary must come first");
+        return STG_E_INVALID;
+    }
+    const double* dc = nullptr;
+    const double* df[3] = {nullptr, nullptr, nullptr};
+    STG_TRY(upload_fields(h, cell_penalty, face_penalty, &dc, df));
+    Level& F = fine(h);
+    STG_TRY(penalty_from_field(h->st, F.g, dc, df[0], df[1], df[2], F.m, F.P64, F.P32));
+    h->have_penalty = true;
+    h->updated = false;
+    h->phys_used = nullptr;
+    STG_CK(cudaStreamSynchronize(h->st));
+    return STG_OK;
+}
+
+int stg_set_rhs(stg_t* h, const double* cell_b, const double* const* face_b) {
+    STG_TRY(check_handle(h));
+    const double* dc = nullptr;
+    const double* df[3] = {nullptr, nullptr, nullptr};
+    STG_TRY(upload_fields(h, cell_b, face_b, &dc, df));
+    STG_TRY(field_to_slots64(h->st, fine(h).g, dc, df[0], df[1], df[2], h->b64));
+    h->have_rhs = true;
+    STG_CK(cudaStreamSynchronize(h->st));
+    return STG_OK;
+}
+
+int stg_solve(stg_t* h, double* p_out, double* const* vel_out, stg_stats* stats) {
+    STG_TRY(check_handle(h));
+    if (!h->have_rhs) {
+        set_error("stg_set_rhs must come first");
+        return STG_E_INVALID;
+    }
+    h->updated = false;  // the reference re-runs the set-up on every solve
+    int rc = solve_core(h, h->b64, h->x64, stats);
+    if (rc != STG_OK && rc != STG_E_NOT_CONVERGED) return rc;
+    h->have_solution = true;
+    if (p_out || vel_out) STG_TRY(download_fields(h, h->x64, p_out, vel_out));
+    return rc;
+}
+
+int stg_get_solution(stg_t* h, double* p_out, double* const* vel_out) {
+    STG_TRY(check_handle(h));
+    if (!h->have_solution) {
+        set_error("no solution yet");
+        return STG_E_INVALID;
+    }
+    return download_fields(h, h->x64, p_out, vel_out);
+}
+
+// ---------------------------------------------------------------- energy
+static int energy_input(stg_t* h, const double* p, const double* const* vel, const d4** x) {
+    if (!p && !vel) {
+        if (!h->have_solution) {
+            set_error("no device-resident solution");
+            return STG_E_INVALID;
+        }
+        *x = h->x64;
+        return STG_OK;
+    }
+    const double* dc = nullptr;
+    const double* df[3] = {nullptr, nullptr, nullptr};
+    STG_TRY(upload_fields(h, p, vel, &dc, df));
+    STG_TRY(field_to_slots64(h->st, fine(h).g, dc, df[0], df[1], df[2], h->r64));
+    *x = h->r64;
+    return STG_OK;
+}
+
+int stg_energy(stg_t* h, const double* p, const double* const* vel, double* J) {
+    STG_TRY(check_handle(h));
+    const d4* x;
+    STG_TRY(energy_input(h, p, vel, &x));
+    Level& F = fine(h);
+    int nb = 0;
+    STG_TRY(op64(h->st, F.g, F.vol, x, F.m, F.P64, nullptr, h->t64, 2, h->d_parts, &nb));
+    STG_TRY(reduce_parts(h->st, h->d_parts, nb, h->dnrm));
+    double s = 0;
+    STG_CK(cudaMemcpyAsync(&s, h->dnrm, sizeof(double), cudaMemcpyDeviceToHost, h->st));
+    STG_CK(cudaStreamSynchronize(h->st));
+    if (J) *J = 0.5 * s;
+    return STG_OK;
+}
+
+int stg_energy_grad_x(stg_t* h, const double* p, const double* const* vel, double* p_grad, double* const* vel_grad) {
+    STG_TRY(check_handle(h));
+    const d4* x;
+    STG_TRY(energy_input(h, p, vel, &x));
+    Level& F = fine(h);
+    STG_TRY(op64(h->st, F.g, F.vol, x, F.m, F.P64, nullptr, h->t64, 2, nullptr, nullptr));
+    return download_fields(h, h->t64, p_grad, vel_grad);
+}
+
+int stg_energy_grad_q(stg_t* h, const double* p, const double* const* vel, double* cell_q, double* const* face_q) {
+    STG_TRY(check_handle(h));
+    const d4* x;
+    STG_TRY(energy_input(h, p, vel, &x));
+    Level& F = fine(h);
+    // 1/2 x^2 per unknown (fluid_topo/FluidEnergy3D.cpp:82-91)
+    STG_TRY(half_square64(h->st, F.g.nslot, x, h->t64));
+    return download_fields(h, h->t64, cell_q, face_q);
+}
+
+// ---------------------------------------------------------------- design loop
+int stg_set_density(stg_t* h, const double* rho, const stg_alpha* law) {
+    STG_TRY(check_handle(h));
+    if (!law || !h->have_boundary) {
+        set_error(!law ? "null alpha law" : "stg_set_boundary must come first");
+        return STG_E_INVALID;
+    }
+    if (rho) STG_CK(cudaMemcpyAsync(h->d_phys, rho, sizeof(double) * h->ncell, cudaMemcpyHostToDevice, h->st));
+    Level& F = fine(h);
+    STG_TRY(face_penalty_from_density(h->st, F.g, h->d_phys, *law, F.m, F.P64, F.P32));
+    h->have_penalty = true;
+    h->updated = false;
+    h->phys_used = h->d_phys;
+    STG_CK(cudaStreamSynchronize(h->st));
+    return STG_OK;
+}
+
+int stg_adjoint_sensitivity(stg_t* h, const stg_alpha* law, double* dJ, stg_stats* stats) {
+    STG_TRY(check_handle(h));
+    if (!law || !h->have_solution || !h->phys_used) {
+        set_error("needs an alpha law, a prior stg_solve and a density set by stg_set_density");
+        return STG_E_INVALID;
+    }
+    Level& F = fine(h);
+    // adjoint right-hand side E x, then A lambda = E x (A is symmetric)
+    STG_TRY(op64(h->st, F.g, F.vol, h->x64, F.m, F.P64, nullptr, h->t64, 2, nullptr, nullptr));
+    int rc = solve_core(h, h->t64, h->lam64, stats);
+    if (rc != STG_OK && rc != STG_E_NOT_CONVERGED) return rc;
+    STG_TRY(sensitivity(h->st, F.g, h->phys_used, *law, h->x64, h->lam64, h->d_sens));
+    if (dJ) STG_CK(cudaMemcpyAsync(dJ, h->d_sens, sizeof(double) * h->ncell, cudaMemcpyDeviceToHost, h->st));
+    STG_CK(cudaStreamSynchronize(h->st));
+    return rc;
+}
+
+int stg_filter(stg_t* h, double rmin, const double* in, double* out, int transpose) {
+    STG_TRY(check_handle(h));
+    if (!(rmin > 0)) {
+        set_error("rmin must be positive");
+        return STG_E_INVALID;
+    }
+    double* src = transpose ? h->d_sens : h->d_design;
+    double* dst = transpose ? h->d_sens_design : h->d_phys;
+    if (in) {
+        STG_CK(cudaMemcpyAsync(h->d_tmp, in, sizeof(double) * h->ncell, cudaMemcpyHostToDevice, h->st));
+        src = h->d_tmp;
+    }
+    STG_TRY(density_filter(h->st, h->n, rmin, src, dst, transpose));
+    if (out) STG_CK(cudaMemcpyAsync(out, dst, sizeof(double) * h->ncell, cudaMemcpyDeviceToHost, h->st));
+    STG_CK(cudaStreamSynchronize(h->st));
+    return STG_OK;
+}
+
+int stg_oc_update(stg_t* h, double rmin, const double* x, const double* dc, double frac, double move, double lo, double hi,
+                  double* x_new, double* lambda_out) {
+    STG_TRY(check_handle(h));
+    const int nc = (int)h->ncell;
+    if (h->vw_rmin != rmin) {
+        // vw_j = sum_i w_ij / W_i: the filtered volume is sum_j vw_j x_j
+        std::vector<double> ones(h->ncell, 1.0);
+        STG_CK(cudaMemcpyAsync(h->d_tmp, ones.data(), sizeof(double) * h->ncell, cudaMemcpyHostToDevice, h->st));
+        STG_TRY(density_filter(h->st, h->n, rmin, h->d_tmp, h->d_vw, 1));
+        STG_CK(cudaStreamSynchronize(h->st));
+        h->vw_rmin = rmin;
+    }
+    if (x) STG_CK(cudaMemcpyAsync(h->d_design, x, sizeof(double) * h->ncell, cudaMemcpyHostToDevice, h->st));
+    const double* ddc = h->d_sens_design;
+    if (dc) {
+        STG_CK(cudaMemcpyAsync(h->d_sens, dc, sizeof(double) * h->ncell, cudaMemcpyHostToDevice, h->st));
+        ddc = h->d_sens;
+    }
+    double l1 = 0.0, l2 = 1e9, lmid = 0.0, target = frac * nc;
+    int steps = 0, np = 0;
+    const double tol = 1e-9;
+    while ((l2 - l1) > tol * (l1 + l2) && steps < 200) {
+        lmid = 0.5 * (l1 + l2);
+        STG_TRY(oc_volume(h->st, nc, h->d_design, ddc, h->d_vw, lmid, move, lo, hi, nullptr, h->d_parts, &np));
+        STG_TRY(reduce_parts(h->st, h->d_parts, np, h->dnrm));
+        double vol = 0;
+        STG_CK(cudaMemcpyAsync(&vol, h->dnrm, sizeof(double), cudaMemcpyDeviceToHost, h->st));
+        STG_CK(cudaStreamSynchronize(h->st));
+        if (vol > target)
+            l1 = lmid;
+        else
+            l2 = lmid;
+        steps++;
+    }
+    lmid = 0.5 * (l1 + l2);
+    STG_TRY(oc_volume(h->st, nc, h->d_design, ddc, h->d_vw, lmid, move, lo, hi, h->d_tmp, h->d_parts, &np));
+    STG_CK(cudaMemcpyAsync(h->d_design, h->d_tmp, sizeof(double) * h->ncell, cudaMemcpyDeviceToDevice, h->st));
+    if (x_new) STG_CK(cudaMemcpyAsync(x_new, h->d_design, sizeof(double) * h->ncell, cudaMemcpyDeviceToHost, h->st));
+    STG_CK(cudaStreamSynchronize(h->st));
+    if (lambda_out) *lambda_out = lmid;
+    return STG_OK;
+}
+
+int stg_density_noise(stg_t* h, uint64_t seed, double sigma, double* out) {
+    STG_TRY(check_handle(h));
+    int R = -1;
+    if (sigma > 0) {
+        R = (int)std::ceil(3.0 * sigma);
+        if (2 * R + 1 > 512) {
+            set_error("sigma too large");
+            return STG_E_INVALID;
+        }
+        std::vector<double> w(2 * R + 1);
+        double s = 0;
+        for (int t = -R; t <= R; t++) s += (w[t + R] = std::exp(-(double)(t * t) / (2.0 * sigma * sigma)));
+        for (auto& v : w) v /= s;
+        STG_CK(cudaMemcpyAsync(h->d_gauss, w.data(), sizeof(double) * w.size(), cudaMemcpyHostToDevice, h->st));
+    }
+    STG_TRY(density_noise(h->st, h->n, seed, h->d_gauss, R, h->d_design, h->d_tmp));
+    if (out) STG_CK(cudaMemcpyAsync(out, h->d_design, sizeof(double) * h->ncell, cudaMemcpyDeviceToHost, h->st));
+    STG_CK(cudaStreamSynchronize(h->st));
+    return STG_OK;
+}
+
+// ---------------------------------------------------------------- LinearMapping adapters
+int stg_apply_A_device(stg_t* h, int level, double* d_Ap, const double* d_p) {
+    STG_TRY(check_handle(h));
+    if (level < 0 || level >= h->L || !d_Ap || !d_p) {
+        set_error("bad level or pointer");
+        return STG_E_INVALID;
+    }
+    if (level < h->L - 1 && !h->updated) STG_TRY(update(h));
+    Level& L = h->lv[level];
+    STG_TRY(ensure_adapter(L));
+    STG_TRY(blocked_to_slots64(h->st, L.g, d_p, L.t0));
+    STG_TRY(op64(h->st, L.g, L.vol, L.t0, L.m, L.P64, nullptr, L.t1, 0, nullptr, nullptr));
+    // padding entries of the reference layout are fixed identity rows
+    STG_TRY(slots_to_blocked64(h->st, L.g, L.t1, d_Ap, d_p));
+    STG_CK(cudaStreamSynchronize(h->st));
+    return STG_OK;
+}
+
+int stg_apply_E_device(stg_t* h, double* d_Ap, const double* d_p) {
+    STG_TRY(check_handle(h));
+    Level& L = fine(h);
+    STG_TRY(ensure_adapter(L));
+    STG_TRY(blocked_to_slots64(h->st, L.g, d_p, L.t0));
+    STG_TRY(op64(h->st, L.g, L.vol, L.t0, L.m, L.P64, nullptr, L.t1, 2, nullptr, nullptr));
+    STG_TRY(slots_to_blocked64(h->st, L.g, L.t1, d_Ap, nullptr));
+    STG_CK(cudaStreamSynchronize(h->st));
+    return STG_OK;
+}
+
+int stg_update(stg_t* h) {
+    STG_TRY(check_handle(h));
+    STG_TRY(update(h));
+    STG_CK(cudaStreamSynchronize(h->st));
+    return STG_OK;
+}
+
+int stg_vcycle_device(stg_t* h, double* d_out, const double* d_in) {
+    STG_TRY(check_handle(h));
+    if (!h->updated) STG_TRY(update(h));
+    Level& F = fine(h);
+    STG_TRY(ensure_adapter(F));
+    STG_TRY(blocked_to_slots64(h->st, F.g, d_in, F.t0));
+    STG_TRY(f64_to_f32(h->st, F.g.nslot, F.t0, 1.0, h->w));
+    STG_TRY(vcycle(h, h->w));
+    STG_TRY(f32_to_f64(h->st, F.g.nslot, F.x(), F.t1));
+    STG_TRY(slots_to_blocked64(h->st, F.g, F.t1, d_out, nullptr));
+    STG_CK(cudaStreamSynchronize(h->st));
+    return STG_OK;
+}
+
+int stg_apply_op_device(stg_t* h, int op, int level, double* d_out, const double* d_in) {
+    STG_TRY(check_handle(h));
+    if (level < 0 || level >= h->L || !d_out || !d_in) {
+        set_error("bad level or pointer");
+        return STG_E_INVALID;
+    }
+    if (!h->updated) STG_TRY(update(h));
+    Level& L = h->lv[level];
+    STG_TRY(ensure_adapter(L));
+    switch (op) {
+        case STG_OP_RESTRICT: {
+            if (level >= h->L - 1) break;
+            Level& F = h->lv[level + 1];
+            STG_TRY(ensure_adapter(F));
+            STG_TRY(blocked_to_slots64(h->st, F.g, d_in, F.t0));
+            STG_TRY(restrict64(h->st, L.g, F.g, F.t0, L.m, L.t1));
+            STG_TRY(slots_to_blocked64(h->st, L.g, L.t1, d_out, nullptr));
+            STG_CK(cudaStreamSynchronize(h->st));
+            return STG_OK;
+        }
+        case STG_OP_PROLONG: {
+            if (level >= h->L - 1) break;
+            Level& F = h->lv[level + 1];
+            STG_TRY(ensure_adapter(F));
+            STG_TRY(blocked_to_slots64(h->st, L.g, d_in, L.t0));
+            STG_TRY(prolong64(h->st, F.g, L.g, L.t0, F.m, F.t1));
+            STG_TRY(slots_to_blocked64(h->st, F.g, F.t1, d_out, nullptr));
+            STG_CK(cudaStreamSynchronize(h->st));
+            return STG_OK;
+        }
+        case STG_OP_SMOOTH_PRE:
+        case STG_OP_SMOOTH_POST:
+        case STG_OP_VANKA_RED:
+        case STG_OP_VANKA_BLACK: {
+            if (level == 0) break;
+            STG_TRY(blocked_to_slots64(h->st, L.g, d_in, L.t0));
+            STG_TRY(f64_to_f32(h->st, L.g.nslot, L.t0, 1.0, L.r));
+            L.cur = 0;
+            if (op == STG_OP_SMOOTH_PRE || op == STG_OP_SMOOTH_POST) {
+                STG_CK(cudaMemsetAsync(L.x(), 0, sizeof(float4) * L.g.nslot, h->st));
+                STG_TRY(smooth(h, L, L.r, op == STG_OP_SMOOTH_POST, true));
+            } else {
+                STG_TRY(vanka32(h->st, L.g, (float)L.vol, L.r, nullptr, L.x(), L.m, L.P32, op == STG_OP_VANKA_BLACK ? 1 : 0));
+            }
+            STG_TRY(f32_to_f64(h->st, L.g.nslot, L.x(), L.t1));
+            STG_TRY(slots_to_blocked64(h->st, L.g, L.t1, d_out, nullptr));
+            STG_CK(cudaStreamSynchronize(h->st));
+            return STG_OK;
+        }
+        case STG_OP_COARSE: {
+            if (level != 0) break;
+            STG_TRY(blocked_to_slots64(h->st, L.g, d_in, L.t0));
+            STG_TRY(dense_apply64(h->st, h->dense, L.g, L.t0, L.t1));
+            STG_TRY(slots_to_blocked64(h->st, L.g, L.t1, d_out, nullptr));
+            STG_CK(cudaStreamSynchronize(h->st));
+            return STG_OK;
+        }
+        default: break;
+    }
+    set_error("operator %d not defined at level %d", op, level);
+    return STG_E_INVALID;
+}
+
+int stg_level_descr_device(stg_t* h, int level, double* d_vol, double* d_penalty, uint8_t* d_fixed) {
+    STG_TRY(check_handle(h));
+    if (level < 0 || level >= h->L) {
+        set_error("bad level");
+        return STG_E_INVALID;
+    }
+    if (!h->updated) STG_TRY(update(h));
+    Level& L = h->lv[level];
+    STG_TRY(ensure_adapter(L));
+    if (d_penalty) STG_TRY(slots_to_blocked64(h->st, L.g, L.P64, d_penalty, nullptr));
+    if (d_fixed) STG_TRY(mask_to_blocked(h->st, L.g, L.m, d_fixed));
+    if (d_vol) {
+        STG_TRY(vol_slots(h->st, L.g, L.m, L.cell_vol, L.vol, L.t0));
+        STG_TRY(slots_to_blocked64(h->st, L.g, L.t0, d_vol, nullptr));
+    }
+    STG_CK(cudaStreamSynchronize(h->st));
+    return STG_OK;
+}
+
+}  // extern "C"

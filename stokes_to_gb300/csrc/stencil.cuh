@@ -1,0 +1,148 @@
+// Device-side stencil of the reference Stokes operator A and energy operator E on the
+// slot layout (internal.cuh).
+//
+// A = StokeFlowMapping3DFixed::applyMapping (stoke/StokeFlowMapping3D.cu:218-348):
+//   Ap_f = -fix_f G fix_c D (V u) + V D1 Cod1 (fix_f u) - V G p + P u + F u
+//   Ap_c =  fix_c D (V u) + P p + F p
+// with D the face->cell divergence (common_cpx/grid3D.cu:330-397), G = Cod0 the
+// cell->face difference c(x)-c(x-1) (:401-465), Cod1/D1 the face->edge->face curls
+// (:469-578, :219-326), V the face vol, P the penalty and F the fixed mask.
+// E = FluidEnergyGrad3D::applyMapping (fluid_topo/FluidEnergyGrad3D.cu:201-308) keeps
+// the two viscous terms and P x only.
+//
+// Uniform-coefficient form: every free face carries the same vol value "vol" (fixed
+// faces carry 0, as StokeFlowDescriptor3D::finish leaves them), so V u = vol * fix_f u.
+// One thread evaluates all four rows of one slot from 13 slots: the 7-point
+// neighbourhood plus the six edge-diagonal slots the curl and the divergence reach.
+#pragma once
+#include "internal.cuh"
+
+namespace stg {
+
+template <class T>
+struct Vec4;
+template <>
+struct Vec4<float> {
+    using type = float4;
+};
+template <>
+struct Vec4<double> {
+    using type = d4;
+};
+
+__device__ __forceinline__ void load4(const float4* a, int q, float& p, float& u, float& v, float& w) {
+    float4 t = __ldg(a + q);
+    p = t.x;
+    u = t.y;
+    v = t.z;
+    w = t.w;
+}
+__device__ __forceinline__ void load4(const d4* a, int q, double& p, double& u, double& v, double& w) {
+    const double2* b = reinterpret_cast<const double2*>(a + q);
+    double2 t0 = __ldg(b), t1 = __ldg(b + 1);
+    p = t0.x;
+    u = t0.y;
+    v = t1.x;
+    w = t1.y;
+}
+__device__ __forceinline__ void store4(float4* a, int q, float p, float u, float v, float w) { a[q] = make_float4(p, u, v, w); }
+__device__ __forceinline__ void store4(d4* a, int q, double p, double u, double v, double w) {
+    double2* b = reinterpret_cast<double2*>(a + q);
+    b[0] = make_double2(p, u);
+    b[1] = make_double2(v, w);
+}
+
+// Masked unknowns of one slot: face values with fixed faces zeroed (fix_f u), the raw
+// pressure, and whether the cell is free (fix_c).
+template <class T>
+struct Nb {
+    T p, ux, uy, uz;
+    bool mc;
+};
+
+template <class T, class V>
+__device__ __forceinline__ Nb<T> nb_load(const V* x, const uint8_t* m, int q) {
+    T p, u, v, w;
+    load4(x, q, p, u, v, w);
+    uint8_t mm = __ldg(m + q);
+    Nb<T> r;
+    r.p = p;
+    r.ux = (mm & MU) ? T(0) : u;
+    r.uy = (mm & MV) ? T(0) : v;
+    r.uz = (mm & MW) ? T(0) : w;
+    r.mc = !(mm & MP);
+    return r;
+}
+
+// Viscous and pressure parts of A (or E when ENERGY) at slot s, without the diagonal
+// P x + F x terms. out = {row p, row u, row v, row w}.
+template <class T, bool ENERGY, class V>
+__device__ __forceinline__ void stencil_rows(const V* __restrict__ x, const uint8_t* __restrict__ m, int s, int di, int dj,
+                                             T vol, uint8_t ms, T out[4]) {
+    const int dk = 1;
+    Nb<T> c0 = nb_load<T>(x, m, s);
+    Nb<T> xm = nb_load<T>(x, m, s - di), xp = nb_load<T>(x, m, s + di);
+    Nb<T> ym = nb_load<T>(x, m, s - dj), yp = nb_load<T>(x, m, s + dj);
+    Nb<T> zm = nb_load<T>(x, m, s - dk), zp = nb_load<T>(x, m, s + dk);
+    Nb<T> xp_ym = nb_load<T>(x, m, s + di - dj), xm_yp = nb_load<T>(x, m, s - di + dj);
+    Nb<T> xp_zm = nb_load<T>(x, m, s + di - dk), xm_zp = nb_load<T>(x, m, s - di + dk);
+    Nb<T> yp_zm = nb_load<T>(x, m, s + dj - dk), ym_zp = nb_load<T>(x, m, s - dj + dk);
+
+    // fix_c D (V u) at the own cell and the three lower neighbours
+    T dv0 = c0.mc ? vol * ((xp.ux - c0.ux) + (yp.uy - c0.uy) + (zp.uz - c0.uz)) : T(0);
+    T dvx = xm.mc ? vol * ((c0.ux - xm.ux) + (xm_yp.uy - xm.uy) + (xm_zp.uz - xm.uz)) : T(0);
+    T dvy = ym.mc ? vol * ((xp_ym.ux - ym.ux) + (c0.uy - ym.uy) + (ym_zp.uz - ym.uz)) : T(0);
+    T dvz = zm.mc ? vol * ((xp_zm.ux - zm.ux) + (yp_zm.uy - zm.uy) + (c0.uz - zm.uz)) : T(0);
+
+    // Cod1 edges (common_cpx/grid3D.cu:469-578) at the slot and its upper neighbours
+    T ex0 = c0.uy - zm.uy - c0.uz + ym.uz;
+    T exk = zp.uy - c0.uy - zp.uz + ym_zp.uz;
+    T exj = yp.uy - yp_zm.uy - yp.uz + c0.uz;
+    T ey0 = zm.ux - c0.ux + c0.uz - xm.uz;
+    T eyk = c0.ux - zp.ux + zp.uz - xm_zp.uz;
+    T eyi = xp_zm.ux - xp.ux + xp.uz - c0.uz;
+    T ez0 = c0.ux - ym.ux + xm.uy - c0.uy;
+    T ezj = yp.ux - c0.ux + xm_yp.uy - yp.uy;
+    T ezi = xp.ux - xp_ym.ux + c0.uy - xp.uy;
+    // D1 back to faces (common_cpx/grid3D.cu:219-326)
+    T ccx = (eyk - ey0) + (ez0 - ezj);
+    T ccy = (ex0 - exk) + (ezi - ez0);
+    T ccz = (exj - ex0) + (ey0 - eyi);
+
+    T gx = -(dv0 - dvx) + vol * ccx;
+    T gy = -(dv0 - dvy) + vol * ccy;
+    T gz = -(dv0 - dvz) + vol * ccz;
+    if (!ENERGY) {
+        gx -= vol * (c0.p - xm.p);
+        gy -= vol * (c0.p - ym.p);
+        gz -= vol * (c0.p - zm.p);
+    }
+    out[0] = ENERGY ? T(0) : dv0;
+    out[1] = (ms & MU) ? T(0) : gx;
+    out[2] = (ms & MV) ? T(0) : gy;
+    out[3] = (ms & MW) ? T(0) : gz;
+}
+
+// Full row values: A x (ENERGY false) or E x (ENERGY true) at slot s.
+template <class T, bool ENERGY, class V>
+__device__ __forceinline__ void apply_rows(const V* __restrict__ x, const uint8_t* __restrict__ m, const V* __restrict__ P,
+                                           int s, int di, int dj, T vol, T out[4]) {
+    uint8_t ms = __ldg(m + s);
+    stencil_rows<T, ENERGY>(x, m, s, di, dj, vol, ms, out);
+    T xp, xu, xv, xw, pp, pu, pv, pw;
+    load4(x, s, xp, xu, xv, xw);
+    load4(P, s, pp, pu, pv, pw);
+    if (ENERGY) {
+        out[0] += pp * xp;
+        out[1] += pu * xu;
+        out[2] += pv * xv;
+        out[3] += pw * xw;
+    } else {
+        out[0] += (pp + ((ms & MP) ? T(1) : T(0))) * xp;
+        out[1] += (pu + ((ms & MU) ? T(1) : T(0))) * xu;
+        out[2] += (pv + ((ms & MV) ? T(1) : T(0))) * xv;
+        out[3] += (pw + ((ms & MW) ? T(1) : T(0))) * xw;
+    }
+}
+
+}  // namespace stg

@@ -1,0 +1,227 @@
+// Design-loop kernels: Brinkman penalty from the density (FluidTopoOpt3D::Update_Fluid),
+// the adjoint chain rule (FluidTopoOpt3D::Update_Grad), the density filter, the
+// optimality-criteria volume pass and the seeded density generator.
+//
+// Cell arrays are in the simplex Field order, (i*N + j)*N + k.
+#include <math.h>
+
+#include "kernels.h"
+#include "stencil.cuh"
+
+namespace stg {
+
+namespace {
+
+constexpr int TPB = 256;
+
+__device__ __forceinline__ double alpha_of(double r, const stg_alpha& L) {
+    if (L.law == STG_ALPHA_REF) {
+        double s = r * r * r;
+        return L.alpha_os + (L.alpha_us - L.alpha_os) * s * (1 + L.q) / (s + L.q);
+    }
+    return L.amax * 0.1 * (1.0 - r) / (0.1 + r);
+}
+// d alpha / d rho including the rho^3 chain of the reference law (FluidTopoOpt3D.cpp:202-208, 273)
+__device__ __forceinline__ double dalpha_of(double r, const stg_alpha& L) {
+    if (L.law == STG_ALPHA_REF) {
+        double s = r * r * r;
+        double da = (L.alpha_us - L.alpha_os) * ((1 + L.q) / (s + L.q) - s * (1 + L.q) / ((s + L.q) * (s + L.q)));
+        return da * 3.0 * (r * r);
+    }
+    return -L.amax * 0.1 * 1.1 / ((0.1 + r) * (0.1 + r));
+}
+
+__device__ __forceinline__ long long cidx(int n, int i, int j, int k) { return ((long long)i * n + j) * n + k; }
+
+// face penalty = 1/2 alpha(left cell) + 1/2 alpha(right cell), zero on fixed / absent faces
+__global__ void k_face_penalty(Geom g, const double* __restrict__ rho, stg_alpha L, const uint8_t* __restrict__ m,
+                               d4* __restrict__ P64, float4* __restrict__ P32) {
+    long long t = (long long)blockIdx.x * TPB + threadIdx.x;
+    if (t >= g.box()) return;
+    int i, j, k;
+    g.box_ijk(t, i, j, k);
+    const int n = g.n;
+    int s = g.slot(i, j, k);
+    uint8_t mm = m[s];
+    double own = cell_ok(n, i, j, k) ? 0.5 * alpha_of(rho[cidx(n, i, j, k)], L) : 0.0;
+    double f[3];
+    for (int d = 0; d < 3; d++) {
+        int li = i - (d == 0), lj = j - (d == 1), lk = k - (d == 2);
+        double lo = (li >= 0 && lj >= 0 && lk >= 0 && cell_ok(n, li, lj, lk)) ? 0.5 * alpha_of(rho[cidx(n, li, lj, lk)], L) : 0.0;
+        f[d] = lo + own;
+    }
+    double u = (mm & MU) ? 0.0 : f[0], v = (mm & MV) ? 0.0 : f[1], w = (mm & MW) ? 0.0 : f[2];
+    store4(P64, s, 0.0, u, v, w);
+    P32[s] = make_float4(0.f, (float)u, (float)v, (float)w);
+}
+
+// dJ/drho_c = 1/2 alpha'(rho_c) sum_{6 faces} (-u lambda + 1/2 u^2)   (FluidTopoOpt3D.cpp:264-281)
+__global__ void k_sensitivity(Geom g, const double* __restrict__ rho, stg_alpha L, const d4* __restrict__ x,
+                              const d4* __restrict__ lam, double* __restrict__ grad) {
+    long long t = (long long)blockIdx.x * TPB + threadIdx.x;
+    const int n = g.n;
+    if (t >= (long long)n * n * n) return;
+    int k = (int)(t % n), j = (int)((t / n) % n), i = (int)(t / ((long long)n * n));
+    const double* xs = reinterpret_cast<const double*>(x);
+    const double* ls = reinterpret_cast<const double*>(lam);
+    double sum = 0.0;
+    for (int d = 0; d < 3; d++) {
+        int s0 = g.slot(i, j, k), s1 = g.slot(i + (d == 0), j + (d == 1), k + (d == 2));
+        double u0 = xs[4ll * s0 + 1 + d], l0 = ls[4ll * s0 + 1 + d];
+        double u1 = xs[4ll * s1 + 1 + d], l1 = ls[4ll * s1 + 1 + d];
+        sum += -(u0 * l0) + (0.5 * u0) * u0;
+        sum += -(u1 * l1) + (0.5 * u1) * u1;
+    }
+    double r = rho[t];
+    grad[t] = sum * (0.5 * dalpha_of(r, L));
+}
+
+// Linear hat filter: out_i = sum_j w_ij in_j / W_i (forward) or sum_j w_ji in_j / W_j (transpose).
+__global__ void k_filter(int n, double rmin, int R, const double* __restrict__ in, double* __restrict__ out, int transpose) {
+    long long t = (long long)blockIdx.x * TPB + threadIdx.x;
+    if (t >= (long long)n * n * n) return;
+    int k = (int)(t % n), j = (int)((t / n) % n), i = (int)(t / ((long long)n * n));
+    auto wsum = [&](int a0, int b0, int c0) {
+        double W = 0;
+        for (int a = -R; a <= R; a++)
+            for (int b = -R; b <= R; b++)
+                for (int c = -R; c <= R; c++) {
+                    int ii = a0 + a, jj = b0 + b, kk = c0 + c;
+                    if (ii < 0 || jj < 0 || kk < 0 || ii >= n || jj >= n || kk >= n) continue;
+                    double w = rmin - sqrt((double)(a * a + b * b + c * c));
+                    if (w > 0) W += w;
+                }
+        return W;
+    };
+    double W = transpose ? 0.0 : wsum(i, j, k), s = 0;
+    for (int a = -R; a <= R; a++)
+        for (int b = -R; b <= R; b++)
+            for (int c = -R; c <= R; c++) {
+                int ii = i + a, jj = j + b, kk = k + c;
+                if (ii < 0 || jj < 0 || kk < 0 || ii >= n || jj >= n || kk >= n) continue;
+                double w = rmin - sqrt((double)(a * a + b * b + c * c));
+                if (w <= 0) continue;
+                if (transpose)
+                    s += w * in[cidx(n, ii, jj, kk)] / wsum(ii, jj, kk);
+                else
+                    s += w * in[cidx(n, ii, jj, kk)];
+            }
+    out[t] = transpose ? s : s / W;
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// One bisection probe of the OC update: x_new(lambda) and its filtered volume partials.
+__global__ void k_oc(int ncell, const double* __restrict__ x, const double* __restrict__ dc, const double* __restrict__ vw,
+                     double lam, double move, double lo, double hi, double* __restrict__ xnew, double* __restrict__ part) {
+    __shared__ double sh[TPB / 32];
+    double acc = 0;
+    double inv_n = 1.0 / ncell;
+    for (long long t = (long long)blockIdx.x * TPB + threadIdx.x; t < ncell; t += (long long)gridDim.x * TPB) {
+        double xi = x[t];
+        double dv = vw[t] * inv_n;
+        double B = fmax(0.0, -dc[t]) / (dv * lam);
+        double xn = xi * sqrt(B);
+        xn = fmin(fmin(hi, xi + move), fmax(fmax(lo, xi - move), xn));
+        if (xnew) xnew[t] = xn;
+        acc += vw[t] * xn;
+    }
+    acc = warp_sum(acc);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0;
+        for (int w = 0; w < TPB / 32; w++) s += sh[w];
+        part[blockIdx.x] = s;
+    }
+}
+
+// seeded density: U[0,1) from a SplitMix64 hash of (seed, Field index)
+__global__ void k_uniform(long long nc, uint64_t seed, double* __restrict__ out) {
+    long long t = (long long)blockIdx.x * TPB + threadIdx.x;
+    if (t >= nc) return;
+    uint64_t z = seed * 0x9E3779B97F4A7C15ull + (uint64_t)t + 0x632BE59BD9B4E019ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z = z ^ (z >> 31);
+    out[t] = (double)(z >> 11) * (1.0 / 9007199254740992.0);
+}
+
+// 1D Gaussian along one axis (stride), clamp-to-edge; clip after the last axis
+__global__ void k_blur(int n, long long stride, const double* __restrict__ w, int R, const double* __restrict__ in,
+                       double* __restrict__ out, int clip) {
+    long long t = (long long)blockIdx.x * TPB + threadIdx.x;
+    long long nc = (long long)n * n * n;
+    if (t >= nc) return;
+    int c = (int)((t / stride) % n);
+    double acc = 0;
+    for (int q = -R; q <= R; q++) {
+        int cc = min(n - 1, max(0, c + q));
+        acc += w[q + R] * in[t + (long long)(cc - c) * stride];
+    }
+    out[t] = clip ? fmin(1.0, fmax(0.0, acc)) : acc;
+}
+
+}  // namespace
+
+int face_penalty_from_density(cudaStream_t st, const Geom& g, const double* rho, const stg_alpha& law, const uint8_t* m,
+                              d4* P64, float4* P32) {
+    k_face_penalty<<<grid_for(g.box(), TPB), TPB, 0, st>>>(g, rho, law, m, P64, P32);
+    STG_LAUNCH_CK();
+    return STG_OK;
+}
+
+int sensitivity(cudaStream_t st, const Geom& g, const double* rho, const stg_alpha& law, const d4* x, const d4* lam,
+                double* grad) {
+    long long nc = (long long)g.n * g.n * g.n;
+    k_sensitivity<<<grid_for(nc, TPB), TPB, 0, st>>>(g, rho, law, x, lam, grad);
+    STG_LAUNCH_CK();
+    return STG_OK;
+}
+
+int density_filter(cudaStream_t st, int n, double rmin, const double* in, double* out, int transpose) {
+    int R = (int)ceil(rmin) - 1;
+    if (R < 0) R = 0;
+    long long nc = (long long)n * n * n;
+    k_filter<<<grid_for(nc, TPB), TPB, 0, st>>>(n, rmin, R, in, out, transpose);
+    STG_LAUNCH_CK();
+    return STG_OK;
+}
+
+int oc_volume(cudaStream_t st, int ncell, const double* x, const double* dc, const double* vw, double lam, double move,
+              double lo, double hi, double* xnew, double* parts, int* nparts) {
+    long long g = (ncell + TPB - 1) / TPB;
+    if (g > 1216) g = 1216;
+    if (g < 1) g = 1;
+    *nparts = (int)g;
+    k_oc<<<(unsigned)g, TPB, 0, st>>>(ncell, x, dc, vw, lam, move, lo, hi, xnew, parts);
+    STG_LAUNCH_CK();
+    return STG_OK;
+}
+
+int density_noise(cudaStream_t st, int n, uint64_t seed, const double* w, int R, double* out, double* tmp) {
+    long long nc = (long long)n * n * n;
+    unsigned gb = grid_for(nc, TPB);
+    k_uniform<<<gb, TPB, 0, st>>>(nc, seed, out);
+    STG_LAUNCH_CK();
+    if (R >= 0 && w) {
+        long long strides[3] = {(long long)n * n, n, 1};
+        double* a = out;
+        double* b = tmp;
+        for (int ax = 0; ax < 3; ax++) {
+            k_blur<<<gb, TPB, 0, st>>>(n, strides[ax], w, R, a, b, ax == 2);
+            STG_LAUNCH_CK();
+            double* c = a;
+            a = b;
+            b = c;
+        }
+        // three passes leave the result in tmp
+        STG_CK(cudaMemcpyAsync(out, a, sizeof(double) * nc, cudaMemcpyDeviceToDevice, st));
+    }
+    return STG_OK;
+}
+
+}  // namespace stg

@@ -1,0 +1,79 @@
+"""Generates the committed golden fixtures under tests/golden/.
+
+ref_grid3d_index.npz   blocked-layout index tables produced by the reference's OWN
+                       grid3D host code (oracle/_ref/libref_grid3d.so, built from the
+                       reference sources by oracle/ref_build.sh). Pins the layout.
+oracle_n8.npz          oracle outputs on a seeded 8^3 problem (A x, E x, a V-cycle, the
+                       solution to 1e-12) as a regression fixture for the oracle and
+                       the GPU path.
+
+usage: python tests/golden/make_golden.py
+"""
+import ctypes
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+
+def ref_index_tables():
+    lib = ctypes.CDLL(os.path.join(ROOT, "oracle", "_ref", "libref_grid3d.so"))
+    out = {}
+    for n in (4, 8, 16):
+        cells = np.array([[x, y, z, lib.ref_cell_ind(n, x, y, z)] for x in range(n) for y in range(n) for z in range(n)],
+                         dtype=np.int32)
+        out[f"cell_ind_{n}"] = cells
+        for d in range(3):
+            rows = []
+            for x in range(n + 4 * (d == 0)):
+                for y in range(n + 4 * (d == 1)):
+                    for z in range(n + 4 * (d == 2)):
+                        rows.append([x, y, z, lib.ref_face_ind(n, x, y, z, d), lib.ref_face_valid(n, x, y, z, d)])
+            out[f"face_ind_{n}_{d}"] = np.array(rows, dtype=np.int32)
+            xyz = (ctypes.c_int * 3)()
+            inv = []
+            for i in range(lib.ref_face_size(n, d)):
+                lib.ref_ind_face(n, i, d, xyz)
+                inv.append([i, xyz[0], xyz[1], xyz[2]])
+            out[f"ind_face_{n}_{d}"] = np.array(inv, dtype=np.int32)
+            erows = []
+            for x in range(n + (d != 0)):
+                for y in range(n + (d != 1)):
+                    for z in range(n + (d != 2)):
+                        erows.append([x, y, z, lib.ref_edge_ind(n, x, y, z, d)])
+            out[f"edge_ind_{n}_{d}"] = np.array(erows, dtype=np.int32)
+        xyz = (ctypes.c_int * 3)()
+        inv = []
+        for i in range(lib.ref_cell_size(n)):
+            lib.ref_ind_cell(n, i, xyz)
+            inv.append([i, xyz[0], xyz[1], xyz[2]])
+        out[f"ind_cell_{n}"] = np.array(inv, dtype=np.int32)
+    np.savez_compressed(os.path.join(HERE, "ref_grid3d_index.npz"), **out)
+
+
+def oracle_regression():
+    from oracle import pyoracle as po
+    from tests.helpers import problem
+
+    n = 8
+    b, rho, phys, fp = problem(po, n, seed=11, sigma=2.0)
+    o = po.Steady3D(n)
+    o.init_boundary(b)
+    o.update_penalty(np.zeros((n, n, n)), fp)
+    o.update_b(b.cell_b, b.face_b)
+    o.setup()
+    x = np.random.default_rng(12).standard_normal(o.level_dof(o.levels - 1))
+    bb = po.field_to_blocked(n, b.cell_b, b.face_b)
+    sol, st = o.solve(max_iter=60, abs_thr=0.0, rel_thr=1e-14, norm_thr=0.0, restarts=4, true_tol=1e-12)
+    np.savez_compressed(os.path.join(HERE, "oracle_n8.npz"), rho=rho, x=x, Ax=o.apply_A(x), Ex=o.apply_E(x),
+                        b=bb, vcycle_b=o.vcycle(bb), solution=sol, rel_true=st["rel_true"])
+
+
+if __name__ == "__main__":
+    ref_index_tables()
+    oracle_regression()
+    print("wrote", os.listdir(HERE))

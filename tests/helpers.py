@@ -1,0 +1,30 @@
+"""Shared problem builders for the parity tests (seeded, small)."""
+import numpy as np
+
+
+def problem(po, n, seed=1, sigma=2.0, law="bp", bc="parabolic"):
+    """Boundary + penalty + rhs of a seeded Brinkman-Stokes problem in Field order."""
+    b = po.bc_parabolic(n) if bc == "parabolic" else po.bc_test0_3d(n)
+    rho = po.density_noise(n, seed, sigma)
+    if law == "bp":
+        rf = po.filt(rho, 1.5)
+        fp = po.face_penalty(rf, 1, [1e4])
+        phys = rf
+    else:
+        prm = [5e2 / (n / 32.0), 1e-3, 0.01]
+        fp = po.face_penalty(rho, 0, prm)
+        phys = rho
+    return b, rho, phys, fp
+
+
+def relerr(a, b):
+    a = np.asarray(a, dtype=np.float64).ravel()
+    b = np.asarray(b, dtype=np.float64).ravel()
+    d = np.linalg.norm(a - b)
+    s = np.linalg.norm(b)
+    return d / s if s > 0 else d
+
+
+def pressure_free(p):
+    """Pressure modulo a constant (the closed-domain null space)."""
+    return p - p.mean()

@@ -1,0 +1,223 @@
+"""GPU parity of every hot-path component against the CPU oracle, through the C ABI.
+
+Tolerances: FP64 operators and transfers 1e-12 relative; FP32 smoothing components
+2e-5 relative (single-precision arithmetic); full solves reach the FP64 true relative
+residual asked for and match the oracle's FP64 solution within 1e-6 relative L2
+(pressure compared modulo a constant: closed domains have a constant-pressure null space).
+"""
+import numpy as np
+import pytest
+
+from tests.helpers import pressure_free, problem, relerr
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+
+def dev(a):
+    return torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64)).cuda()
+
+
+def host(t):
+    torch.cuda.synchronize()
+    return t.cpu().numpy()
+
+
+def build_pair(po, capi, n, seed=1, law="bp", bc="parabolic", **opts):
+    b, rho, phys, fp = problem(po, n, seed=seed, law=law, bc=bc)
+    o = po.Steady3D(n)
+    o.init_boundary(b)
+    o.update_penalty(np.zeros((n, n, n)), fp)
+    o.update_b(b.cell_b, b.face_b)
+    o.setup()
+    s = capi.Solver(n, **opts)
+    s.set_boundary_from(b)
+    s.set_penalty(np.zeros((n, n, n)), fp)
+    s.set_rhs(b.cell_b, b.face_b)
+    s.update()
+    return b, rho, phys, fp, o, s
+
+
+@pytest.mark.parametrize("n", [8, 16])
+def test_descriptors_all_levels(oracle, stg, n):
+    b, rho, phys, fp, o, s = build_pair(oracle, stg, n)
+    assert s.levels == o.levels
+    for lvl in range(s.levels):
+        m = s.level_dof(lvl)
+        assert m == o.level_dof(lvl)
+        vol_o, pen_o, fix_o = o.descr(lvl)
+        vol = torch.zeros(m, dtype=torch.float64, device="cuda")
+        pen = torch.zeros(m, dtype=torch.float64, device="cuda")
+        fix = torch.zeros(m, dtype=torch.uint8, device="cuda")
+        s.level_descr_device(lvl, vol.data_ptr(), pen.data_ptr(), fix.data_ptr())
+        assert np.array_equal(host(fix), fix_o), f"fixed mask differs at level {lvl}"
+        assert relerr(host(pen), pen_o) < 1e-13
+        nc = (n >> (s.levels - 1 - lvl)) ** 3
+        # face vol (cell vol never enters A) must agree exactly
+        assert np.array_equal(host(vol)[nc:], vol_o[nc:])
+
+
+@pytest.mark.parametrize("n", [8, 16])
+def test_operator_A_every_level(oracle, stg, n):
+    b, rho, phys, fp, o, s = build_pair(oracle, stg, n)
+    rng = np.random.default_rng(3)
+    for lvl in range(s.levels):
+        x = rng.standard_normal(o.level_dof(lvl))
+        y_ref = o.apply_A(x, lvl)
+        xd = dev(x)
+        yd = torch.zeros_like(xd)
+        s.apply_A_device(lvl, yd.data_ptr(), xd.data_ptr())
+        assert relerr(host(yd), y_ref) < 1e-12, f"level {lvl}"
+
+
+def test_operator_E(oracle, stg):
+    n = 16
+    b, rho, phys, fp, o, s = build_pair(oracle, stg, n)
+    x = np.random.default_rng(4).standard_normal(o.level_dof(o.levels - 1))
+    xd = dev(x)
+    yd = torch.zeros_like(xd)
+    s.apply_E_device(yd.data_ptr(), xd.data_ptr())
+    assert relerr(host(yd), o.apply_E(x)) < 1e-12
+
+
+@pytest.mark.parametrize("n", [8, 16])
+def test_transfers(oracle, stg, n):
+    b, rho, phys, fp, o, s = build_pair(oracle, stg, n)
+    rng = np.random.default_rng(5)
+    for lvl in range(s.levels - 1):
+        rf = rng.standard_normal(o.level_dof(lvl + 1))
+        out = torch.zeros(o.level_dof(lvl), dtype=torch.float64, device="cuda")
+        s.apply_op_device(stg.STG_OP_RESTRICT, lvl, out.data_ptr(), dev(rf).data_ptr())
+        assert relerr(host(out), o.restrict(lvl, rf)) < 1e-13
+        xc = rng.standard_normal(o.level_dof(lvl))
+        outf = torch.zeros(o.level_dof(lvl + 1), dtype=torch.float64, device="cuda")
+        s.apply_op_device(stg.STG_OP_PROLONG, lvl, outf.data_ptr(), dev(xc).data_ptr())
+        assert relerr(host(outf), o.prolong(lvl, xc)) < 1e-13
+
+
+@pytest.mark.parametrize("n", [8, 16])
+def test_vanka_blocks_and_smoothers(oracle, stg, n):
+    b, rho, phys, fp, o, s = build_pair(oracle, stg, n)
+    rng = np.random.default_rng(6)
+    for lvl in range(1, s.levels):
+        m = o.level_dof(lvl)
+        _, _, fixed = o.descr(lvl)
+        r = rng.standard_normal(m) * (1 - fixed)
+        rd = dev(r)
+        out = torch.zeros_like(rd)
+        for op, flag in ((stg.STG_OP_VANKA_RED, 0), (stg.STG_OP_VANKA_BLACK, 1)):
+            s.apply_op_device(op, lvl, out.data_ptr(), rd.data_ptr())
+            assert relerr(host(out), o.vanka_apply(lvl, flag, r)) < 2e-5, f"vanka flag {flag} level {lvl}"
+        for op, post in ((stg.STG_OP_SMOOTH_PRE, 0), (stg.STG_OP_SMOOTH_POST, 1)):
+            s.apply_op_device(op, lvl, out.data_ptr(), rd.data_ptr())
+            assert relerr(host(out), o.smooth(lvl, post, r)) < 2e-5, f"smoother post={post} level {lvl}"
+
+
+@pytest.mark.parametrize("n", [4, 8])
+def test_coarsest_dense_solve(oracle, stg, n):
+    b, rho, phys, fp, o, s = build_pair(oracle, stg, n)
+    assert o.coarse_info() == 0
+    _, _, fixed = o.descr(0)
+    r = np.random.default_rng(7).standard_normal(o.level_dof(0)) * (1 - fixed)
+    out = torch.zeros(o.level_dof(0), dtype=torch.float64, device="cuda")
+    s.apply_op_device(stg.STG_OP_COARSE, 0, out.data_ptr(), dev(r).data_ptr())
+    assert relerr(host(out), o.coarse_apply(r)) < 1e-9
+
+
+@pytest.mark.parametrize("n", [8, 16, 32])
+def test_vcycle(oracle, stg, n):
+    b, rho, phys, fp, o, s = build_pair(oracle, stg, n)
+    bb = oracle.field_to_blocked(n, b.cell_b, b.face_b)
+    out = torch.zeros(bb.size, dtype=torch.float64, device="cuda")
+    s.vcycle_device(out.data_ptr(), dev(bb).data_ptr())
+    assert relerr(host(out), o.vcycle(bb)) < 1e-4
+
+
+@pytest.mark.parametrize("n,law,bc", [(8, "bp", "parabolic"), (16, "bp", "parabolic"), (32, "bp", "parabolic"),
+                                      (64, "ref", "test0")])
+@pytest.mark.parametrize("method", [0, 1])
+def test_solve_matches_oracle(oracle, stg, n, law, bc, method):
+    b, rho, phys, fp, o, s = build_pair(oracle, stg, n, law=law, bc=bc, tol=1e-10, method=method)
+    p, vel, st = s.solve()
+    assert st["status"] == 0 and st["rel_residual"] <= 1e-10
+    x_ref, ost = o.solve(max_iter=60, abs_thr=0.0, rel_thr=1e-13, norm_thr=0.0, restarts=4, true_tol=1e-11)
+    assert ost["rel_true"] <= 1e-10
+    p_ref, vel_ref = oracle.blocked_to_field(n, x_ref)
+    for d in range(3):
+        assert relerr(vel[d], vel_ref[d]) < 1e-6
+    assert relerr(pressure_free(p), pressure_free(p_ref)) < 1e-6
+    # energy of the GPU solution against the oracle's energy of its own solution
+    J = s.energy()
+    assert abs(J - o.energy(x_ref)) <= 1e-6 * abs(o.energy(x_ref))
+
+
+def test_energy_gradients(oracle, stg):
+    n = 16
+    b, rho, phys, fp, o, s = build_pair(oracle, stg, n)
+    rng = np.random.default_rng(8)
+    p = rng.standard_normal((n, n, n))
+    vel = [rng.standard_normal(oracle.face_shape(n, d)) for d in range(3)]
+    x = oracle.field_to_blocked(n, p, vel)
+    assert abs(s.energy(p, vel) - o.energy(x)) <= 1e-12 * abs(o.energy(x))
+    gp, gv = s.energy_grad_x(p, vel)
+    gp_ref, gv_ref = oracle.blocked_to_field(n, o.apply_E(x))
+    for d in range(3):
+        assert relerr(gv[d], gv_ref[d]) < 1e-12
+    qp, qv = s.energy_grad_q(p, vel)
+    for d in range(3):
+        assert relerr(qv[d], 0.5 * vel[d] ** 2) < 1e-15
+
+
+@pytest.mark.parametrize("law", ["bp", "ref"])
+def test_adjoint_sensitivity(oracle, stg, law):
+    n = 16
+    b, rho, phys, fp, o, s = build_pair(oracle, stg, n, law=law, tol=1e-11)
+    L = stg.alpha_bp() if law == "bp" else stg.alpha_ref(n)
+    s.set_density(phys, L)
+    p, vel, st = s.solve()
+    g, ast = s.adjoint_sensitivity(L)
+    assert ast["rel_residual"] <= 1e-11
+    # oracle: forward solve, adjoint rhs E x, adjoint solve, chain rule
+    x_ref, _ = o.solve(max_iter=60, abs_thr=0.0, rel_thr=1e-13, norm_thr=0.0, restarts=4, true_tol=1e-12)
+    o.set_b_blocked(o.apply_E(x_ref))
+    lam_ref, _ = o.solve(max_iter=60, abs_thr=0.0, rel_thr=1e-13, norm_thr=0.0, restarts=4, true_tol=1e-12)
+    _, u = oracle.blocked_to_field(n, x_ref)
+    _, lam = oracle.blocked_to_field(n, lam_ref)
+    prm = [1e4] if law == "bp" else [5e2 / (n / 32.0), 1e-3, 0.01]
+    g_ref = oracle.sensitivity(phys, 1 if law == "bp" else 0, prm, u, lam)
+    assert relerr(g, g_ref) < 1e-6
+
+
+def test_filter_oc_and_noise(oracle, stg):
+    n = 16
+    s = stg.Solver(n)
+    rho = s.density_noise(7, 2.0)
+    assert relerr(rho, oracle.density_noise(n, 7, 2.0)) < 1e-14
+    rf = s.filter(1.5, rho)
+    assert relerr(rf, oracle.filt(rho, 1.5)) < 1e-14
+    g = np.random.default_rng(9).standard_normal((n, n, n))
+    gt = s.filter(1.5, g, transpose=True)
+    assert relerr(gt, oracle.filt(g, 1.5, transpose=True)) < 1e-14
+    dc = -np.abs(np.random.default_rng(10).standard_normal((n, n, n)))
+    xn, lam = s.oc_update(1.5, rho, dc, 0.3)
+    vw = oracle.filt(np.ones((n, n, n)), 1.5, transpose=True)
+    xn_ref, lam_ref, _ = oracle.oc_update(rho, dc, vw / n ** 3, vw, 0.3)
+    assert relerr(xn, xn_ref.reshape(n, n, n)) < 1e-9
+    assert abs(np.sum(vw * xn) / n ** 3 - 0.3) < 1e-6
+
+
+def test_errors_are_reported(stg):
+    with pytest.raises(stg.StgError) as e:
+        stg.Solver(6)
+    assert e.value.code == stg.STG_E_INVALID
+    s = stg.Solver(8)
+    with pytest.raises(stg.StgError):
+        s.solve()  # no rhs
+    n = 8
+    vol = [np.ones(stg.face_shape(n, d)) for d in range(3)]
+    vol[0][3, 3, 3] = 2.0
+    fixed = [np.zeros(stg.face_shape(n, d), dtype=np.int32) for d in range(3)]
+    with pytest.raises(stg.StgError) as e:
+        s.set_boundary(np.ones((n, n, n)), np.zeros((n, n, n), dtype=np.int32), vol, fixed)
+    assert e.value.code == stg.STG_E_UNSUPPORTED

@@ -1,0 +1,198 @@
+"""CPU tests of the oracle: pinned against the reference's own compiled layout code,
+regression against the committed fixtures, and the structural facts the GPU kernels
+build on (operator symmetry, arrow-shaped Vanka blocks with no coupling between blocks,
+transfer adjointness, coarsest solve, GMRES convergence, adjoint gradient)."""
+import os
+
+import numpy as np
+import pytest
+
+from tests.helpers import problem, relerr
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def test_layout_matches_reference_index_tables(oracle):
+    """Blocked layout of common_cpx/grid3D.cu:24-146, tables produced by the reference's code."""
+    L = oracle.lib()
+    tab = np.load(os.path.join(GOLD, "ref_grid3d_index.npz"))
+    xyz = (oracle.ctypes.c_int * 3)()
+    for n in (4, 8, 16):
+        for x, y, z, idx in tab[f"cell_ind_{n}"]:
+            assert L.orc3_index(n, 0, int(x), int(y), int(z), 0, xyz) == idx
+        for i, x, y, z in tab[f"ind_cell_{n}"]:
+            L.orc3_index(n, 3, int(i), 0, 0, 0, xyz)
+            assert tuple(xyz) == (x, y, z)
+        for d in range(3):
+            for x, y, z, idx, valid in tab[f"face_ind_{n}_{d}"]:
+                assert L.orc3_index(n, 1, int(x), int(y), int(z), d, xyz) == idx
+            for i, x, y, z in tab[f"ind_face_{n}_{d}"]:
+                L.orc3_index(n, 4, int(i), 0, 0, d, xyz)
+                assert tuple(xyz) == (x, y, z)
+            for x, y, z, idx in tab[f"edge_ind_{n}_{d}"]:
+                assert L.orc3_index(n, 2, int(x), int(y), int(z), d, xyz) == idx
+
+
+def test_oracle_regression_fixture(oracle):
+    g = np.load(os.path.join(GOLD, "oracle_n8.npz"))
+    n = 8
+    b, rho, phys, fp = problem(oracle, n, seed=11, sigma=2.0)
+    assert np.array_equal(rho, g["rho"])
+    o = oracle.Steady3D(n)
+    o.init_boundary(b)
+    o.update_penalty(np.zeros((n, n, n)), fp)
+    o.update_b(b.cell_b, b.face_b)
+    o.setup()
+    assert relerr(o.apply_A(g["x"]), g["Ax"]) < 1e-14
+    assert relerr(o.apply_E(g["x"]), g["Ex"]) < 1e-14
+    assert relerr(o.vcycle(g["b"]), g["vcycle_b"]) < 1e-12
+
+
+def _setup(oracle, n, **kw):
+    b, rho, phys, fp = problem(oracle, n, **kw)
+    o = oracle.Steady3D(n)
+    o.init_boundary(b)
+    o.update_penalty(np.zeros((n, n, n)), fp)
+    o.update_b(b.cell_b, b.face_b)
+    o.setup()
+    return b, o
+
+
+def test_operators_symmetric(oracle):
+    b, o = _setup(oracle, 8)
+    rng = np.random.default_rng(0)
+    for lvl in range(o.levels):
+        m = o.level_dof(lvl)
+        x, y = rng.standard_normal(m), rng.standard_normal(m)
+        assert abs(y @ o.apply_A(x, lvl) - x @ o.apply_A(y, lvl)) < 1e-12 * abs(y @ o.apply_A(x, lvl))
+    m = o.level_dof(o.levels - 1)
+    x, y = rng.standard_normal(m), rng.standard_normal(m)
+    assert abs(y @ o.apply_E(x) - x @ o.apply_E(y)) < 1e-12 * abs(y @ o.apply_E(x))
+    assert x @ o.apply_E(x) > 0
+
+
+def test_transfers_are_adjoint(oracle):
+    b, o = _setup(oracle, 16)
+    rng = np.random.default_rng(1)
+    for lvl in range(o.levels - 1):
+        _, _, ff = o.descr(lvl + 1)
+        _, _, fc = o.descr(lvl)
+        r = rng.standard_normal(o.level_dof(lvl + 1)) * (1 - ff)
+        xc = rng.standard_normal(o.level_dof(lvl)) * (1 - fc)
+        assert abs(o.restrict(lvl, r) @ xc - r @ o.prolong(lvl, xc)) < 1e-12 * np.linalg.norm(r) * np.linalg.norm(xc)
+
+
+def test_vanka_blocks_are_exact_arrow_blocks(oracle):
+    """B = M_w A M_w + M_b A M_b couples no two red blocks and is an arrow matrix in each
+    block (uniform vol, no fixed cell); the GPU smoother solves these blocks in closed form."""
+    n = 8
+    b, o = _setup(oracle, n)
+    lvl = o.levels - 1
+    m = o.level_dof(lvl)
+    rng = np.random.default_rng(2)
+    _, _, fixed = o.descr(lvl)
+    for flag in (0, 1):
+        r = rng.standard_normal(m)
+        d = o.vanka_apply(lvl, flag, r)
+        touched = d != 0
+        # applying the block-diagonal B to d reproduces r on every touched DOF
+        # (B from masked operator applies, as the reference's PartialMapping does)
+        L = oracle.lib()
+        y = np.zeros(m)
+        cells = n ** 3
+        fx = np.zeros(m, dtype=bool)
+        xyz = (oracle.ctypes.c_int * 3)()
+        for face_flag in (0, 1):
+            mask = np.zeros(m, dtype=bool)
+            for i in range(cells):
+                L.orc3_index(n, 3, i, 0, 0, 0, xyz)
+                mask[i] = (xyz[0] + xyz[1] + xyz[2] + flag) % 2 == 0
+            off = cells
+            for dd in range(3):
+                fs = (n + 4 * (dd == 0)) * (n + 4 * (dd == 1)) * (n + 4 * (dd == 2))
+                for i in range(fs):
+                    L.orc3_index(n, 4, i, 0, 0, dd, xyz)
+                    mask[off + i] = (xyz[0] + xyz[1] + xyz[2] + face_flag) % 2 == 0
+                off += fs
+            y += np.where(mask, o.apply_A(np.where(mask, d, 0.0), lvl), 0.0)
+        assert np.max(np.abs(y[touched] - r[touched])) < 1e-10 * np.max(np.abs(r))
+        del fx
+
+
+def test_coarsest_solve_inverts_closed_matrix(oracle):
+    b, o = _setup(oracle, 4)
+    assert o.coarse_info() == 0
+    m = o.level_dof(0)
+    _, _, fixed = o.descr(0)
+    r = np.random.default_rng(3).standard_normal(m) * (1 - fixed)
+    x = o.coarse_apply(r)
+    res = o.apply_A(x, 0) - r
+    # closed: the assembled matrix adds sum(p) to every pressure row (stoke/StokeLike.cu:605-608)
+    res[:64] += x[:64].sum()
+    assert np.linalg.norm(res) < 1e-10 * np.linalg.norm(r)
+
+
+@pytest.mark.parametrize("n", [8, 16])
+def test_gmres_reaches_tight_tolerance(oracle, n):
+    b, o = _setup(oracle, n)
+    x, st = o.solve(max_iter=60, abs_thr=0.0, rel_thr=1e-13, norm_thr=0.0, restarts=3, true_tol=1e-11)
+    assert st["rel_true"] < 1e-11
+
+
+def test_reference_stopping_rule_is_loose(oracle):
+    """The reference thresholds (GMRES.h:15-17) stop on the preconditioned residual."""
+    b, o = _setup(oracle, 8)
+    x, st = o.solve()  # max_iter 50, abs 1e-3, rel 1e-4
+    assert st["iters"] >= 1 and st["rel_true"] < 1e-2
+
+
+def test_adjoint_gradient_matches_central_differences(oracle):
+    """Central differences on the design (fluid_topo/FluidTopoOpt3D.cpp:206-223), BP law."""
+    n = 8
+    b = oracle.bc_parabolic(n)
+    rho = 0.3 + 0.4 * oracle.density_noise(n, 3, 1.0)
+
+    def objective(r):
+        fp = oracle.face_penalty(r, 1, [1e4])
+        o = oracle.Steady3D(n)
+        o.init_boundary(b)
+        o.update_penalty(np.zeros((n, n, n)), fp)
+        o.update_b(b.cell_b, b.face_b)
+        o.setup()
+        x, st = o.solve(max_iter=60, abs_thr=0.0, rel_thr=1e-14, norm_thr=0.0, restarts=4, true_tol=1e-13)
+        return o, x, o.energy(x)
+
+    o, x, J = objective(rho)
+    o.set_b_blocked(o.apply_E(x))
+    lam, _ = o.solve(max_iter=60, abs_thr=0.0, rel_thr=1e-14, norm_thr=0.0, restarts=4, true_tol=1e-13)
+    _, u = oracle.blocked_to_field(n, x)
+    _, la = oracle.blocked_to_field(n, lam)
+    g = oracle.sensitivity(rho, 1, [1e4], u, la)
+    h = 1e-5
+    for c in [(1, 3, 4), (4, 4, 4), (6, 2, 5)]:
+        rp, rm = rho.copy(), rho.copy()
+        rp[c] += h
+        rm[c] -= h
+        num = (objective(rp)[2] - objective(rm)[2]) / (2 * h)
+        assert abs(num - g[c]) <= 1e-4 * max(abs(num), 1e-3 * abs(J))
+
+
+def test_filter_and_oc(oracle):
+    n = 8
+    one = np.ones((n, n, n))
+    assert np.allclose(oracle.filt(one, 1.5), 1.0)
+    rng = np.random.default_rng(4)
+    a, c = rng.random((n, n, n)), rng.random((n, n, n))
+    assert abs((oracle.filt(a, 1.5) * c).sum() - (a * oracle.filt(c, 1.5, transpose=True)).sum()) < 1e-12
+    x = np.full((n, n, n), 0.3)
+    dc = -rng.random((n, n, n))
+    vw = oracle.filt(one, 1.5, transpose=True)
+    xn, lam, steps = oracle.oc_update(x, dc, vw / n ** 3, vw, 0.3)
+    assert abs((vw.ravel() * xn).sum() / n ** 3 - 0.3) < 1e-8
+    assert np.all(np.abs(xn - x.ravel()) <= 0.2 + 1e-15)
+
+
+def test_density_noise_statistics(oracle):
+    r = oracle.density_noise(16, 0, 4.0)
+    assert r.min() >= 0 and r.max() <= 1 and abs(r.mean() - 0.5) < 0.05
+    assert np.array_equal(r, oracle.density_noise(16, 0, 4.0))
