@@ -1,0 +1,408 @@
+"""Benchmark: seconds per 256^3 Brinkman-Stokes solve to FP64 relative residual 1e-8.
+
+One step = one full solve (coarse re-discretisation, coarsest inverse, FP32 V-cycle
+FGMRES inside FP64 refinement) of the 256^3 parabolic-inlet problem with a seeded,
+Gaussian-smoothed density (sigma 4 cells), density filter r = 1.5 and the
+Borrvall-Petersson alpha law (amax 1e4). Working set is ~25 GB, far above the 129 MB L2.
+
+  value  device-resident inputs, CUDA events on the solve stream      (method: mixed)
+  e2e    host buffers through the C ABI: set_penalty + set_rhs + solve + read back
+  --impl reference: the CPU reference restatement (oracle) on the host cores.
+
+N>1 (torchrun): independent replicas, one per GPU, barrier + max over ranks.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_DEFAULT = 256
+TOL = 1e-8
+FALLBACK_HBM_GBS = 6800.0
+METRIC = "s per 256^3 Stokes solve to FP64 resid 1e-8 (mixed precision)"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=N_DEFAULT)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-plain", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def face_shape(n, d):
+    s = [n, n, n]
+    s[d] += 1
+    return tuple(s)
+
+
+def parabolic_bc(n):
+    """Parabolic inlet on a centred N/4 x N/4 patch of x = 0, mirrored outlet at x = 1,
+    every boundary face fixed, in the reference's source-term encoding."""
+    W = n // 4
+    lo = n // 2 - W // 2
+    cell_vol = np.ones((n, n, n))
+    cell_fixed = np.zeros((n, n, n), dtype=np.int32)
+    cell_b = np.zeros((n, n, n))
+    face_vol = [np.ones(face_shape(n, d)) for d in range(3)]
+    face_fixed = [np.zeros(face_shape(n, d), dtype=np.int32) for d in range(3)]
+    face_b = [np.zeros(face_shape(n, d)) for d in range(3)]
+    face_fixed[0][0], face_fixed[0][n] = 1, 1
+    face_fixed[1][:, 0], face_fixed[1][:, n] = 1, 1
+    face_fixed[2][:, :, 0], face_fixed[2][:, :, n] = 1, 1
+    t = np.arange(lo, lo + W)
+    s = (t + 0.5) - n / 2.0
+    g1 = 1.0 - (2.0 * s / W) ** 2
+    g = np.outer(g1, g1)
+    cell_b[0, lo:lo + W, lo:lo + W] = g
+    face_b[0][1, lo:lo + W, lo:lo + W] = g
+    cell_b[n - 1, lo:lo + W, lo:lo + W] = -g
+    face_b[0][n - 1, lo:lo + W, lo:lo + W] = g
+    return cell_vol, cell_fixed, cell_b, face_vol, face_fixed, face_b
+
+
+def face_penalty_host(rho_f, amax=1e4):
+    """Face penalty = sum over the two adjacent cells of 1/2 alpha(rho~) (host arrays for e2e)."""
+    a = 0.5 * amax * 0.1 * (1.0 - rho_f) / (0.1 + rho_f)
+    out = []
+    for d in range(3):
+        f = np.zeros(face_shape(rho_f.shape[0], d))
+        sl_lo = [slice(None)] * 3
+        sl_hi = [slice(None)] * 3
+        sl_lo[d] = slice(0, -1)
+        sl_hi[d] = slice(1, None)
+        f[tuple(sl_hi)] += a
+        f[tuple(sl_lo)] += a
+        out.append(f)
+    return out
+
+
+class Clocks:
+    """Samples nvidia-smi every 200 ms while the timed region runs."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 7:
+                continue
+            try:
+                sm.append(float(p[0]))
+                mx.append(float(p[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        try:
+            d = json.load(open(p))
+            for k in ("hbm_gbs", "hbm_GBps", "hbm"):
+                if k in d:
+                    v = d[k]
+                    return float(v["burst"] if isinstance(v, dict) and "burst" in v else v), "measured"
+        except Exception:
+            pass
+    return FALLBACK_HBM_GBS, "fallback"
+
+
+def ncu_traffic():
+    """DRAM bytes per launch of each kernel class from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "ncu_traffic_256.txt")
+    out = {}
+    if os.path.exists(p):
+        for ln in open(p):
+            ln = ln.strip()
+            if ln.startswith("traffic "):
+                _, cls, val = ln.split()[:3]
+                out[cls] = float(val)
+    return out
+
+
+# ------------------------------------------------------------------ reference (CPU) arm
+def cpu_reference_sample(sample_n=64):
+    """The reference algorithm restated on the CPU (GMRES with the reference V-cycle: Vanka
+    smoother, re-discretised coarse levels, dense coarsest solve), run to the same FP64
+    tolerance on the same problem family at sample_n^3, scaled by the cell count."""
+    from oracle import pyoracle as po
+
+    po.build()
+    n = sample_n
+    b = po.bc_parabolic(n)
+    rho = po.density_noise(n, 1, 4.0)
+    fp = po.face_penalty(po.filt(rho, 1.5), 1, [1e4])
+    t0 = time.perf_counter()
+    o = po.Steady3D(n)
+    o.init_boundary(b)
+    o.update_penalty(np.zeros((n, n, n)), fp)
+    o.update_b(b.cell_b, b.face_b)
+    o.setup()
+    x, st = o.solve(max_iter=60, abs_thr=0.0, rel_thr=1e-12, norm_thr=0.0, restarts=3, true_tol=TOL)
+    sec = time.perf_counter() - t0
+    o.close()
+    scale = (N_DEFAULT / n) ** 3
+    return sec * scale, sec, st
+
+
+def run_reference(args):
+    world, rank, local = dist_env()
+    if rank != 0:
+        return
+    cores = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
+    times = []
+    for i in range(args.warmup + args.steps):
+        v, sec, st = cpu_reference_sample()
+        if i >= args.warmup:
+            times.append(v)
+    value = statistics.mean(times)
+    sample = (f"oracle GMRES(V-cycle) solve of the 64^3 instance of the same problem to FP64 rel. residual "
+              f"{TOL:g} ({st['iters']} GMRES iterations, {sec:.2f} s), scaled x64 by cell count to 256^3")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "s/solve", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": value * 1e3, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "3D 256^3 Brinkman-Stokes solve to FP64 rel. residual 1e-8", "n": 256, "tol": TOL},
+        "cpu_baseline": {"value": value, "unit": "s/solve", "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": "s/solve", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------ our arm
+def run_ours(args):
+    import torch
+
+    world, rank, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    from stokes_to_gb300 import build, capi
+
+    build.build()
+    n = args.n
+    cell_vol, cell_fixed, cell_b, face_vol, face_fixed, face_b = parabolic_bc(n)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    def max_over_ranks(v):
+        if world == 1:
+            return v
+        t = torch.tensor([v], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum_over_ranks(v):
+        if world == 1:
+            return v
+        t = torch.tensor([v], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(t)
+        return float(t.item())
+
+    stream = torch.cuda.current_stream()
+
+    def make_solver(method):
+        s = capi.Solver(n, method=method, tol=TOL)
+        s.set_stream(stream.cuda_stream)
+        s.set_boundary(cell_vol, cell_fixed, face_vol, face_fixed, True)
+        s.density_noise(1 + rank, 4.0, want=False)
+        s.filter(1.5, None, want=False)
+        s.set_density(None, capi.alpha_bp(1e4))
+        s.set_rhs(cell_b, face_b)
+        return s
+
+    def timed_device(s, steps, warmup, profile=False):
+        for _ in range(warmup):
+            s.solve(want=False)
+        barrier()
+        if profile:
+            s.profile(True)
+        l0 = capi.kernel_launches()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        stats = []
+        with Clocks(local) as clk:
+            barrier()
+            e0.record(stream)
+            for _ in range(steps):
+                _, _, st = s.solve(want=False)
+                stats.append(st)
+            e1.record(stream)
+            barrier()
+        ms = e0.elapsed_time(e1)
+        launches = capi.kernel_launches() - l0
+        prof = s.profile_read() if profile else None
+        return ms, stats, launches, clk.summary(), prof
+
+    # ---- headline: mixed method, inputs resident
+    s = make_solver(capi.STG_METHOD_MIXED)
+    ms, stats, launches, clocks, prof = timed_device(s, args.steps, args.warmup, profile=True)
+    t_max = max_over_ranks(ms / 1e3)
+    value = t_max / (args.steps * world)
+    launches = int(sum_over_ranks(launches))
+
+    # ---- e2e: host (pinned) buffers through the C ABI, copies inside the timed region
+    rho = s.density_noise(1 + rank, 4.0, want=True)
+    rho_f = s.filter(1.5, rho, want=True)
+    fpen = face_penalty_host(rho_f)
+    pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
+    fpen_p = [pin(f) for f in fpen]
+    cb_p, fb_p = pin(cell_b), [pin(f) for f in face_b]
+    p_out = pin(np.zeros((n, n, n)))
+    v_out = [pin(np.zeros(face_shape(n, d))) for d in range(3)]
+    tabs = (capi.DP * 3)(*[capi.dp(v) for v in v_out])
+    ftab = (capi.DP * 3)(*[capi.dp(f) for f in fpen_p])
+    btab = (capi.DP * 3)(*[capi.dp(f) for f in fb_p])
+    L = capi.lib()
+
+    def e2e_step():
+        capi.check(L.stg_set_penalty(s.h, None, ftab))
+        capi.check(L.stg_set_rhs(s.h, capi.dp(cb_p), btab))
+        st = capi.Stats()
+        capi.check(L.stg_solve(s.h, capi.dp(p_out), tabs, capi.ctypes.byref(st)))
+        return st
+
+    for _ in range(args.warmup):
+        e2e_step()
+    barrier()
+    t0 = time.perf_counter()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        e2e_step()
+    e1.record(stream)
+    barrier()
+    e2e_ms = max(e0.elapsed_time(e1), (time.perf_counter() - t0) * 1e3)
+    e2e_value = max_over_ranks(e2e_ms / 1e3) / (args.steps * world)
+    h2d = sum(f.nbytes for f in fpen_p) + cb_p.nbytes + sum(f.nbytes for f in fb_p)
+    d2h = p_out.nbytes + sum(v.nbytes for v in v_out)
+
+    # ---- plain FP32/FP64 method for context
+    plain = None
+    if not args.no_plain:
+        sp = make_solver(capi.STG_METHOD_PLAIN)
+        pms, pstats, _, _, _ = timed_device(sp, max(2, args.steps // 2), 1)
+        plain = max_over_ranks(pms / 1e3) / (max(2, args.steps // 2) * world)
+        plain_vc = statistics.mean(st["inner_iters"] for st in pstats)
+        sp.close()
+
+    # ---- roofline of the dominant kernel class, measured over the timed region
+    peak, peak_kind = measured_peak()
+    dom = max((k for k in prof if prof[k]["launches"]), key=lambda k: prof[k]["ms"])
+    d = prof[dom]
+    achieved = d["bytes"] / (d["ms"] * 1e-3) / 1e9
+    traffic = ncu_traffic().get(dom)
+    kernel_table = {k: {"launches": v["launches"], "ms": round(v["ms"], 3),
+                        "GBps": round(v["bytes"] / (v["ms"] * 1e-3) / 1e9, 1) if v["ms"] > 0 and v["bytes"] > 0 else None}
+                    for k, v in prof.items() if v["launches"]}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count() or 1))
+        cv, csec, cst = cpu_reference_sample()
+        cpu = {"value": cv, "unit": "s/solve", "cores": int(os.environ["OMP_NUM_THREADS"]), "kind": "port",
+               "sample": f"oracle GMRES(V-cycle) solve of the 64^3 instance to FP64 rel. residual {TOL:g} "
+                         f"({cst['iters']} iterations, {csec:.2f} s on the host cores), scaled x64 by cell count"}
+
+    vc = statistics.mean(st["inner_iters"] for st in stats)
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "s/solve", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": value * 1e3 * world, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 V-cycle / bf16 coarse corrections / f64 refinement", "data": "synthetic",
+            "config": {"workload": f"3D {n}^3 Brinkman-Stokes solve to FP64 rel. residual {TOL:g}, mixed precision",
+                       "n": n, "method": "mixed", "tol": TOL, "bc": "parabolic inlet N/4 patch, mirrored outlet",
+                       "density": "seeded U[0,1], Gaussian sigma 4, filter r 1.5, BP alpha amax 1e4",
+                       "l2": "inputs larger than L2 (~25 GB working set)", "parallelism": f"replicas x{world}"},
+            "e2e": {"value": e2e_value, "unit": "s/solve", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "gpu_launches": launches,
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                         "frac": round(achieved / peak, 4), "peak_source": peak_kind,
+                         "traffic": traffic, "algorithmic_bytes_per_launch": d["bytes"] / d["launches"]},
+            "cpu_baseline": cpu,
+            "clocks": clocks,
+            "solver": {"v_cycles_per_solve": vc, "outer_per_solve": statistics.mean(st["outer_iters"] for st in stats),
+                       "final_rel_residual_max": max(st["rel_residual"] for st in stats),
+                       "plain_s_per_solve": plain, "plain_v_cycles": plain_vc if plain else None},
+            "kernels": kernel_table,
+        }
+        print(json.dumps(line), flush=True)
+    s.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -68,20 +68,27 @@ __global__ void __launch_bounds__(TPB) k_axpy_multi_32to64(long long n4, Tab z, 
     }
 }
 
-template <int NV>
+// Per-thread partial sums are FP32 (a thread covers a few hundred products; GB300's FP64
+// pipe cannot keep up with HBM for these streams); block and grid sums are FP64.
+// With WW the pass also returns <w, w> in column NV.
+template <int NV, bool WW>
 __global__ void __launch_bounds__(TPB) k_multidot32(long long n4, Tab v, const float4* __restrict__ w, double* __restrict__ part) {
-    double acc[NV];
+    float acc[NV + 1];
 #pragma unroll
-    for (int q = 0; q < NV; q++) acc[q] = 0;
+    for (int q = 0; q <= NV; q++) acc[q] = 0.f;
     for (long long t = (long long)blockIdx.x * TPB + threadIdx.x; t < n4; t += (long long)gridDim.x * TPB) {
         float4 a = __ldg(w + t);
 #pragma unroll
         for (int q = 0; q < NV; q++) {
             float4 b = __ldg(v.p[q] + t);
-            acc[q] += (double)a.x * b.x + (double)a.y * b.y + (double)a.z * b.z + (double)a.w * b.w;
+            acc[q] += a.x * b.x + a.y * b.y + a.z * b.z + a.w * b.w;
         }
+        if (WW) acc[NV] += a.x * a.x + a.y * a.y + a.z * a.z + a.w * a.w;
     }
-    block_sums<NV>(acc, part + (long long)blockIdx.x * MAXV);
+    double d[NV + 1];
+#pragma unroll
+    for (int q = 0; q <= NV; q++) d[q] = acc[q];
+    block_sums<NV + 1>(d, part + (long long)blockIdx.x * (MAXV + 1));
 }
 
 // w -= sum_q h[q] v_q ; partial ||w||^2 per block (computed after the update)
@@ -91,7 +98,7 @@ __global__ void __launch_bounds__(TPB) k_multiaxpy32(long long n4, Tab v, const 
     float c[NV];
 #pragma unroll
     for (int q = 0; q < NV; q++) c[q] = (float)h[q];
-    double acc[1] = {0.0};
+    float accf = 0.f;
     for (long long t = (long long)blockIdx.x * TPB + threadIdx.x; t < n4; t += (long long)gridDim.x * TPB) {
         float4 a = w[t];
 #pragma unroll
@@ -103,8 +110,9 @@ __global__ void __launch_bounds__(TPB) k_multiaxpy32(long long n4, Tab v, const 
             a.w -= c[q] * b.w;
         }
         w[t] = a;
-        if (want_norm) acc[0] += (double)a.x * a.x + (double)a.y * a.y + (double)a.z * a.z + (double)a.w * a.w;
+        if (want_norm) accf += a.x * a.x + a.y * a.y + a.z * a.z + a.w * a.w;
     }
+    double acc[1] = {(double)accf};
     if (want_norm) block_sums<1>(acc, part + blockIdx.x);
 }
 
@@ -202,29 +210,38 @@ int axpy_multi_32to64(cudaStream_t st, long long n4, const float4* const* z, con
 }
 
 template <int NV>
-static void launch_dot(cudaStream_t st, long long n4, const Tab& t, const float4* w, double* part) {
-    k_multidot32<NV><<<rgrid(n4), TPB, 0, st>>>(n4, t, w, part);
+static void launch_dot(cudaStream_t st, long long n4, const Tab& t, const float4* w, double* part, bool ww) {
+    if (ww)
+        k_multidot32<NV, true><<<rgrid(n4), TPB, 0, st>>>(n4, t, w, part);
+    else
+        k_multidot32<NV, false><<<rgrid(n4), TPB, 0, st>>>(n4, t, w, part);
 }
 
-int multidot32(cudaStream_t st, long long n4, const float4* const* v, int nv, const float4* w, double* h, double* scratch) {
+int multidot32(cudaStream_t st, long long n4, const float4* const* v, int nv, const float4* w, double* h, double* scratch,
+               double* ww) {
     unsigned g = rgrid(n4);
     for (int j0 = 0; j0 < nv; j0 += MAXV) {
         int nb = nv - j0 < MAXV ? nv - j0 : MAXV;
+        bool want_ww = ww && j0 == 0;
         Tab t{};
         for (int q = 0; q < nb; q++) t.p[q] = v[j0 + q];
         switch (nb) {
-            case 1: launch_dot<1>(st, n4, t, w, scratch); break;
-            case 2: launch_dot<2>(st, n4, t, w, scratch); break;
-            case 3: launch_dot<3>(st, n4, t, w, scratch); break;
-            case 4: launch_dot<4>(st, n4, t, w, scratch); break;
-            case 5: launch_dot<5>(st, n4, t, w, scratch); break;
-            case 6: launch_dot<6>(st, n4, t, w, scratch); break;
-            case 7: launch_dot<7>(st, n4, t, w, scratch); break;
-            default: launch_dot<8>(st, n4, t, w, scratch); break;
+            case 1: launch_dot<1>(st, n4, t, w, scratch, want_ww); break;
+            case 2: launch_dot<2>(st, n4, t, w, scratch, want_ww); break;
+            case 3: launch_dot<3>(st, n4, t, w, scratch, want_ww); break;
+            case 4: launch_dot<4>(st, n4, t, w, scratch, want_ww); break;
+            case 5: launch_dot<5>(st, n4, t, w, scratch, want_ww); break;
+            case 6: launch_dot<6>(st, n4, t, w, scratch, want_ww); break;
+            case 7: launch_dot<7>(st, n4, t, w, scratch, want_ww); break;
+            default: launch_dot<8>(st, n4, t, w, scratch, want_ww); break;
         }
         STG_LAUNCH_CK();
-        k_reduce_cols<<<1, TPB, 0, st>>>(scratch, (int)g, MAXV, nb, h + j0);
+        k_reduce_cols<<<1, TPB, 0, st>>>(scratch, (int)g, MAXV + 1, nb, h + j0);
         STG_LAUNCH_CK();
+        if (want_ww) {
+            k_reduce_cols<<<1, TPB, 0, st>>>(scratch + nb, (int)g, MAXV + 1, 1, ww);
+            STG_LAUNCH_CK();
+        }
     }
     return STG_OK;
 }

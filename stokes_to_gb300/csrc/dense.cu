@@ -7,8 +7,9 @@
 // entries are never recorded (as in the reference); with `closed` the pressure block
 // gets +1 everywhere (:605-608). Unknowns that exist only as padding in the reference
 // layout are identity rows decoupled from the rest, so the dense system here keeps the
-// unknowns that exist. It is LU-factorised with partial pivoting (getrf semantics),
-// inverted once per set-up, and applied as a GEMV inside each V-cycle.
+// unknowns that exist. It is inverted once per set-up by Gauss-Jordan elimination with
+// partial pivoting on [A | I] (one grid-wide kernel per pivot, double-buffered in L2), and
+// the inverse is applied as a GEMV inside each V-cycle.
 #include <vector>
 
 #include "kernels.h"
@@ -95,111 +96,82 @@ __global__ void k_scatter(Geom g, int kind, int flag, int nd, const int* __restr
     }
     int col = dense_of[4 * g.slot(ci, cj, ck) + cc];
     if (col < 0) return;
-    A[row + (long long)col * nd] = val;
+    A[(long long)row * 2 * nd + col] = val;
 }
 
 __global__ void k_closed(int nd, const int* __restrict__ comp_of, double* __restrict__ A) {
     long long t = (long long)blockIdx.x * TPB + threadIdx.x;
     if (t >= (long long)nd * nd) return;
-    int row = (int)(t % nd), col = (int)(t / nd);
-    if (comp_of[row] == 0 && comp_of[col] == 0) A[t] += 1.0;
+    int row = (int)(t / nd), col = (int)(t % nd);
+    if (comp_of[row] == 0 && comp_of[col] == 0) A[(long long)row * 2 * nd + col] += 1.0;
 }
 
-// Single-CTA right-looking LU with partial pivoting (first maximal |a| wins, as idamax).
-constexpr int LU_T = 1024;
-__global__ void __launch_bounds__(LU_T) k_lu(int nd, double* __restrict__ A, int* __restrict__ piv, int* __restrict__ info) {
-    __shared__ double sv[LU_T / 32];
-    __shared__ int si[LU_T / 32];
+// [A | I]: zero the left half (filled by the probes), identity on the right half
+__global__ void k_aug_init(int nd, double* __restrict__ A) {
+    long long t = (long long)blockIdx.x * TPB + threadIdx.x;
+    if (t >= 2ll * nd * nd) return;
+    int row = (int)(t / (2 * nd)), col = (int)(t % (2 * nd));
+    A[t] = (col >= nd && col - nd == row) ? 1.0 : 0.0;
+}
+
+// One Gauss-Jordan pivot step on the row-major nd x 2nd matrix: every block finds the
+// pivot of column k among rows k..nd-1 (largest |a|, first on ties, as LAPACK), then
+// rewrites its rows into the other buffer: row k <- row p / a_pk, row p <- row k - a_kk
+// row k', other rows i <- row i - a_ik row k'. Block b handles row b.
+__global__ void __launch_bounds__(TPB) k_gj_step(int nd, int k, const double* __restrict__ in, double* __restrict__ out,
+                                                 int* __restrict__ info) {
+    __shared__ double sv[TPB / 32];
+    __shared__ int si[TPB / 32];
     __shared__ int sp;
-    if (threadIdx.x == 0) *info = 0;
-    for (int jc = 0; jc < nd; jc++) {
-        double best = -1.0;
-        int bi = nd;
-        for (int r = jc + threadIdx.x; r < nd; r += LU_T) {
-            double a = fabs(A[r + (long long)jc * nd]);
-            if (a > best || (a == best && r < bi)) {
-                best = a;
-                bi = r;
-            }
+    const int W = 2 * nd;
+    double best = -1.0;
+    int bi = nd;
+    for (int r = k + threadIdx.x; r < nd; r += TPB) {
+        double a = fabs(in[(long long)r * W + k]);
+        if (a > best || (a == best && r < bi)) {
+            best = a;
+            bi = r;
         }
-        for (int o = 16; o > 0; o >>= 1) {
-            double ob = __shfl_xor_sync(0xffffffffu, best, o);
-            int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-            if (ob > best || (ob == best && oi < bi)) {
-                best = ob;
-                bi = oi;
-            }
-        }
-        if ((threadIdx.x & 31) == 0) {
-            sv[threadIdx.x >> 5] = best;
-            si[threadIdx.x >> 5] = bi;
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            double b = -1.0;
-            int ii = nd;
-            for (int w = 0; w < LU_T / 32; w++)
-                if (sv[w] > b || (sv[w] == b && si[w] < ii)) {
-                    b = sv[w];
-                    ii = si[w];
-                }
-            sp = ii;
-            piv[jc] = ii;
-            if (A[ii + (long long)jc * nd] == 0.0 && *info == 0) *info = jc + 1;
-        }
-        __syncthreads();
-        int p = sp;
-        if (p != jc)
-            for (int c = threadIdx.x; c < nd; c += LU_T) {
-                double t0 = A[jc + (long long)c * nd];
-                A[jc + (long long)c * nd] = A[p + (long long)c * nd];
-                A[p + (long long)c * nd] = t0;
-            }
-        __syncthreads();
-        double d = A[jc + (long long)jc * nd];
-        if (d != 0.0) {
-            double inv = 1.0 / d;
-            for (int r = jc + 1 + threadIdx.x; r < nd; r += LU_T) A[r + (long long)jc * nd] *= inv;
-        }
-        __syncthreads();
-        int m = nd - jc - 1;
-        if (d != 0.0)
-            for (long long e = threadIdx.x; e < (long long)m * m; e += LU_T) {
-                int r = jc + 1 + (int)(e % m), c = jc + 1 + (int)(e / m);
-                A[r + (long long)c * nd] -= A[r + (long long)jc * nd] * A[jc + (long long)c * nd];
-            }
-        __syncthreads();
     }
-}
-
-// Column c of the inverse from the LU factors; written row-major (Ainv[row*nd + c]).
-__global__ void k_inverse(int nd, const double* __restrict__ LU, const int* __restrict__ piv, double* __restrict__ Ainv,
-                          double* __restrict__ work) {
-    int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= nd) return;
-    // x[r] lives at work[r*nd + c]: consecutive threads touch consecutive addresses
-#define XR(r) work[(long long)(r) * nd + c]
-    for (int r = 0; r < nd; r++) XR(r) = (r == c) ? 1.0 : 0.0;
-    for (int r = 0; r < nd; r++)
-        if (piv[r] != r) {
-            double t = XR(r);
-            XR(r) = XR(piv[r]);
-            XR(piv[r]) = t;
+    for (int o = 16; o > 0; o >>= 1) {
+        double ob = __shfl_xor_sync(0xffffffffu, best, o);
+        int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+        if (ob > best || (ob == best && oi < bi)) {
+            best = ob;
+            bi = oi;
         }
-    for (int q = 0; q < nd; q++) {
-        double xq = XR(q);
-        if (xq != 0.0)
-            for (int r = q + 1; r < nd; r++) XR(r) -= LU[r + (long long)q * nd] * xq;
     }
-    for (int q = nd - 1; q >= 0; q--) {
-        double dq = LU[q + (long long)q * nd];
-        double xq = dq != 0.0 ? XR(q) / dq : 0.0;
-        XR(q) = xq;
-        if (xq != 0.0)
-            for (int r = 0; r < q; r++) XR(r) -= LU[r + (long long)q * nd] * xq;
+    if ((threadIdx.x & 31) == 0) {
+        sv[threadIdx.x >> 5] = best;
+        si[threadIdx.x >> 5] = bi;
     }
-    for (int r = 0; r < nd; r++) Ainv[(long long)r * nd + c] = XR(r);
-#undef XR
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double b = -1.0;
+        int ii = nd;
+        for (int w = 0; w < TPB / 32; w++)
+            if (sv[w] > b || (sv[w] == b && si[w] < ii)) {
+                b = sv[w];
+                ii = si[w];
+            }
+        sp = ii;
+    }
+    __syncthreads();
+    const int p = sp;
+    const int row = blockIdx.x;
+    const double piv = in[(long long)p * W + k];
+    if (piv == 0.0) {
+        if (row == 0 && threadIdx.x == 0 && *info == 0) *info = k + 1;
+        for (int c = threadIdx.x; c < W; c += TPB) out[(long long)row * W + c] = in[(long long)row * W + c];
+        return;
+    }
+    const double inv = 1.0 / piv;
+    const int src = row == k ? p : (row == p ? k : row);
+    const double f = row == k ? 0.0 : in[(long long)src * W + k];
+    for (int c = threadIdx.x; c < W; c += TPB) {
+        double pr = in[(long long)p * W + c] * inv;
+        out[(long long)row * W + c] = row == k ? pr : in[(long long)src * W + c] - f * pr;
+    }
 }
 
 template <class V>
@@ -222,13 +194,13 @@ __global__ void k_gather(int nd, const int* __restrict__ slot_of, const int* __r
 
 // one warp per row: x[row] = sum_c Ainv[row, c] rd[c], scattered into the slot vector
 template <class T>
-__global__ void k_gemv(int nd, const double* __restrict__ Ainv, const double* __restrict__ rd, const int* __restrict__ slot_of,
-                       const int* __restrict__ comp_of, T* __restrict__ x) {
+__global__ void k_gemv(int nd, const double* __restrict__ Ainv, int ld, const double* __restrict__ rd,
+                       const int* __restrict__ slot_of, const int* __restrict__ comp_of, T* __restrict__ x) {
     int row = (blockIdx.x * TPB + threadIdx.x) >> 5;
     int lane = threadIdx.x & 31;
     if (row >= nd) return;
     double s = 0;
-    for (int c = lane; c < nd; c += 32) s += Ainv[(long long)row * nd + c] * rd[c];
+    for (int c = lane; c < nd; c += 32) s += Ainv[(long long)row * ld + c] * rd[c];
     for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
     if (lane == 0) x[4ll * slot_of[row] + comp_of[row]] = (T)s;
 }
@@ -255,13 +227,12 @@ int dense_init(DenseCoarse& D, const Geom& g) {
     STG_CK(cudaMalloc(&D.slot_of, sizeof(int) * nd));
     STG_CK(cudaMalloc(&D.comp_of, sizeof(int) * nd));
     STG_CK(cudaMalloc(&D.dense_of, sizeof(int) * dense_of.size()));
-    STG_CK(cudaMalloc(&D.A, sizeof(double) * nd * nd));
-    STG_CK(cudaMalloc(&D.Ainv, sizeof(double) * nd * nd));
+    STG_CK(cudaMalloc(&D.A, sizeof(double) * 2 * nd * nd));
+    STG_CK(cudaMalloc(&D.Ainv, sizeof(double) * 2 * nd * nd));
     STG_CK(cudaMalloc(&D.piv, sizeof(int) * nd));
     STG_CK(cudaMalloc(&D.info, sizeof(int)));
     STG_CK(cudaMalloc(&D.probe, sizeof(d4) * g.nslot));
     STG_CK(cudaMalloc(&D.image, sizeof(d4) * g.nslot));
-    STG_CK(cudaMalloc(&D.work, sizeof(double) * nd * nd));
     STG_CK(cudaMalloc(&D.rd, sizeof(double) * nd));
     STG_CK(cudaMemcpy(D.slot_of, slot_of.data(), sizeof(int) * nd, cudaMemcpyHostToDevice));
     STG_CK(cudaMemcpy(D.comp_of, comp_of.data(), sizeof(int) * nd, cudaMemcpyHostToDevice));
@@ -281,14 +252,14 @@ void dense_free(DenseCoarse& D) {
     cudaFree(D.info);
     cudaFree(D.probe);
     cudaFree(D.image);
-    cudaFree(D.work);
     cudaFree(D.rd);
     D = DenseCoarse();
 }
 
 int dense_setup(cudaStream_t st, DenseCoarse& D, const Geom& g, double vol, const uint8_t* m, const d4* P64, int closed) {
     const int nd = D.nd;
-    STG_CK(cudaMemsetAsync(D.A, 0, sizeof(double) * nd * nd, st));
+    k_aug_init<<<grid_for(2ll * nd * nd, TPB), TPB, 0, st>>>(nd, D.A);
+    STG_LAUNCH_CK();
     for (int kind = 0; kind < 2; kind++) {
         int nflags = kind == 0 ? 2 : 7;
         for (int f = 0; f < nflags; f++) {
@@ -303,10 +274,16 @@ int dense_setup(cudaStream_t st, DenseCoarse& D, const Geom& g, double vol, cons
         k_closed<<<grid_for((long long)nd * nd, TPB), TPB, 0, st>>>(nd, D.comp_of, D.A);
         STG_LAUNCH_CK();
     }
-    k_lu<<<1, LU_T, 0, st>>>(nd, D.A, D.piv, D.info);
-    STG_LAUNCH_CK();
-    k_inverse<<<grid_for(nd, 64), 64, 0, st>>>(nd, D.A, D.piv, D.Ainv, D.work);
-    STG_LAUNCH_CK();
+    STG_CK(cudaMemsetAsync(D.info, 0, sizeof(int), st));
+    double *a = D.A, *b = D.Ainv;
+    for (int k = 0; k < nd; k++) {
+        k_gj_step<<<nd, TPB, 0, st>>>(nd, k, a, b, D.info);
+        STG_LAUNCH_CK();
+        double* t = a;
+        a = b;
+        b = t;
+    }
+    D.inv = a + nd;  // right half of the final buffer, row stride 2 nd
     return STG_OK;
 }
 
@@ -315,7 +292,7 @@ int dense_apply32(cudaStream_t st, const DenseCoarse& D, const Geom& g, const fl
     k_gather<float4><<<grid_for(D.nd, TPB), TPB, 0, st>>>(D.nd, D.slot_of, D.comp_of, r, rd);
     STG_LAUNCH_CK();
     STG_CK(cudaMemsetAsync(x, 0, sizeof(float4) * g.nslot, st));
-    k_gemv<float><<<grid_for(32ll * D.nd, TPB), TPB, 0, st>>>(D.nd, D.Ainv, rd, D.slot_of, D.comp_of,
+    k_gemv<float><<<grid_for(32ll * D.nd, TPB), TPB, 0, st>>>(D.nd, D.inv, 2 * D.nd, rd, D.slot_of, D.comp_of,
                                                               reinterpret_cast<float*>(x));
     STG_LAUNCH_CK();
     return STG_OK;
@@ -326,7 +303,7 @@ int dense_apply64(cudaStream_t st, const DenseCoarse& D, const Geom& g, const d4
     k_gather<d4><<<grid_for(D.nd, TPB), TPB, 0, st>>>(D.nd, D.slot_of, D.comp_of, r, rd);
     STG_LAUNCH_CK();
     STG_CK(cudaMemsetAsync(x, 0, sizeof(d4) * g.nslot, st));
-    k_gemv<double><<<grid_for(32ll * D.nd, TPB), TPB, 0, st>>>(D.nd, D.Ainv, rd, D.slot_of, D.comp_of,
+    k_gemv<double><<<grid_for(32ll * D.nd, TPB), TPB, 0, st>>>(D.nd, D.inv, 2 * D.nd, rd, D.slot_of, D.comp_of,
                                                                 reinterpret_cast<double*>(x));
     STG_LAUNCH_CK();
     return STG_OK;

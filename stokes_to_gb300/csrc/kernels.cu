@@ -94,23 +94,18 @@ __global__ void __launch_bounds__(TPB) k_op32(Geom g, float vol, const float4* _
 //               a = 2 (P_p + F_p)  (the pressure diagonal is counted by both masks)
 // and is solved exactly by its Schur complement. (If the complement is 0 the
 // reference's LU has a zero pivot; this kernel leaves the pressure unchanged there.)
-struct Blk {
-    float dp;
-    float dL[3], dR[3];
-};
-
-__device__ __forceinline__ Blk vanka_block(const float4* __restrict__ rr, const uint8_t* __restrict__ m,
-                                           const float4* __restrict__ P, int c, int di, int dj, float vol) {
+// Pressure update of the arrow block of red cell c (its Schur-complement equation).
+__device__ __forceinline__ float vanka_dp(const float4* __restrict__ rr, const uint8_t* __restrict__ m,
+                                          const float4* __restrict__ P, int c, int di, int dj, float vol) {
     const int off[3] = {di, dj, 1};
+    const uint8_t bit[3] = {MU, MV, MW};
     float4 rc = __ldg(rr + c);
     float4 pc = __ldg(P + c);
     uint8_t m0 = __ldg(m + c);
-    const float fc = (m0 & MP) ? 0.f : 1.f;
+    if (m0 & MP) return rc.x / (2.f * (pc.x + 1.f));  // fixed cell: b = 0, a = 2 (P + 1)
     const float rL[3] = {rc.y, rc.z, rc.w};
     const float pL[3] = {pc.y, pc.z, pc.w};
-    const uint8_t bit[3] = {MU, MV, MW};
-    float DL[3], DR[3], cL[3], cR[3], rR[3];
-    float num = rc.x, den = 2.f * (pc.x + (1.f - fc));
+    float num = rc.x, den = 2.f * pc.x;
 #pragma unroll
     for (int d = 0; d < 3; d++) {
         uint8_t mlo = __ldg(m + c - off[d]);
@@ -121,53 +116,89 @@ __device__ __forceinline__ Blk vanka_block(const float4* __restrict__ rr, const 
         float phv = d == 0 ? ph.y : d == 1 ? ph.z : ph.w;
         bool fixL = m0 & bit[d], fixR = mhi & bit[d];
         float vL = fixL ? 0.f : vol, vR = fixR ? 0.f : vol;
-        float cmL = (mlo & MP) ? 0.f : 1.f, cmR = (mhi & MP) ? 0.f : 1.f;
-        DL[d] = vL * (4.f + fc + cmL) + pL[d] + (fixL ? 1.f : 0.f);
-        DR[d] = vR * (4.f + cmR + fc) + phv + (fixR ? 1.f : 0.f);
-        cL[d] = -vL;
-        cR[d] = vR;
-        rR[d] = rhv;
-        float bL = fc * cL[d], bR = fc * cR[d];
-        num -= bL * rL[d] / DL[d] + bR * rhv / DR[d];
-        den -= bL * cL[d] / DL[d] + bR * cR[d] / DR[d];
+        float DL = vL * (5.f + ((mlo & MP) ? 0.f : 1.f)) + pL[d] + (fixL ? 1.f : 0.f);
+        float DR = vR * (5.f + ((mhi & MP) ? 0.f : 1.f)) + phv + (fixR ? 1.f : 0.f);
+        // b_f = c_f = -vL (left), +vR (right) for a free cell
+        num -= (-vL) * rL[d] / DL + vR * rhv / DR;
+        den -= vL * vL / DL + vR * vR / DR;
     }
-    Blk b;
-    b.dp = den != 0.f ? num / den : 0.f;
-#pragma unroll
-    for (int d = 0; d < 3; d++) {
-        b.dL[d] = (rL[d] - cL[d] * b.dp) / DL[d];
-        b.dR[d] = (rR[d] - cR[d] * b.dp) / DR[d];
-    }
-    return b;
+    return den != 0.f ? num / den : 0.f;
 }
 
+// Tiled box-Vanka step. A block owns a 32 (k) x 8 (j) column of slots and marches along i
+// through VT_CHUNK planes. Per plane it first forms the pressure update of every red cell
+// of the plane over the tile plus a one-slot low halo in j and k (shared memory), then
+// every slot updates its own unknowns: its pressure if its cell is red, and each face
+// from the red cell that owns it (the cell itself, or its lower neighbour along the
+// face normal), with the face diagonal D_f formed from the slot's own coefficients.
+constexpr int VT_K = 32, VT_J = 8, VT_CHUNK = 16;
+
 template <bool HAS_X>
-__global__ void __launch_bounds__(TPB) k_vanka32(Geom g, float vol, const float4* __restrict__ rr,
-                                                 const float4* __restrict__ xin, float4* __restrict__ xout,
-                                                 const uint8_t* __restrict__ m, const float4* __restrict__ P, int flag) {
-    long long t = (long long)blockIdx.x * TPB + threadIdx.x;
-    if (t >= g.box()) return;
-    int i, j, k;
-    g.box_ijk(t, i, j, k);
+__global__ void __launch_bounds__(VT_K* VT_J) k_vanka_tiled(Geom g, float vol, const float4* __restrict__ rr,
+                                                          const float4* __restrict__ xin, float4* __restrict__ xout,
+                                                          const uint8_t* __restrict__ m, const float4* __restrict__ P,
+                                                          int flag) {
+    __shared__ float dp_cur[VT_J + 1][VT_K + 1];
+    __shared__ float dp_prev[VT_J][VT_K];
     const int n = g.n, di = g.di(), dj = g.dj();
-    int s = g.slot(i, j, k);
-    float4 xo = HAS_X ? __ldg(xin + s) : make_float4(0.f, 0.f, 0.f, 0.f);
-    if (cell_ok(n, i, j, k) && ((i + j + k + flag) & 1) == 0) {
-        Blk b = vanka_block(rr, m, P, s, di, dj, vol);
-        xo.x += b.dp;
-        xo.y += b.dL[0];
-        xo.z += b.dL[1];
-        xo.w += b.dL[2];
-    } else {
-        // faces of this slot that are the right faces of a red neighbour
-        if (i >= 1 && cell_ok(n, i - 1, j, k) && ((i - 1 + j + k + flag) & 1) == 0)
-            xo.y += vanka_block(rr, m, P, s - di, di, dj, vol).dR[0];
-        if (j >= 1 && cell_ok(n, i, j - 1, k) && ((i + j - 1 + k + flag) & 1) == 0)
-            xo.z += vanka_block(rr, m, P, s - dj, di, dj, vol).dR[1];
-        if (k >= 1 && cell_ok(n, i, j, k - 1) && ((i + j + k - 1 + flag) & 1) == 0)
-            xo.w += vanka_block(rr, m, P, s - 1, di, dj, vol).dR[2];
+    const int tk = threadIdx.x, tj = threadIdx.y, tid = tj * VT_K + tk;
+    const int k0 = blockIdx.x * VT_K, j0 = blockIdx.y * VT_J, i0 = blockIdx.z * VT_CHUNK;
+    const int i1 = min(i0 + VT_CHUNK, n + 1);
+    const int k = k0 + tk, j = j0 + tj;
+    const bool in_box = k <= n && j <= n;
+    // pressure updates of plane i0 - 1 (owners of the x-faces of plane i0)
+    {
+        int i = i0 - 1;
+        bool red = i >= 0 && cell_ok(n, i, j, k) && ((i + j + k + flag) & 1) == 0;
+        dp_prev[tj][tk] = red ? vanka_dp(rr, m, P, g.slot(i, j, k), di, dj, vol) : 0.f;
     }
-    xout[s] = xo;
+    for (int i = i0; i < i1; i++) {
+        for (int e = tid; e < (VT_J + 1) * (VT_K + 1); e += VT_K * VT_J) {
+            int jj = j0 - 1 + e / (VT_K + 1), kk = k0 - 1 + e % (VT_K + 1);
+            bool red = jj >= 0 && kk >= 0 && cell_ok(n, i, jj, kk) && ((i + jj + kk + flag) & 1) == 0;
+            dp_cur[e / (VT_K + 1)][e % (VT_K + 1)] = red ? vanka_dp(rr, m, P, g.slot(i, jj, kk), di, dj, vol) : 0.f;
+        }
+        __syncthreads();
+        if (in_box) {
+            int s = g.slot(i, j, k);
+            float4 r = __ldg(rr + s);
+            float4 pp = __ldg(P + s);
+            uint8_t m0 = __ldg(m + s);
+            float4 xo = HAS_X ? __ldg(xin + s) : make_float4(0.f, 0.f, 0.f, 0.f);
+            const bool own_red = cell_ok(n, i, j, k) && ((i + j + k + flag) & 1) == 0;
+            const float fc = (m0 & MP) ? 0.f : 1.f;
+            if (own_red) xo.x += dp_cur[tj + 1][tk + 1];
+            // faces: owner = this cell if red (left face, c_f = -vol), else the lower neighbour (right face, +vol)
+            const float rf[3] = {r.y, r.z, r.w};
+            const float pf[3] = {pp.y, pp.z, pp.w};
+            const uint8_t bit[3] = {MU, MV, MW};
+            const int offs[3] = {di, dj, 1};
+            float upd[3];
+#pragma unroll
+            for (int d = 0; d < 3; d++) {
+                upd[d] = 0.f;
+                int li = i - (d == 0), lj = j - (d == 1), lk = k - (d == 2);
+                bool lower_red = !own_red && li >= 0 && lj >= 0 && lk >= 0 && cell_ok(n, li, lj, lk) &&
+                                 ((li + lj + lk + flag) & 1) == 0;
+                if (!own_red && !lower_red) continue;
+                bool fix = m0 & bit[d];
+                float v = fix ? 0.f : vol;
+                uint8_t mlo = __ldg(m + s - offs[d]);
+                float D = v * (4.f + fc + ((mlo & MP) ? 0.f : 1.f)) + pf[d] + (fix ? 1.f : 0.f);
+                float dpo = own_red ? dp_cur[tj + 1][tk + 1]
+                                    : (d == 0 ? dp_prev[tj][tk] : d == 1 ? dp_cur[tj][tk + 1] : dp_cur[tj + 1][tk]);
+                float cf = own_red ? -v : v;
+                upd[d] = (rf[d] - cf * dpo) / D;
+            }
+            xo.y += upd[0];
+            xo.z += upd[1];
+            xo.w += upd[2];
+            xout[s] = xo;
+        }
+        __syncthreads();
+        dp_prev[tj][tk] = dp_cur[tj + 1][tk + 1];
+        __syncthreads();
+    }
 }
 
 // ------------------------------------------------------------------ transfers
@@ -509,11 +540,11 @@ int apply32(cudaStream_t st, const Geom& g, float vol, const float4* x, const ui
 
 int vanka32(cudaStream_t st, const Geom& g, float vol, const float4* rr, const float4* xin, float4* xout, const uint8_t* m,
             const float4* P, int flag) {
-    unsigned nb = grid_for(g.box(), TPB);
+    dim3 grid((g.n + VT_K) / VT_K, (g.n + VT_J) / VT_J, (g.n + VT_CHUNK) / VT_CHUNK), block(VT_K, VT_J);
     if (xin)
-        k_vanka32<true><<<nb, TPB, 0, st>>>(g, vol, rr, xin, xout, m, P, flag);
+        k_vanka_tiled<true><<<grid, block, 0, st>>>(g, vol, rr, xin, xout, m, P, flag);
     else
-        k_vanka32<false><<<nb, TPB, 0, st>>>(g, vol, rr, xin, xout, m, P, flag);
+        k_vanka_tiled<false><<<grid, block, 0, st>>>(g, vol, rr, xin, xout, m, P, flag);
     STG_LAUNCH_CK();
     return STG_OK;
 }

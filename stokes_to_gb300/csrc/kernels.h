@@ -61,12 +61,15 @@ int f64_to_f32(cudaStream_t st, long long n4, const d4* a, double scale, float4*
 int f32_to_f64(cudaStream_t st, long long n4, const float4* a, d4* out);
 // x64 += alpha * sum_j y[j] z[j]  (z FP32 vectors), y on device (nz entries)
 int axpy_multi_32to64(cudaStream_t st, long long n4, const float4* const* z, const double* y, int nz, double alpha, d4* x);
-// h[j] = <v_j, w> for j < nv  (FP64 accumulation), written to hpart then reduced into h
-int multidot32(cudaStream_t st, long long n4, const float4* const* v, int nv, const float4* w, double* h, double* scratch);
+// h[j] = <v_j, w> for j < nv (FP32 per-thread partials, FP64 block and grid sums),
+// and <w, w> into *ww when ww != nullptr
+
+int multidot32(cudaStream_t st, long long n4, const float4* const* v, int nv, const float4* w, double* h, double* scratch,
+               double* ww);
 // w -= sum_j h[j] v_j ; then returns ||w||^2 into nrm2 (device)
 int multiaxpy32_norm(cudaStream_t st, long long n4, const float4* const* v, int nv, const double* h, float4* w, double* nrm2,
                      double* scratch);
-// x *= s (s on device, s = 1/sqrt(*nrm2) if invsqrt)
+// out = x / sqrt(*nrm2)
 int scale32(cudaStream_t st, long long n4, float4* x, const double* nrm2, float4* out);
 // deterministic sum of nparts partials -> *out
 int reduce_parts(cudaStream_t st, const double* parts, int nparts, double* out);
@@ -78,13 +81,13 @@ struct DenseCoarse {
     int* slot_of = nullptr;    // dense index -> slot
     int* comp_of = nullptr;    // dense index -> 0 p, 1 u, 2 v, 3 w
     int* dense_of = nullptr;   // slot*4+comp -> dense index or -1
-    double* A = nullptr;       // nd x nd column-major; LU then inverse
+    double* A = nullptr;       // two row-major nd x 2nd buffers for Gauss-Jordan on [A | I]
     double* Ainv = nullptr;
+    const double* inv = nullptr;  // the inverse: right half of the final buffer, row stride 2 nd
     int* piv = nullptr;
     int* info = nullptr;
     d4* probe = nullptr;       // probe vector and its image (slots)
     d4* image = nullptr;
-    double* work = nullptr;    // nd x nd inversion work area
     double* rd = nullptr;      // gathered right-hand side (nd)
 };
 int dense_init(DenseCoarse& D, const Geom& g);

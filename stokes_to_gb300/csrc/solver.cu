@@ -319,24 +319,39 @@ int solve_core(stg_t* h, const d4* b, d4* x, stg_stats* stats) {
         // v0 = r / ||r|| in FP32
         PROF(h, 6, 48.0 * n4, f64_to_f32(h->st, n4, h->r64, 1.0 / rn, h->V[0]));
         double beta = 1.0;
+        // ask this step for what the target still needs, within [inner_tol / 10, inner_tol]
+        const double itol = std::min(h->opts.inner_tol, std::max(0.3 * h->opts.tol / rel, 0.1 * h->opts.inner_tol));
         std::fill(g.begin(), g.end(), 0.0);
         g[0] = beta;
         int k = 0;
         for (int j = 0; j < m; j++) {
-            STG_TRY(vcycle(h, h->V[j]));
-            STG_CK(cudaMemcpyAsync(h->Z[j], F.x(), sizeof(float4) * n4, cudaMemcpyDeviceToDevice, h->st));
+            // the V-cycle leaves its result in the finest level's second buffer: point it at Z[j]
+            float4* keep = F.xb;
+            F.xb = h->Z[j];
+            int vrc = vcycle(h, h->V[j]);
+            float4* res = F.x();
+            F.xb = keep;
+            STG_TRY(vrc);
+            if (res != h->Z[j]) STG_CK(cudaMemcpyAsync(h->Z[j], res, sizeof(float4) * n4, cudaMemcpyDeviceToDevice, h->st));
             PROF(h, 4, 49.0 * F.g.box(), apply32(h->st, F.g, (float)F.vol, h->Z[j], F.m, F.P32, h->w));
-            PROF(h, 6, 16.0 * (j + 2) * n4, multidot32(h->st, n4, h->V.data(), j + 1, h->w, h->dh, h->dscr));
+            // classical Gram-Schmidt; a second pass only when the first one cancelled most
+            // of w (||w_new|| < 0.7 ||w||, "twice is enough")
+            PROF(h, 6, 16.0 * (j + 2) * n4, multidot32(h->st, n4, h->V.data(), j + 1, h->w, h->dh, h->dscr, h->dnrm + 1));
             PROF(h, 6, 16.0 * (j + 3) * n4, multiaxpy32_norm(h->st, n4, h->V.data(), j + 1, h->dh, h->w, h->dnrm, h->dscr));
-            // second classical Gram-Schmidt pass (CGS2): keeps the FP32 basis orthogonal
-            PROF(h, 6, 16.0 * (j + 2) * n4, multidot32(h->st, n4, h->V.data(), j + 1, h->w, h->dh + m + 2, h->dscr));
-            PROF(h, 6, 16.0 * (j + 3) * n4, multiaxpy32_norm(h->st, n4, h->V.data(), j + 1, h->dh + m + 2, h->w, h->dnrm, h->dscr));
-            std::vector<double> h1(j + 1), h2(j + 1);
-            double nw2 = 0;
+            std::vector<double> h1(j + 1), h2(j + 1, 0.0);
+            double nrm[2] = {0, 0};
             STG_CK(cudaMemcpyAsync(h1.data(), h->dh, sizeof(double) * (j + 1), cudaMemcpyDeviceToHost, h->st));
-            STG_CK(cudaMemcpyAsync(h2.data(), h->dh + m + 2, sizeof(double) * (j + 1), cudaMemcpyDeviceToHost, h->st));
-            STG_CK(cudaMemcpyAsync(&nw2, h->dnrm, sizeof(double), cudaMemcpyDeviceToHost, h->st));
+            STG_CK(cudaMemcpyAsync(nrm, h->dnrm, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->st));
             STG_CK(cudaStreamSynchronize(h->st));
+            double nw2 = nrm[0];
+            if (nrm[0] < 0.49 * nrm[1]) {
+                PROF(h, 6, 16.0 * (j + 2) * n4, multidot32(h->st, n4, h->V.data(), j + 1, h->w, h->dh + m + 2, h->dscr, nullptr));
+                PROF(h, 6, 16.0 * (j + 3) * n4,
+                     multiaxpy32_norm(h->st, n4, h->V.data(), j + 1, h->dh + m + 2, h->w, h->dnrm, h->dscr));
+                STG_CK(cudaMemcpyAsync(h2.data(), h->dh + m + 2, sizeof(double) * (j + 1), cudaMemcpyDeviceToHost, h->st));
+                STG_CK(cudaMemcpyAsync(&nw2, h->dnrm, sizeof(double), cudaMemcpyDeviceToHost, h->st));
+                STG_CK(cudaStreamSynchronize(h->st));
+            }
             S.inner_iters++;
             double hn = std::sqrt(nw2);
             for (int q = 0; q <= j; q++) hcol[q] = h1[q] + h2[q];
@@ -365,7 +380,7 @@ int solve_core(stg_t* h, const d4* b, d4* x, stg_stats* stats) {
             k = j + 1;
             double est = std::fabs(g[j + 1]);
             if (h->opts.verbose > 1) fprintf(stderr, "[stg]   inner %d  est %.3e\n", j, est);
-            if (est <= h->opts.inner_tol * beta || hn == 0.0) break;
+            if (est <= itol * beta || hn == 0.0) break;
         }
         if (status == STG_E_NONFINITE) break;
         for (int q = k - 1; q >= 0; q--) {
@@ -530,7 +545,7 @@ int stg_create(int dim, int n, const stg_opts* opts, stg_t** out) {
         if ((rc = dalloc(&p, ns))) return fail(rc);
     for (auto& p : h->Z)
         if ((rc = dalloc(&p, ns))) return fail(rc);
-    if ((rc = dalloc(&h->dscr, 1216 * 8)) || (rc = dalloc(&h->dh, 2 * (h->m + 2))) || (rc = dalloc(&h->dnrm, 4)) ||
+    if ((rc = dalloc(&h->dscr, 1216 * 16)) || (rc = dalloc(&h->dh, 2 * (h->m + 2))) || (rc = dalloc(&h->dnrm, 8)) ||
         (rc = dalloc(&h->dy, h->m + 1)) || (rc = dalloc(&h->d_parts, (size_t)grid_for(F.g.box(), 256) + 1216)))
         return fail(rc);
     h->ncell = (size_t)n * n * n;
