@@ -1,6 +1,6 @@
-// Grid kernels of the multigrid hierarchy: FP64/FP32 operator and residual, the
-// colored box-Vanka block update, fused residual + restriction, prolongation,
-// coarse re-discretisation and layout conversions.
+// Grid kernels of the multigrid hierarchy: FP64/FP32 operator and residual, fused
+// residual + restriction, prolongation, coarse re-discretisation and layout conversions.
+// (The smoothing sweep lives in sweep.cu.)
 #include <cuda_bf16.h>
 
 #include "kernels.h"
@@ -80,124 +80,6 @@ __global__ void __launch_bounds__(TPB) k_op32(Geom g, float vol, const float4* _
         out[s] = make_float4(rv.x - o[0], rv.y - o[1], rv.z - o[2], rv.w - o[3]);
     } else {
         out[s] = make_float4(o[0], o[1], o[2], o[3]);
-    }
-}
-
-// ------------------------------------------------------------------ box-Vanka
-// Block of red cell c (7 unknowns: the six faces and the pressure), as extracted by
-// DirectSolveBlockInverse<7> from B = M_w A M_w + M_b A M_b (stoke/StokeLike.cu:41-96,
-// 345-372). With one vol value on the free faces and no fixed cell, the face-face
-// couplings of B inside a block cancel (grad-div against curl-curl) and B's couplings to
-// other red blocks vanish, so the block is an arrow matrix:
-//   face rows   D_f u_f + c_f p = r_f ,  D_f = vol*free_f*(4 + free_cell(left) + free_cell(right)) + P_f + F_f
-//   pressure    sum_f b_f u_f + a p = r_p,  c_f = -/+ vol*free_f (left/right face), b_f = free_c * c_f,
-//               a = 2 (P_p + F_p)  (the pressure diagonal is counted by both masks)
-// and is solved exactly by its Schur complement. (If the complement is 0 the
-// reference's LU has a zero pivot; this kernel leaves the pressure unchanged there.)
-// Pressure update of the arrow block of red cell c (its Schur-complement equation).
-__device__ __forceinline__ float vanka_dp(const float4* __restrict__ rr, const uint8_t* __restrict__ m,
-                                          const float4* __restrict__ P, int c, int di, int dj, float vol) {
-    const int off[3] = {di, dj, 1};
-    const uint8_t bit[3] = {MU, MV, MW};
-    float4 rc = __ldg(rr + c);
-    float4 pc = __ldg(P + c);
-    uint8_t m0 = __ldg(m + c);
-    if (m0 & MP) return rc.x / (2.f * (pc.x + 1.f));  // fixed cell: b = 0, a = 2 (P + 1)
-    const float rL[3] = {rc.y, rc.z, rc.w};
-    const float pL[3] = {pc.y, pc.z, pc.w};
-    float num = rc.x, den = 2.f * pc.x;
-#pragma unroll
-    for (int d = 0; d < 3; d++) {
-        uint8_t mlo = __ldg(m + c - off[d]);
-        uint8_t mhi = __ldg(m + c + off[d]);
-        float4 rh = __ldg(rr + c + off[d]);
-        float4 ph = __ldg(P + c + off[d]);
-        float rhv = d == 0 ? rh.y : d == 1 ? rh.z : rh.w;
-        float phv = d == 0 ? ph.y : d == 1 ? ph.z : ph.w;
-        bool fixL = m0 & bit[d], fixR = mhi & bit[d];
-        float vL = fixL ? 0.f : vol, vR = fixR ? 0.f : vol;
-        float DL = vL * (5.f + ((mlo & MP) ? 0.f : 1.f)) + pL[d] + (fixL ? 1.f : 0.f);
-        float DR = vR * (5.f + ((mhi & MP) ? 0.f : 1.f)) + phv + (fixR ? 1.f : 0.f);
-        // b_f = c_f = -vL (left), +vR (right) for a free cell
-        num -= (-vL) * rL[d] / DL + vR * rhv / DR;
-        den -= vL * vL / DL + vR * vR / DR;
-    }
-    return den != 0.f ? num / den : 0.f;
-}
-
-// Tiled box-Vanka step. A block owns a 32 (k) x 8 (j) column of slots and marches along i
-// through VT_CHUNK planes. Per plane it first forms the pressure update of every red cell
-// of the plane over the tile plus a one-slot low halo in j and k (shared memory), then
-// every slot updates its own unknowns: its pressure if its cell is red, and each face
-// from the red cell that owns it (the cell itself, or its lower neighbour along the
-// face normal), with the face diagonal D_f formed from the slot's own coefficients.
-constexpr int VT_K = 32, VT_J = 8, VT_CHUNK = 16;
-
-template <bool HAS_X>
-__global__ void __launch_bounds__(VT_K* VT_J) k_vanka_tiled(Geom g, float vol, const float4* __restrict__ rr,
-                                                          const float4* __restrict__ xin, float4* __restrict__ xout,
-                                                          const uint8_t* __restrict__ m, const float4* __restrict__ P,
-                                                          int flag) {
-    __shared__ float dp_cur[VT_J + 1][VT_K + 1];
-    __shared__ float dp_prev[VT_J][VT_K];
-    const int n = g.n, di = g.di(), dj = g.dj();
-    const int tk = threadIdx.x, tj = threadIdx.y, tid = tj * VT_K + tk;
-    const int k0 = blockIdx.x * VT_K, j0 = blockIdx.y * VT_J, i0 = blockIdx.z * VT_CHUNK;
-    const int i1 = min(i0 + VT_CHUNK, n + 1);
-    const int k = k0 + tk, j = j0 + tj;
-    const bool in_box = k <= n && j <= n;
-    // pressure updates of plane i0 - 1 (owners of the x-faces of plane i0)
-    {
-        int i = i0 - 1;
-        bool red = i >= 0 && cell_ok(n, i, j, k) && ((i + j + k + flag) & 1) == 0;
-        dp_prev[tj][tk] = red ? vanka_dp(rr, m, P, g.slot(i, j, k), di, dj, vol) : 0.f;
-    }
-    for (int i = i0; i < i1; i++) {
-        for (int e = tid; e < (VT_J + 1) * (VT_K + 1); e += VT_K * VT_J) {
-            int jj = j0 - 1 + e / (VT_K + 1), kk = k0 - 1 + e % (VT_K + 1);
-            bool red = jj >= 0 && kk >= 0 && cell_ok(n, i, jj, kk) && ((i + jj + kk + flag) & 1) == 0;
-            dp_cur[e / (VT_K + 1)][e % (VT_K + 1)] = red ? vanka_dp(rr, m, P, g.slot(i, jj, kk), di, dj, vol) : 0.f;
-        }
-        __syncthreads();
-        if (in_box) {
-            int s = g.slot(i, j, k);
-            float4 r = __ldg(rr + s);
-            float4 pp = __ldg(P + s);
-            uint8_t m0 = __ldg(m + s);
-            float4 xo = HAS_X ? __ldg(xin + s) : make_float4(0.f, 0.f, 0.f, 0.f);
-            const bool own_red = cell_ok(n, i, j, k) && ((i + j + k + flag) & 1) == 0;
-            const float fc = (m0 & MP) ? 0.f : 1.f;
-            if (own_red) xo.x += dp_cur[tj + 1][tk + 1];
-            // faces: owner = this cell if red (left face, c_f = -vol), else the lower neighbour (right face, +vol)
-            const float rf[3] = {r.y, r.z, r.w};
-            const float pf[3] = {pp.y, pp.z, pp.w};
-            const uint8_t bit[3] = {MU, MV, MW};
-            const int offs[3] = {di, dj, 1};
-            float upd[3];
-#pragma unroll
-            for (int d = 0; d < 3; d++) {
-                upd[d] = 0.f;
-                int li = i - (d == 0), lj = j - (d == 1), lk = k - (d == 2);
-                bool lower_red = !own_red && li >= 0 && lj >= 0 && lk >= 0 && cell_ok(n, li, lj, lk) &&
-                                 ((li + lj + lk + flag) & 1) == 0;
-                if (!own_red && !lower_red) continue;
-                bool fix = m0 & bit[d];
-                float v = fix ? 0.f : vol;
-                uint8_t mlo = __ldg(m + s - offs[d]);
-                float D = v * (4.f + fc + ((mlo & MP) ? 0.f : 1.f)) + pf[d] + (fix ? 1.f : 0.f);
-                float dpo = own_red ? dp_cur[tj + 1][tk + 1]
-                                    : (d == 0 ? dp_prev[tj][tk] : d == 1 ? dp_cur[tj][tk + 1] : dp_cur[tj + 1][tk]);
-                float cf = own_red ? -v : v;
-                upd[d] = (rf[d] - cf * dpo) / D;
-            }
-            xo.y += upd[0];
-            xo.z += upd[1];
-            xo.w += upd[2];
-            xout[s] = xo;
-        }
-        __syncthreads();
-        dp_prev[tj][tk] = dp_cur[tj + 1][tk + 1];
-        __syncthreads();
     }
 }
 
@@ -534,17 +416,6 @@ int resid32(cudaStream_t st, const Geom& g, float vol, const float4* r, const fl
 
 int apply32(cudaStream_t st, const Geom& g, float vol, const float4* x, const uint8_t* m, const float4* P, float4* y) {
     k_op32<true, false><<<grid_for(g.box(), TPB), TPB, 0, st>>>(g, vol, nullptr, x, m, P, y);
-    STG_LAUNCH_CK();
-    return STG_OK;
-}
-
-int vanka32(cudaStream_t st, const Geom& g, float vol, const float4* rr, const float4* xin, float4* xout, const uint8_t* m,
-            const float4* P, int flag) {
-    dim3 grid((g.n + VT_K) / VT_K, (g.n + VT_J) / VT_J, (g.n + VT_CHUNK) / VT_CHUNK), block(VT_K, VT_J);
-    if (xin)
-        k_vanka_tiled<true><<<grid, block, 0, st>>>(g, vol, rr, xin, xout, m, P, flag);
-    else
-        k_vanka_tiled<false><<<grid, block, 0, st>>>(g, vol, rr, xin, xout, m, P, flag);
     STG_LAUNCH_CK();
     return STG_OK;
 }

@@ -17,9 +17,9 @@ int resid32(cudaStream_t st, const Geom& g, float vol, const float4* r, const fl
             float4* rr);
 // y = A x in FP32
 int apply32(cudaStream_t st, const Geom& g, float vol, const float4* x, const uint8_t* m, const float4* P, float4* y);
-// One colour of the box-Vanka block-Jacobi step: xout = xin + SHATTER(B^-1 GATHER(rr)).
-// xin == nullptr means xin = 0.
-int vanka32(cudaStream_t st, const Geom& g, float vol, const float4* rr, const float4* xin, float4* xout, const uint8_t* m,
+// One colour of the box-Vanka block-Jacobi step on the residual equation, fused with the
+// residual: xout = xin + SHATTER(B^-1 GATHER(r - A xin)) (sweep.cu). xin == nullptr: xin = 0.
+int sweep32(cudaStream_t st, const Geom& g, float vol, const float4* r, const float4* xin, float4* xout, const uint8_t* m,
             const float4* P, int flag);
 // rc = R (rf - A xf) with R the 8-child sum masked by the coarse mask (xf == nullptr: rc = R rf).
 int restrict_resid32(cudaStream_t st, const Geom& gc, const Geom& gf, float volf, const float4* rf, const float4* xf,

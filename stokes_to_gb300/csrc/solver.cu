@@ -220,11 +220,10 @@ int sweep(stg_t* h, Level& L, const float4* r, int flag, bool first) {
     float vol = (float)L.vol;
     if (first) {
         // x = 0: the residual is r itself
-        PROF(h, 1, 49.0 * L.g.box(), vanka32(h->st, L.g, vol, r, nullptr, L.x(), L.m, L.P32, flag));
+        PROF(h, 1, 49.0 * L.g.box(), sweep32(h->st, L.g, vol, r, nullptr, L.x(), L.m, L.P32, flag));
         return STG_OK;
     }
-    PROF(h, 0, 65.0 * L.g.box(), resid32(h->st, L.g, vol, r, L.x(), L.m, L.P32, L.rr));
-    PROF(h, 1, 65.0 * L.g.box(), vanka32(h->st, L.g, vol, L.rr, L.x(), L.other(), L.m, L.P32, flag));
+    PROF(h, 1, 65.0 * L.g.box(), sweep32(h->st, L.g, vol, r, L.x(), L.other(), L.m, L.P32, flag));
     L.cur ^= 1;
     return STG_OK;
 }
@@ -473,7 +472,7 @@ int stg_profile_read(stg_t* h, int cls, int64_t* launches, double* ms, double* b
 }
 
 const char* stg_profile_name(int cls) {
-    static const char* names[STG_PROF_NCLASS] = {"resid32",  "vanka32", "restrict32", "prolong32", "apply32",
+    static const char* names[STG_PROF_NCLASS] = {"resid32",  "sweep32", "restrict32", "prolong32", "apply32",
                                                  "resid64",  "krylov",  "coarse",     "setup",     "other"};
     return (cls >= 0 && cls < STG_PROF_NCLASS) ? names[cls] : "";
 }
@@ -962,7 +961,7 @@ int stg_apply_op_device(stg_t* h, int op, int level, double* d_out, const double
                 STG_CK(cudaMemsetAsync(L.x(), 0, sizeof(float4) * L.g.nslot, h->st));
                 STG_TRY(smooth(h, L, L.r, op == STG_OP_SMOOTH_POST, true));
             } else {
-                STG_TRY(vanka32(h->st, L.g, (float)L.vol, L.r, nullptr, L.x(), L.m, L.P32, op == STG_OP_VANKA_BLACK ? 1 : 0));
+                STG_TRY(sweep32(h->st, L.g, (float)L.vol, L.r, nullptr, L.x(), L.m, L.P32, op == STG_OP_VANKA_BLACK ? 1 : 0));
             }
             STG_TRY(f32_to_f64(h->st, L.g.nslot, L.x(), L.t1));
             STG_TRY(slots_to_blocked64(h->st, L.g, L.t1, d_out, nullptr));

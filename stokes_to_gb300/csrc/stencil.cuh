@@ -74,19 +74,18 @@ __device__ __forceinline__ Nb<T> nb_load(const V* x, const uint8_t* m, int q) {
     return r;
 }
 
-// Viscous and pressure parts of A (or E when ENERGY) at slot s, without the diagonal
-// P x + F x terms. out = {row p, row u, row v, row w}.
-template <class T, bool ENERGY, class V>
-__device__ __forceinline__ void stencil_rows(const V* __restrict__ x, const uint8_t* __restrict__ m, int s, int di, int dj,
-                                             T vol, uint8_t ms, T out[4]) {
-    const int dk = 1;
-    Nb<T> c0 = nb_load<T>(x, m, s);
-    Nb<T> xm = nb_load<T>(x, m, s - di), xp = nb_load<T>(x, m, s + di);
-    Nb<T> ym = nb_load<T>(x, m, s - dj), yp = nb_load<T>(x, m, s + dj);
-    Nb<T> zm = nb_load<T>(x, m, s - dk), zp = nb_load<T>(x, m, s + dk);
-    Nb<T> xp_ym = nb_load<T>(x, m, s + di - dj), xm_yp = nb_load<T>(x, m, s - di + dj);
-    Nb<T> xp_zm = nb_load<T>(x, m, s + di - dk), xm_zp = nb_load<T>(x, m, s - di + dk);
-    Nb<T> yp_zm = nb_load<T>(x, m, s + dj - dk), ym_zp = nb_load<T>(x, m, s - dj + dk);
+// Viscous and pressure parts of A (or E when ENERGY) at one slot, without the diagonal
+// P x + F x terms. ld(a, b, c) returns the masked unknowns of the slot at offset (a, b, c)
+// along (i, j, k). out = {row p, row u, row v, row w}.
+template <class T, bool ENERGY, class LD>
+__device__ __forceinline__ void stencil_core(LD ld, T vol, uint8_t ms, T out[4]) {
+    Nb<T> c0 = ld(0, 0, 0);
+    Nb<T> xm = ld(-1, 0, 0), xp = ld(1, 0, 0);
+    Nb<T> ym = ld(0, -1, 0), yp = ld(0, 1, 0);
+    Nb<T> zm = ld(0, 0, -1), zp = ld(0, 0, 1);
+    Nb<T> xp_ym = ld(1, -1, 0), xm_yp = ld(-1, 1, 0);
+    Nb<T> xp_zm = ld(1, 0, -1), xm_zp = ld(-1, 0, 1);
+    Nb<T> yp_zm = ld(0, 1, -1), ym_zp = ld(0, -1, 1);
 
     // fix_c D (V u) at the own cell and the three lower neighbours
     T dv0 = c0.mc ? vol * ((xp.ux - c0.ux) + (yp.uy - c0.uy) + (zp.uz - c0.uz)) : T(0);
@@ -121,6 +120,24 @@ __device__ __forceinline__ void stencil_rows(const V* __restrict__ x, const uint
     out[1] = (ms & MU) ? T(0) : gx;
     out[2] = (ms & MV) ? T(0) : gy;
     out[3] = (ms & MW) ? T(0) : gz;
+}
+
+template <class T, bool ENERGY, class V>
+__device__ __forceinline__ void stencil_rows(const V* __restrict__ x, const uint8_t* __restrict__ m, int s, int di, int dj,
+                                             T vol, uint8_t ms, T out[4]) {
+    auto ld = [&](int a, int b, int c) { return nb_load<T>(x, m, s + a * di + b * dj + c); };
+    stencil_core<T, ENERGY>(ld, vol, ms, out);
+}
+
+template <class T>
+__device__ __forceinline__ Nb<T> nb_make(T p, T u, T v, T w, uint8_t mm) {
+    Nb<T> r;
+    r.p = p;
+    r.ux = (mm & MU) ? T(0) : u;
+    r.uy = (mm & MV) ? T(0) : v;
+    r.uz = (mm & MW) ? T(0) : w;
+    r.mc = !(mm & MP);
+    return r;
 }
 
 // Full row values: A x (ENERGY false) or E x (ENERGY true) at slot s.
