@@ -177,6 +177,23 @@ int stg_filter(stg_t* h, double rmin, const double* in, double* out, int transpo
 int stg_oc_update(stg_t* h, double rmin, const double* x, const double* dc, double frac, double move, double lo, double hi,
                   double* x_new, double* lambda_out);
 
+/* The optimality-criteria update of stg_oc_update for callers that cannot allocate
+ * device memory: applications that reserve the whole GPU for their own pool, plugins
+ * running under another framework's allocator budget, and latency-sensitive loops that
+ * cannot afford the device-wide synchronisation of cudaMalloc/cudaFree. No counterpart
+ * in the reference. The caller passes device arrays of N^3 cells (Field order): the
+ * design d_x, the sensitivity d_dc and the result d_xnew (which may alias d_x); no
+ * handle is needed and nothing is allocated.
+ * The only scratch is a fixed 16 KB array inside this library's device image (every GPU
+ * that loads the library holds it until exit). The first call on a device resolves that
+ * array's device address (with the device current) - make it before any stream capture.
+ * All calls share the array, so calls that overlap on the GPU (other streams, other host
+ * threads on the same device) race; serialise them. N above 1024 is rejected with
+ * STG_E_INVALID. Work is issued on cuda_stream (a cudaStream_t, NULL = legacy default
+ * stream) and synchronised before return. Results equal stg_oc_update's. */
+int stg_oc_update_noalloc(int n, double rmin, const double* d_x, const double* d_dc, double frac, double move, double lo,
+                          double hi, double* d_xnew, double* lambda_out, void* cuda_stream);
+
 /* ----------------------------------------------------------------------------
  * LinearMapping plugin API (common_cpx/LinearMapping.h:4-14) on raw device pointers in
  * the reference blocked layout; issued on the handle's stream and synchronised

@@ -39,7 +39,7 @@ EXPORTS = [
     "stg_energy_grad_x", "stg_energy_grad_q", "stg_set_density", "stg_adjoint_sensitivity", "stg_filter", "stg_oc_update",
     "stg_apply_A_device", "stg_apply_E_device", "stg_update", "stg_vcycle_device", "stg_apply_op_device",
     "stg_level_descr_device", "stg_density_noise", "stg_set_stream", "stg_kernel_launches", "stg_profile",
-    "stg_profile_read", "stg_profile_name",
+    "stg_profile_read", "stg_profile_name", "stg_oc_update_noalloc",
 ]
 STG_PROF_NCLASS = 10
 
@@ -122,6 +122,7 @@ def lib():
         L.stg_profile_read.argtypes = [P, I, ctypes.POINTER(ctypes.c_int64), DP, DP]
         L.stg_profile_name.restype = ctypes.c_char_p
         L.stg_profile_name.argtypes = [I]
+        L.stg_oc_update_noalloc.argtypes = [I, D, P, P, D, D, D, D, P, DP, P]
         _LIB = L
     return _LIB
 
