@@ -4,6 +4,7 @@
 // reference's own blocked DOF layout [cells | x-faces | y-faces | z-faces] so the
 // oracle can be compared entry by entry with the reference's LinearMapping vectors.
 #include "oracle3d.h"
+#include "krylov.h"
 
 #include <algorithm>
 #include <cmath>
@@ -643,112 +644,22 @@ void mg_apply(Hierarchy& H, double* out, const double* in) {
 }
 
 // ---------------------------------------------------------------- Krylov
-static double dot(const double* a, const double* b, int n) {
-    double s = 0;
-#pragma omp parallel for reduction(+ : s)
-    for (int i = 0; i < n; i++) s += a[i] * b[i];
-    return s;
-}
-
-// Small least squares min ||e0 - H y|| for the (i+1) x i Hessenberg, solved with Givens
-// rotations. The reference uses Eigen's colPivHouseholderQr on the same system
-// (common_cpx/GMRES.cpp:84); for a full-rank H both give the unique minimiser.
-static void hess_lsq(const std::vector<double>& Hm, int ld, int i, double e0, std::vector<double>& y, double& res) {
-    std::vector<double> R((size_t)(i + 1) * i), g(i + 1, 0.0);
-    for (int c = 0; c < i; c++)
-        for (int rr = 0; rr <= i; rr++) R[rr + (size_t)c * (i + 1)] = Hm[rr + (size_t)c * ld];
-    g[0] = e0;
-    for (int c = 0; c < i; c++) {
-        double a = R[c + (size_t)c * (i + 1)], b = R[c + 1 + (size_t)c * (i + 1)];
-        double h = std::hypot(a, b);
-        double cs = h == 0 ? 1.0 : a / h, sn = h == 0 ? 0.0 : b / h;
-        for (int k = c; k < i; k++) {
-            double u = R[c + (size_t)k * (i + 1)], v = R[c + 1 + (size_t)k * (i + 1)];
-            R[c + (size_t)k * (i + 1)] = cs * u + sn * v;
-            R[c + 1 + (size_t)k * (i + 1)] = -sn * u + cs * v;
-        }
-        double u = g[c], v = g[c + 1];
-        g[c] = cs * u + sn * v;
-        g[c + 1] = -sn * u + cs * v;
-    }
-    y.assign(i, 0.0);
-    for (int c = i - 1; c >= 0; c--) {
-        double s = g[c];
-        for (int k = c + 1; k < i; k++) s -= R[c + (size_t)k * (i + 1)] * y[k];
-        double dgn = R[c + (size_t)c * (i + 1)];
-        y[c] = dgn != 0.0 ? s / dgn : 0.0;
-    }
-    res = std::fabs(g[i]);
-}
-
-
-// GMRES::Solve (common_cpx/GMRES.cpp:20-110): left-preconditioned, classical Gram-Schmidt,
-// x recomputed from the whole basis each iteration; stops on the preconditioned residual.
-// The thresholds and the basis size are the reference's public members. 'restarts' lets
-// the oracle reach a tight tolerance: each restart runs the reference loop on the
-// current true residual (a restart count of 0 is exactly the reference).
+// GMRES::Solve (common_cpx/GMRES.cpp:20-110) with A = the finest operator and the V-cycle
+// as left preconditioner (stoke/FluidSteadyState3D.cpp:120-125); see krylov.h.
 void gmres_solve(Hierarchy& H, const double* b, double* x, int max_iter, double abs_thres, double rel_thres,
                  double norm_thres, int restarts, double true_tol, SolveStats& st) {
     const int t = H.l - 1;
     const Descr& ds = H.lv[t];
     const int n = ds.g.size();
-    std::vector<double> rr(n), Ax(n), Aq(n), q(n);
-    std::fill(x, x + n, 0.0);
-    double bn = std::sqrt(dot(b, b, n));
-    st = SolveStats();
-    for (int cyc = 0; cyc <= restarts; cyc++) {
-        apply_A(ds, Ax.data(), x, H.w);
-        for (int k = 0; k < n; k++) rr[k] = b[k] - Ax[k];
-        double tr = std::sqrt(dot(rr.data(), rr.data(), n));
-        if (cyc > 0 && (bn == 0 || tr / bn <= true_tol)) break;
-        if (cyc > 0) st.restarts++;
-        std::vector<std::vector<double>> Q;
-        Q.emplace_back(n);
-        mg_apply(H, Q[0].data(), rr.data());
-        double e0 = std::sqrt(dot(Q[0].data(), Q[0].data(), n));
-        if (e0 == 0) break;
-        for (int k = 0; k < n; k++) Q[0][k] /= e0;
-        std::vector<double> Hm((size_t)(max_iter + 1) * max_iter, 0.0), y;
-        const int ld = max_iter + 1;
-        int used = 0;
-        bool stop = false;
-        for (int i = 1; i < max_iter; i++) {
-            apply_A(ds, Aq.data(), Q[i - 1].data(), H.w);
-            mg_apply(H, q.data(), Aq.data());
-            std::vector<double> hcol(i);
-            for (int j = 0; j < i; j++) hcol[j] = dot(q.data(), Q[j].data(), n);
-            for (int j = 0; j < i; j++) {
-                Hm[j + (size_t)(i - 1) * ld] = hcol[j];
-                const double* qj = Q[j].data();
-                double hj = hcol[j];
-#pragma omp parallel for
-                for (int k = 0; k < n; k++) q[k] -= hj * qj[k];
-            }
-            double nq = std::sqrt(dot(q.data(), q.data(), n));
-            if (nq < norm_thres) stop = true;
-            Hm[i + (size_t)(i - 1) * ld] = nq;
-            Q.emplace_back(n);
-            for (int k = 0; k < n; k++) Q[i][k] = nq > 0 ? q[k] / nq : 0.0;
-            double res;
-            hess_lsq(Hm, ld, i, e0, y, res);
-            used = i;
-            st.iters++;
-            st.precond_res = res;
-            if (res < abs_thres) stop = true;
-            if (res < rel_thres * e0) stop = true;
-            if (stop) break;
-        }
-        for (int j = 0; j < used; j++) {
-            const double* qj = Q[j].data();
-            double yj = y[j];
-#pragma omp parallel for
-            for (int k = 0; k < n; k++) x[k] += yj * qj[k];
-        }
-    }
-    apply_A(ds, Ax.data(), x, H.w);
-    for (int k = 0; k < n; k++) rr[k] = b[k] - Ax[k];
-    st.abs_true = std::sqrt(dot(rr.data(), rr.data(), n));
-    st.rel_true = bn > 0 ? st.abs_true / bn : 0.0;
+    VecOp A = [&](double* out, const double* in) { apply_A(ds, out, in, H.w); };
+    VecOp M = [&](double* out, const double* in) { mg_apply(H, out, in); };
+    KrylovStats ks;
+    gmres_generic(n, A, M, b, x, max_iter, abs_thres, rel_thres, norm_thres, restarts, true_tol, ks);
+    st.iters = ks.iters;
+    st.restarts = ks.restarts;
+    st.rel_true = ks.rel_true;
+    st.abs_true = ks.abs_true;
+    st.precond_res = ks.precond_res;
 }
 
 }  // namespace orc

@@ -302,3 +302,164 @@ class Steady3D:
 
     def vcycle(self, r):
         return self._vec_op(self.L.orc3_vcycle, self.levels - 1, self.levels - 1, r)
+
+
+# ------------------------------------------------------------------ 2D solver handle
+_L2 = {}
+
+
+def _lib2():
+    L = lib()
+    if "init" not in _L2:
+        L.orc2_create.restype = P
+        L.orc2_create.argtypes = [I]
+        L.orc2_destroy.argtypes = [P]
+        L.orc2_dof.restype = I
+        L.orc2_levels.restype = I
+        L.orc2_index.restype = I
+        L.orc2_index.argtypes = [I, I, I, I, I]
+        L.orc2_level_dof.restype = I
+        L.orc2_level_dof.argtypes = [P, I]
+        L.orc2_solve.restype = I
+        L.orc2_solve.argtypes = [P, I, D, D, D, I, D, DP, DP]
+        L.orc2_energy.restype = D
+        L.orc2_energy.argtypes = [P, DP]
+        L.orc2_coarse_info.restype = I
+        L.orc2_coarse_info.argtypes = [P]
+        for name in ["orc2_init_boundary", "orc2_update_penalty", "orc2_update_b", "orc2_set_b_blocked", "orc2_apply_A",
+                     "orc2_apply_E", "orc2_level_descr", "orc2_restrict", "orc2_prolong", "orc2_smooth_colour",
+                     "orc2_smooth", "orc2_coarse_apply", "orc2_vcycle", "orc2_field_to_blocked", "orc2_blocked_to_field",
+                     "orc_bc_test0_2d"]:
+            getattr(L, name).restype = None
+        L.orc2_init_boundary.argtypes = [P, DP, IP, DP, DP, IP, IP, I]
+        L.orc2_update_penalty.argtypes = [P, DP, DP, DP]
+        L.orc2_update_b.argtypes = [P, DP, DP, DP]
+        L.orc2_set_b_blocked.argtypes = [P, DP]
+        L.orc2_apply_A.argtypes = [P, I, DP, DP]
+        L.orc2_apply_E.argtypes = [P, DP, DP]
+        L.orc2_level_descr.argtypes = [P, I, DP, DP, U8P, DP]
+        L.orc2_restrict.argtypes = [P, I, DP, DP]
+        L.orc2_prolong.argtypes = [P, I, DP, DP]
+        L.orc2_smooth_colour.argtypes = [P, I, I, DP, DP]
+        L.orc2_smooth.argtypes = [P, I, I, DP, DP]
+        L.orc2_coarse_apply.argtypes = [P, DP, DP]
+        L.orc2_vcycle.argtypes = [P, DP, DP]
+        L.orc2_field_to_blocked.argtypes = [I, DP, DP, DP, DP]
+        L.orc2_blocked_to_field.argtypes = [I, DP, DP, DP, DP]
+        L.orc_bc_test0_2d.argtypes = [I, DP, IP, DP, DP, DP, IP, IP, DP, DP]
+        _L2["init"] = True
+    return L
+
+
+def dof2(n):
+    return _lib2().orc2_dof(n)
+
+
+def field_to_blocked2(n, cell, faces):
+    out = np.zeros(dof2(n))
+    f = [np.ascontiguousarray(x, dtype=np.float64) for x in faces]
+    c = np.ascontiguousarray(cell, dtype=np.float64) if cell is not None else None
+    _lib2().orc2_field_to_blocked(n, dp(c), dp(f[0]), dp(f[1]), dp(out))
+    return out
+
+
+def blocked_to_field2(n, v):
+    v = np.ascontiguousarray(v, dtype=np.float64)
+    cell = np.zeros((n, n))
+    faces = [np.zeros(face_shape(n, d, 2)) for d in range(2)]
+    _lib2().orc2_blocked_to_field(n, dp(v), dp(cell), dp(faces[0]), dp(faces[1]))
+    return cell, faces
+
+
+def bc_test0_2d(n):
+    b = Boundary(n, 2)
+    _lib2().orc_bc_test0_2d(n, dp(b.cell_vol), ip(b.cell_fixed), dp(b.cell_b), dp(b.face_vol[0]), dp(b.face_vol[1]),
+                            ip(b.face_fixed[0]), ip(b.face_fixed[1]), dp(b.face_b[0]), dp(b.face_b[1]))
+    return b
+
+
+class Steady2D:
+    """Mirror of FluidSteadyState (2D) + FluidEnergy on the CPU oracle."""
+
+    def __init__(self, n):
+        self.n = n
+        self.L = _lib2()
+        self.h = self.L.orc2_create(n)
+        self.levels = self.L.orc2_levels(n)
+
+    def close(self):
+        if self.h:
+            self.L.orc2_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def level_dof(self, level):
+        return self.L.orc2_level_dof(self.h, level)
+
+    def init_boundary(self, b):
+        ff = [np.ascontiguousarray(x, dtype=np.int32) for x in b.face_fixed]
+        fv = [np.ascontiguousarray(x, dtype=np.float64) for x in b.face_vol]
+        self.L.orc2_init_boundary(self.h, dp(np.ascontiguousarray(b.cell_vol, dtype=np.float64)),
+                                  ip(np.ascontiguousarray(b.cell_fixed, dtype=np.int32)), dp(fv[0]), dp(fv[1]), ip(ff[0]),
+                                  ip(ff[1]), 1 if b.closed else 0)
+
+    def update_penalty(self, cell_pen, face_pen):
+        fp = [np.ascontiguousarray(x, dtype=np.float64) for x in face_pen]
+        self.L.orc2_update_penalty(self.h, dp(np.ascontiguousarray(cell_pen, dtype=np.float64)), dp(fp[0]), dp(fp[1]))
+
+    def update_b(self, cell_b, face_b):
+        fb = [np.ascontiguousarray(x, dtype=np.float64) for x in face_b]
+        self.L.orc2_update_b(self.h, dp(np.ascontiguousarray(cell_b, dtype=np.float64)), dp(fb[0]), dp(fb[1]))
+
+    def set_b_blocked(self, b):
+        self.L.orc2_set_b_blocked(self.h, dp(np.ascontiguousarray(b, dtype=np.float64)))
+
+    def solve(self, max_iter=40, abs_thr=1e-3, rel_thr=1e-4, norm_thr=1e-3, restarts=0, true_tol=0.0):
+        x = np.zeros(self.level_dof(self.levels - 1))
+        st = np.zeros(6)
+        self.L.orc2_solve(self.h, max_iter, abs_thr, rel_thr, norm_thr, restarts, true_tol, dp(x), dp(st))
+        return x, dict(iters=int(st[0]), restarts=int(st[1]), rel_true=st[2], abs_true=st[3], precond_res=st[4])
+
+    def _op(self, fn, nout, x, *extra):
+        y = np.zeros(nout)
+        fn(self.h, *extra, dp(np.ascontiguousarray(x, dtype=np.float64)), dp(y))
+        return y
+
+    def apply_A(self, x, level=None):
+        level = self.levels - 1 if level is None else level
+        return self._op(self.L.orc2_apply_A, self.level_dof(level), x, level)
+
+    def apply_E(self, x):
+        return self._op(self.L.orc2_apply_E, self.level_dof(self.levels - 1), x)
+
+    def energy(self, x):
+        return self.L.orc2_energy(self.h, dp(np.ascontiguousarray(x, dtype=np.float64)))
+
+    def descr(self, level):
+        s = self.level_dof(level)
+        vol, pen, fx, lap = np.zeros(s), np.zeros(s), np.zeros(s, dtype=np.uint8), np.zeros(1)
+        self.L.orc2_level_descr(self.h, level, dp(vol), dp(pen), fx.ctypes.data_as(U8P), dp(lap))
+        return vol, pen, fx, float(lap[0])
+
+    def restrict(self, coarse_level, rf):
+        return self._op(self.L.orc2_restrict, self.level_dof(coarse_level), rf, coarse_level)
+
+    def prolong(self, coarse_level, xc):
+        return self._op(self.L.orc2_prolong, self.level_dof(coarse_level + 1), xc, coarse_level)
+
+    def smooth_colour(self, level, flag, r):
+        return self._op(self.L.orc2_smooth_colour, self.level_dof(level), r, level, flag)
+
+    def smooth(self, level, post, r):
+        return self._op(self.L.orc2_smooth, self.level_dof(level), r, level, post)
+
+    def coarse_apply(self, r):
+        return self._op(self.L.orc2_coarse_apply, self.level_dof(0), r)
+
+    def coarse_info(self):
+        return self.L.orc2_coarse_info(self.h)
+
+    def vcycle(self, r):
+        return self._op(self.L.orc2_vcycle, self.level_dof(self.levels - 1), r)

@@ -18,3 +18,7 @@ NVCC="${NVCC:-nvcc}"
 "$NVCC" -std=c++14 -O2 -Xcompiler -fPIC -shared -gencode arch=compute_103a,code=sm_103a \
   -I "$CC_DIR" "$HERE/ref_grid3d_wrap.cu" "$CC_DIR/grid3D.cu" -o "$OUT/libref_grid3d.so"
 echo "built $OUT/libref_grid3d.so"
+# grid2D lives in form01mapping.cu beside the 2D mapping kernels (extended lambdas, gpuUtils)
+"$NVCC" -std=c++14 -O2 -Xcompiler -fPIC -shared --extended-lambda -w -gencode arch=compute_103a,code=sm_103a \
+  -I "$CC_DIR" "$HERE/ref_grid2d_wrap.cu" "$CC_DIR/form01mapping.cu" "$CC_DIR/gpuUtils.cu" -o "$OUT/libref_grid2d.so" -lcublas
+echo "built $OUT/libref_grid2d.so"

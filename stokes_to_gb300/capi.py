@@ -145,7 +145,7 @@ def _faces(arrs, ctype=DP, dtype=np.float64):
     if arrs is None:
         return None, []
     keep = [np.ascontiguousarray(a, dtype=dtype) for a in arrs]
-    tab = (ctype * 3)(*[k.ctypes.data_as(ctype) for k in keep])
+    tab = (ctype * len(keep))(*[k.ctypes.data_as(ctype) for k in keep])
     return tab, keep
 
 
@@ -173,7 +173,9 @@ def face_shape(n, d, dim=3):
 
 
 class Solver:
-    """Thin Python handle over the C ABI (mirrors FluidSteadyState3D + FluidEnergy3D)."""
+    """Thin Python handle over the C ABI (mirrors FluidSteadyState3D + FluidEnergy3D for
+    dim = 3, FluidSteadyState + FluidEnergy for dim = 2). Field-order arrays: cells
+    (n,)*dim, faces of axis d one longer along d."""
 
     def __init__(self, n, dim=3, **opts):
         self.n, self.dim = n, dim
@@ -218,10 +220,10 @@ class Solver:
         return check(self.L.stg_set_rhs(self.h, dp(_c64(cell_b)), fb))
 
     def _out_fields(self):
-        n = self.n
-        p = np.zeros((n,) * 3)
-        vel = [np.zeros(face_shape(n, d)) for d in range(3)]
-        tab = (DP * 3)(*[dp(v) for v in vel])
+        n, dim = self.n, self.dim
+        p = np.zeros((n,) * dim)
+        vel = [np.zeros(face_shape(n, d, dim)) for d in range(dim)]
+        tab = (DP * dim)(*[dp(v) for v in vel])
         return p, vel, tab
 
     def solve(self, want=True, allow_not_converged=False):
@@ -267,23 +269,23 @@ class Solver:
 
     def adjoint_sensitivity(self, law, want=True):
         st = Stats()
-        g = np.zeros((self.n,) * 3) if want else None
+        g = np.zeros((self.n,) * self.dim) if want else None
         check(self.L.stg_adjoint_sensitivity(self.h, ctypes.byref(law), dp(g), ctypes.byref(st)))
         return g, st.as_dict()
 
     def filter(self, rmin, rho=None, transpose=False, want=True):
-        out = np.zeros((self.n,) * 3) if want else None
+        out = np.zeros((self.n,) * self.dim) if want else None
         check(self.L.stg_filter(self.h, rmin, dp(_c64(rho)), dp(out), 1 if transpose else 0))
         return out
 
     def oc_update(self, rmin, x, dc, frac, move=0.2, lo=0.0, hi=1.0, want=True):
-        out = np.zeros((self.n,) * 3) if want else None
+        out = np.zeros((self.n,) * self.dim) if want else None
         lam = np.zeros(1)
         check(self.L.stg_oc_update(self.h, rmin, dp(_c64(x)), dp(_c64(dc)), frac, move, lo, hi, dp(out), dp(lam)))
         return out, float(lam[0])
 
     def density_noise(self, seed, sigma, want=True):
-        out = np.zeros((self.n,) * 3) if want else None
+        out = np.zeros((self.n,) * self.dim) if want else None
         check(self.L.stg_density_noise(self.h, seed, sigma, dp(out)))
         return out
 

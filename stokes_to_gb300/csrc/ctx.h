@@ -1,0 +1,125 @@
+// Handle state shared by the 3D (solver.cu) and 2D (solver2d.cu) translation units.
+#pragma once
+#include <cuda_bf16.h>
+
+#include <vector>
+
+#include "kernels.h"
+
+namespace stg {
+
+struct Level {
+    Geom g;
+    double vol = 1.0;       // vol of the free faces
+    double cell_vol = 1.0;  // cell vol (reported by the descriptor adapter only)
+    uint8_t* m = nullptr;
+    d4* P64 = nullptr;
+    float4* P32 = nullptr;
+    float4 *r = nullptr, *xa = nullptr, *xb = nullptr, *rr = nullptr;
+    int cur = 0;  // which of xa/xb holds the current correction
+    __nv_bfloat16* xbf = nullptr;
+    d4 *t0 = nullptr, *t1 = nullptr;  // FP64 adapter buffers (allocated on first use)
+    float4* x() { return cur ? xb : xa; }
+    float4* other() { return cur ? xa : xb; }
+};
+
+}  // namespace stg
+
+using stg::DenseCoarse;
+using stg::Level;
+
+// Per-kernel-class CUDA-event timing on the handle's stream.
+struct Prof {
+    bool on = false;
+    std::vector<cudaEvent_t> pool;
+    size_t used = 0;
+    struct Pending {
+        int cls;
+        size_t ev;
+        double bytes;
+    };
+    std::vector<Pending> pend;
+    long long launches[STG_PROF_NCLASS] = {};
+    double ms[STG_PROF_NCLASS] = {};
+    double bytes[STG_PROF_NCLASS] = {};
+};
+
+struct stg_ctx {
+    int dim = 3, n = 0, L = 0;
+    Prof prof;
+    cudaStream_t own_st = nullptr;
+    stg_opts opts{};
+    cudaStream_t st = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    std::vector<stg::Level> lv;  // lv[0] coarsest ... lv[L-1] finest (reference order)
+    DenseCoarse dense;
+    bool closed = true, have_boundary = false, have_penalty = false, have_rhs = false, updated = false, have_solution = false;
+    // fine-level FP64
+    stg::d4 *b64 = nullptr, *x64 = nullptr, *r64 = nullptr, *t64 = nullptr, *lam64 = nullptr;
+    // Krylov (FP32)
+    int m = 0;
+    std::vector<float4*> V, Z;
+    float4* w = nullptr;
+    double *dscr = nullptr, *dh = nullptr, *dnrm = nullptr, *dy = nullptr;
+    // host-order staging (cells + 3 face arrays)
+    double* stage = nullptr;
+    int* istage = nullptr;
+    size_t ncell = 0, nface = 0;
+    // design loop
+    double *d_design = nullptr, *d_phys = nullptr, *d_sens = nullptr, *d_sens_design = nullptr, *d_vw = nullptr,
+           *d_tmp = nullptr, *d_gauss = nullptr, *d_parts = nullptr;
+    double vw_rmin = -1.0;
+    const double* phys_used = nullptr;
+    // fine vector length in float4 / d4 units and the per-dimension hooks of solve_core
+    long long n4 = 0;
+    int (*setup)(stg_t*) = nullptr;
+    int (*resid64)(stg_t*, const stg::d4* b, const stg::d4* x, stg::d4* r, double* nrm2_host) = nullptr;
+    int (*precond)(stg_t*, const float4* rhs, float4* out) = nullptr;
+    int (*apply32)(stg_t*, const float4* x, float4* y) = nullptr;
+    struct Ctx2* c2 = nullptr;  // 2D state (dim == 2)
+};
+
+
+namespace stg {
+int prof_flush(stg_t* h);
+int prof_begin(stg_t* h, size_t* ev);
+int prof_end(stg_t* h, int cls, double bytes, size_t ev);
+int solve_core(stg_t* h, const d4* b, d4* x, stg_stats* stats);
+// 2D path (solver2d.cu): vectors in the reference's 8x8-blocked layout, d4 views of
+// dof/4 entries. Field-order inputs are device arrays (null = zeros).
+int create2d(stg_t* h);
+void destroy2d(stg_t* h);
+long long dof2d(const stg_t* h, int level);
+int level_n2d(const stg_t* h, int level);
+int set_boundary2d(stg_t* h, const double* cvol, const int* cfix, const double* fv0, const double* fv1, const int* ff0,
+                   const int* ff1);
+int set_penalty2d(stg_t* h, const double* cp, const double* f0, const double* f1);
+int set_density2d(stg_t* h, const double* rho, const stg_alpha& law);
+int field_to_vec2d(stg_t* h, const double* cell, const double* f0, const double* f1, d4* out);
+int vec_to_field2d(stg_t* h, const d4* in, double* cell, double* f0, double* f1);
+// out = E x; with part != nullptr, per-block partials of x.out and their count in *nb
+int energy2d(stg_t* h, const d4* x, d4* out, double* part, int* nb);
+int sensitivity2d(stg_t* h, const double* rho, const stg_alpha& law, const d4* x, const d4* lam, double* grad);
+int apply_A2d(stg_t* h, int level, double* out, const double* in);
+int apply_E2d(stg_t* h, double* out, const double* in);
+int vcycle2d(stg_t* h, double* out, const double* in);
+int apply_op2d(stg_t* h, int op, int level, double* out, const double* in);
+int level_descr2d(stg_t* h, int level, double* vol, double* pen, uint8_t* fixed);
+
+template <class T>
+int dalloc(T** p, size_t count) {
+    cudaError_t e = cudaMalloc((void**)p, sizeof(T) * (count ? count : 1));
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc", __FILE__, __LINE__);
+    e = cudaMemset(*p, 0, sizeof(T) * (count ? count : 1));
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemset", __FILE__, __LINE__);
+    return STG_OK;
+}
+}  // namespace stg
+
+#define PROF(h, cls, bytes, expr)                          \
+    do {                                                   \
+        size_t ev_ = 0;                                    \
+        STG_TRY(::stg::prof_begin((h), &ev_));             \
+        STG_TRY(expr);                                     \
+        STG_TRY(::stg::prof_end((h), (cls), (bytes), ev_)); \
+    } while (0)

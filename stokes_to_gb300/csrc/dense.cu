@@ -274,16 +274,19 @@ int dense_setup(cudaStream_t st, DenseCoarse& D, const Geom& g, double vol, cons
         k_closed<<<grid_for((long long)nd * nd, TPB), TPB, 0, st>>>(nd, D.comp_of, D.A);
         STG_LAUNCH_CK();
     }
-    STG_CK(cudaMemsetAsync(D.info, 0, sizeof(int), st));
-    double *a = D.A, *b = D.Ainv;
+    return gj_invert(st, nd, D.A, D.Ainv, D.info, &D.inv);
+}
+
+int gj_invert(cudaStream_t st, int nd, double* a, double* b, int* info, const double** inv) {
+    STG_CK(cudaMemsetAsync(info, 0, sizeof(int), st));
     for (int k = 0; k < nd; k++) {
-        k_gj_step<<<nd, TPB, 0, st>>>(nd, k, a, b, D.info);
+        k_gj_step<<<nd, TPB, 0, st>>>(nd, k, a, b, info);
         STG_LAUNCH_CK();
         double* t = a;
         a = b;
         b = t;
     }
-    D.inv = a + nd;  // right half of the final buffer, row stride 2 nd
+    *inv = a + nd;  // right half of the final buffer, row stride 2 nd
     return STG_OK;
 }
 

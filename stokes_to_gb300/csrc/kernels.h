@@ -94,6 +94,10 @@ int dense_init(DenseCoarse& D, const Geom& g);
 void dense_free(DenseCoarse& D);
 // DirectSolve3D::update: probe assembly + (closed) all-ones p-block + inversion
 int dense_setup(cudaStream_t st, DenseCoarse& D, const Geom& g, double vol, const uint8_t* m, const d4* P64, int closed);
+// In-place Gauss-Jordan inversion of the row-major nd x 2nd [A | I] held in a (b is the
+// second buffer of the same size); *inv receives the inverse (row stride 2 nd), which
+// lies in whichever buffer the last step wrote. *info = first zero pivot + 1, or 0.
+int gj_invert(cudaStream_t st, int nd, double* a, double* b, int* info, const double** inv);
 // x = A^-1 r on the slots (FP32 in/out, FP64 inside)
 int dense_apply32(cudaStream_t st, const DenseCoarse& D, const Geom& g, const float4* r, float4* x);
 int dense_apply64(cudaStream_t st, const DenseCoarse& D, const Geom& g, const d4* r, d4* x);
@@ -103,10 +107,10 @@ int face_penalty_from_density(cudaStream_t st, const Geom& g, const double* rho,
                               d4* P64, float4* P32);
 int sensitivity(cudaStream_t st, const Geom& g, const double* rho, const stg_alpha& law, const d4* x, const d4* lam,
                 double* grad);
-int density_filter(cudaStream_t st, int n, double rmin, const double* in, double* out, int transpose);
-int filter_volume_weights(cudaStream_t st, int n, double rmin, double* vw);
+// dim 2: cells (i,j) -> i*n + j; dim 3: (i*n + j)*n + k
+int density_filter(cudaStream_t st, int dim, int n, double rmin, const double* in, double* out, int transpose);
 int oc_volume(cudaStream_t st, int ncell, const double* x, const double* dc, const double* vw, double lam, double move,
               double lo, double hi, double* xnew, double* parts, int* nparts);
-int density_noise(cudaStream_t st, int n, uint64_t seed, const double* w, int R, double* out, double* tmp);
+int density_noise(cudaStream_t st, int dim, int n, uint64_t seed, const double* w, int R, double* out, double* tmp);
 
 }  // namespace stg

@@ -1,12 +1,14 @@
 // Host orchestration of libstokes_gb300 and its C ABI (include/stokes_gb300.h).
 //
-// Solve = FluidSteadyState3D::solve (stoke/FluidSteadyState3D.cpp:152-170) re-designed
+// 3D solve = FluidSteadyState3D::solve (stoke/FluidSteadyState3D.cpp:152-170) re-designed
 // for one GB300: the coarse re-discretisation, the smoother blocks and the coarsest
 // inverse are rebuilt on the device; the reference's host GMRES with the V-cycle as
 // left preconditioner (common_cpx/GMRES.cpp:20-110) becomes a device-resident FP64
 // defect-correction loop whose correction equations are solved by right-preconditioned
 // FGMRES in FP32 with the same V-cycle (common_cpx/MultigridSolve.cpp:73-114) as
 // preconditioner. Every vector stays in HBM; the host only sees the Hessenberg scalars.
+// The 2D path (FluidSteadyState, stoke/FluidSteadyState.cpp) lives in solver2d.cu and
+// plugs its set-up, residual, preconditioner and operator into the same driver.
 #include <cuda_bf16.h>
 
 #include <atomic>
@@ -17,7 +19,7 @@
 #include <cstring>
 #include <vector>
 
-#include "kernels.h"
+#include "ctx.h"
 
 namespace stg {
 
@@ -39,70 +41,11 @@ int cuda_fail(cudaError_t e, const char* what, const char* file, int line) {
     return e == cudaErrorMemoryAllocation ? STG_E_NOMEM : STG_E_CUDA;
 }
 
-struct Level {
-    Geom g;
-    double vol = 1.0;       // vol of the free faces
-    double cell_vol = 1.0;  // cell vol (reported by the descriptor adapter only)
-    uint8_t* m = nullptr;
-    d4* P64 = nullptr;
-    float4* P32 = nullptr;
-    float4 *r = nullptr, *xa = nullptr, *xb = nullptr, *rr = nullptr;
-    int cur = 0;  // which of xa/xb holds the current correction
-    __nv_bfloat16* xbf = nullptr;
-    d4 *t0 = nullptr, *t1 = nullptr;  // FP64 adapter buffers (allocated on first use)
-    float4* x() { return cur ? xb : xa; }
-    float4* other() { return cur ? xa : xb; }
-};
-
 }  // namespace stg
 
 using namespace stg;
 
-// Per-kernel-class CUDA-event timing on the handle's stream.
-struct Prof {
-    bool on = false;
-    std::vector<cudaEvent_t> pool;
-    size_t used = 0;
-    struct Pending {
-        int cls;
-        size_t ev;
-        double bytes;
-    };
-    std::vector<Pending> pend;
-    long long launches[STG_PROF_NCLASS] = {};
-    double ms[STG_PROF_NCLASS] = {};
-    double bytes[STG_PROF_NCLASS] = {};
-};
-
-struct stg_ctx {
-    int dim = 3, n = 0, L = 0;
-    Prof prof;
-    cudaStream_t own_st = nullptr;
-    stg_opts opts{};
-    cudaStream_t st = nullptr;
-    cudaEvent_t e0 = nullptr, e1 = nullptr;
-    std::vector<Level> lv;  // lv[0] coarsest ... lv[L-1] finest (reference order)
-    DenseCoarse dense;
-    bool closed = true, have_boundary = false, have_penalty = false, have_rhs = false, updated = false, have_solution = false;
-    // fine-level FP64
-    d4 *b64 = nullptr, *x64 = nullptr, *r64 = nullptr, *t64 = nullptr, *lam64 = nullptr;
-    // Krylov (FP32)
-    int m = 0;
-    std::vector<float4*> V, Z;
-    float4* w = nullptr;
-    double *dscr = nullptr, *dh = nullptr, *dnrm = nullptr, *dy = nullptr;
-    // host-order staging (cells + 3 face arrays)
-    double* stage = nullptr;
-    int* istage = nullptr;
-    size_t ncell = 0, nface = 0;
-    // design loop
-    double *d_design = nullptr, *d_phys = nullptr, *d_sens = nullptr, *d_sens_design = nullptr, *d_vw = nullptr,
-           *d_tmp = nullptr, *d_gauss = nullptr, *d_parts = nullptr;
-    double vw_rmin = -1.0;
-    const double* phys_used = nullptr;
-};
-
-namespace {
+namespace stg {
 
 Level& fine(stg_t* h) { return h->lv[h->L - 1]; }
 
@@ -145,27 +88,11 @@ int prof_end(stg_t* h, int cls, double bytes, size_t ev) {
     return STG_OK;
 }
 
-#define PROF(h, cls, bytes, expr)                     \
-    do {                                              \
-        size_t ev_ = 0;                               \
-        STG_TRY(prof_begin((h), &ev_));               \
-        STG_TRY(expr);                                \
-        STG_TRY(prof_end((h), (cls), (bytes), ev_));  \
-    } while (0)
 
 int level_count(int n) {
     int low = n & -n;
     int l = (int)std::lround(std::log2((double)low)) - 1;
     return l < 1 ? 1 : l;
-}
-
-template <class T>
-int dalloc(T** p, size_t count) {
-    cudaError_t e = cudaMalloc((void**)p, sizeof(T) * (count ? count : 1));
-    if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc", __FILE__, __LINE__);
-    e = cudaMemset(*p, 0, sizeof(T) * (count ? count : 1));
-    if (e != cudaSuccess) return cuda_fail(e, "cudaMemset", __FILE__, __LINE__);
-    return STG_OK;
 }
 
 double* stage_cell(stg_t* h) { return h->stage; }
@@ -174,7 +101,7 @@ double* stage_face(stg_t* h, int d) { return h->stage + h->ncell + (size_t)d * h
 int upload_fields(stg_t* h, const double* cell, const double* const* faces, const double** dc, const double** df) {
     if (cell) STG_CK(cudaMemcpyAsync(stage_cell(h), cell, sizeof(double) * h->ncell, cudaMemcpyHostToDevice, h->st));
     *dc = cell ? stage_cell(h) : nullptr;
-    for (int d = 0; d < 3; d++) {
+    for (int d = 0; d < h->dim; d++) {
         const double* f = faces ? faces[d] : nullptr;
         if (f) STG_CK(cudaMemcpyAsync(stage_face(h, d), f, sizeof(double) * h->nface, cudaMemcpyHostToDevice, h->st));
         df[d] = f ? stage_face(h, d) : nullptr;
@@ -183,13 +110,29 @@ int upload_fields(stg_t* h, const double* cell, const double* const* faces, cons
 }
 
 int download_fields(stg_t* h, const d4* src, double* cell, double* const* faces) {
-    STG_TRY(slots_to_field64(h->st, fine(h).g, src, stage_cell(h), stage_face(h, 0), stage_face(h, 1), stage_face(h, 2)));
+    if (h->dim == 2)
+        STG_TRY(vec_to_field2d(h, src, stage_cell(h), stage_face(h, 0), stage_face(h, 1)));
+    else
+        STG_TRY(slots_to_field64(h->st, fine(h).g, src, stage_cell(h), stage_face(h, 0), stage_face(h, 1), stage_face(h, 2)));
     if (cell) STG_CK(cudaMemcpyAsync(cell, stage_cell(h), sizeof(double) * h->ncell, cudaMemcpyDeviceToHost, h->st));
-    for (int d = 0; d < 3; d++)
+    for (int d = 0; d < h->dim; d++)
         if (faces && faces[d])
             STG_CK(cudaMemcpyAsync(faces[d], stage_face(h, d), sizeof(double) * h->nface, cudaMemcpyDeviceToHost, h->st));
     STG_CK(cudaStreamSynchronize(h->st));
     return STG_OK;
+}
+
+// Field-order device arrays -> the fine-level FP64 vector of either dimension
+int fields_to_vec(stg_t* h, const double* dc, const double* const* df, d4* out) {
+    if (h->dim == 2) return field_to_vec2d(h, dc, df[0], df[1], out);
+    return field_to_slots64(h->st, fine(h).g, dc, df[0], df[1], df[2], out);
+}
+
+// out = E x on the fine level; part != nullptr also gives the per-block partials of x.out
+int energy_op(stg_t* h, const d4* x, d4* out, double* part, int* nb) {
+    if (h->dim == 2) return energy2d(h, x, out, part, nb);
+    Level& F = fine(h);
+    return op64(h->st, F.g, F.vol, x, F.m, F.P64, nullptr, out, 2, part, nb);
 }
 
 // ---------------------------------------------------------------- hierarchy set-up
@@ -277,13 +220,32 @@ int residual64(stg_t* h, const d4* b, const d4* x, d4* r, double* nrm2_host) {
     return STG_OK;
 }
 
-int solve_core(stg_t* h, const d4* b, d4* x, stg_stats* stats) {
+// 3D hooks of solve_core
+int precond3(stg_t* h, const float4* rhs, float4* out) {
     Level& F = fine(h);
-    const long long n4 = F.g.nslot;
+    // the V-cycle leaves its result in the finest level's second buffer: point it at out
+    float4* keep = F.xb;
+    F.xb = out;
+    int vrc = vcycle(h, rhs);
+    float4* res = F.x();
+    F.xb = keep;
+    STG_TRY(vrc);
+    if (res != out) STG_CK(cudaMemcpyAsync(out, res, sizeof(float4) * F.g.nslot, cudaMemcpyDeviceToDevice, h->st));
+    return STG_OK;
+}
+
+int apply3(stg_t* h, const float4* x, float4* y) {
+    Level& F = fine(h);
+    PROF(h, 4, 49.0 * F.g.box(), apply32(h->st, F.g, (float)F.vol, x, F.m, F.P32, y));
+    return STG_OK;
+}
+
+int solve_core(stg_t* h, const d4* b, d4* x, stg_stats* stats) {
+    const long long n4 = h->n4;
     stg_stats S{};
     if (!h->updated) {
         auto t0 = std::chrono::steady_clock::now();
-        STG_TRY(update(h));
+        STG_TRY(h->setup(h));
         STG_CK(cudaStreamSynchronize(h->st));
         S.setup_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     }
@@ -300,7 +262,7 @@ int solve_core(stg_t* h, const d4* b, d4* x, stg_stats* stats) {
     int status = STG_E_NOT_CONVERGED;
     for (int outer = 0; outer <= h->opts.max_outer; outer++) {
         double rn2 = 0;
-        STG_TRY(residual64(h, b, x, h->r64, &rn2));
+        STG_TRY(h->resid64(h, b, x, h->r64, &rn2));
         rn = std::sqrt(rn2);
         rel = bn > 0 ? rn / bn : 0.0;
         if (!std::isfinite(rn)) {
@@ -324,15 +286,8 @@ int solve_core(stg_t* h, const d4* b, d4* x, stg_stats* stats) {
         g[0] = beta;
         int k = 0;
         for (int j = 0; j < m; j++) {
-            // the V-cycle leaves its result in the finest level's second buffer: point it at Z[j]
-            float4* keep = F.xb;
-            F.xb = h->Z[j];
-            int vrc = vcycle(h, h->V[j]);
-            float4* res = F.x();
-            F.xb = keep;
-            STG_TRY(vrc);
-            if (res != h->Z[j]) STG_CK(cudaMemcpyAsync(h->Z[j], res, sizeof(float4) * n4, cudaMemcpyDeviceToDevice, h->st));
-            PROF(h, 4, 49.0 * F.g.box(), apply32(h->st, F.g, (float)F.vol, h->Z[j], F.m, F.P32, h->w));
+            STG_TRY(h->precond(h, h->V[j], h->Z[j]));
+            STG_TRY(h->apply32(h, h->Z[j], h->w));
             // classical Gram-Schmidt; a second pass only when the first one cancelled most
             // of w (||w_new|| < 0.7 ||w||, "twice is enough")
             PROF(h, 6, 16.0 * (j + 2) * n4, multidot32(h->st, n4, h->V.data(), j + 1, h->w, h->dh, h->dscr, h->dnrm + 1));
@@ -419,7 +374,7 @@ int check_handle(const stg_t* h) {
     return STG_OK;
 }
 
-}  // namespace
+}  // namespace stg
 
 // ====================================================================== C ABI
 extern "C" {
@@ -485,16 +440,24 @@ int stg_create(int dim, int n, const stg_opts* opts, stg_t** out) {
         return STG_E_INVALID;
     }
     *out = nullptr;
-    if (dim != 3) {
-        set_error("dim %d: this build implements the 3D path", dim);
-        return STG_E_UNSUPPORTED;
+    if (dim != 2 && dim != 3) {
+        set_error("dim %d: must be 2 or 3", dim);
+        return STG_E_INVALID;
     }
-    if (n < 4 || n % 4 != 0) {
+    if (dim == 3 && (n < 4 || n % 4 != 0)) {
         set_error("N = %d must be a positive multiple of 4", n);
         return STG_E_INVALID;
     }
-    if (n > 1024) {
+    if (dim == 3 && n > 1024) {
         set_error("N = %d exceeds the 32-bit slot indexing limit of 1024", n);
+        return STG_E_UNSUPPORTED;
+    }
+    if (dim == 2 && (n < 8 || n % 8 != 0)) {
+        set_error("N = %d must be a positive multiple of 8 (8x8-blocked 2D layout)", n);
+        return STG_E_INVALID;
+    }
+    if (dim == 2 && n > 16384) {
+        set_error("N = %d exceeds the 32-bit 2D indexing limit of 16384", n);
         return STG_E_UNSUPPORTED;
     }
     stg_t* h = new stg_t();
@@ -506,7 +469,7 @@ int stg_create(int dim, int n, const stg_opts* opts, stg_t** out) {
         stg_default_opts(&h->opts);
     if (h->opts.inner_max < 1) h->opts.inner_max = 1;
     h->m = h->opts.inner_max;
-    h->L = level_count(n);
+    h->L = dim == 3 ? level_count(n) : 0;
     int rc = STG_OK;
     auto fail = [&](int r) {
         stg_destroy(h);
@@ -520,8 +483,9 @@ int stg_create(int dim, int n, const stg_opts* opts, stg_t** out) {
     h->st = h->own_st;
     cudaEventCreate(&h->e0);
     cudaEventCreate(&h->e1);
-    h->lv.resize(h->L);
-    for (int i = h->L - 1, nn = n; i >= 0; i--, nn /= 2) {
+    if (dim == 2 && (rc = create2d(h))) return fail(rc);
+    h->lv.resize(dim == 3 ? h->L : 0);
+    for (int i = (int)h->lv.size() - 1, nn = n; i >= 0; i--, nn /= 2) {
         Level& L = h->lv[i];
         L.g = Geom::make(nn);
         size_t ns = L.g.nslot;
@@ -532,9 +496,22 @@ int stg_create(int dim, int n, const stg_opts* opts, stg_t** out) {
         // halo and absent unknowns fixed; the box is rewritten by set_boundary / coarsen
         if ((rc = mask_from_field(h->st, L.g, nullptr, nullptr, nullptr, nullptr, L.m))) return fail(rc);
     }
-    if ((rc = dense_init(h->dense, h->lv[0].g))) return fail(rc);
-    Level& F = fine(h);
-    size_t ns = F.g.nslot;
+    long long nparts = 0;
+    if (dim == 3) {
+        if ((rc = dense_init(h->dense, h->lv[0].g))) return fail(rc);
+        Level& F = fine(h);
+        h->n4 = (long long)F.g.nslot;
+        h->setup = update;
+        h->resid64 = residual64;
+        h->precond = precond3;
+        h->apply32 = apply3;
+        h->ncell = (size_t)n * n * n;
+        h->nface = (size_t)n * n * (n + 1);
+        nparts = grid_for(F.g.box(), 256);
+    } else {
+        nparts = grid_for(4 * h->n4, 256);
+    }
+    const size_t ns = (size_t)h->n4;
     if ((rc = dalloc(&h->b64, ns)) || (rc = dalloc(&h->x64, ns)) || (rc = dalloc(&h->r64, ns)) || (rc = dalloc(&h->t64, ns)) ||
         (rc = dalloc(&h->lam64, ns)) || (rc = dalloc(&h->w, ns)))
         return fail(rc);
@@ -545,10 +522,8 @@ int stg_create(int dim, int n, const stg_opts* opts, stg_t** out) {
     for (auto& p : h->Z)
         if ((rc = dalloc(&p, ns))) return fail(rc);
     if ((rc = dalloc(&h->dscr, 1216 * 16)) || (rc = dalloc(&h->dh, 2 * (h->m + 2))) || (rc = dalloc(&h->dnrm, 8)) ||
-        (rc = dalloc(&h->dy, h->m + 1)) || (rc = dalloc(&h->d_parts, (size_t)grid_for(F.g.box(), 256) + 1216)))
+        (rc = dalloc(&h->dy, h->m + 1)) || (rc = dalloc(&h->d_parts, (size_t)nparts + 1216)))
         return fail(rc);
-    h->ncell = (size_t)n * n * n;
-    h->nface = (size_t)n * n * (n + 1);
     if ((rc = dalloc(&h->stage, h->ncell + 3 * h->nface)) || (rc = dalloc(&h->istage, h->ncell + 3 * h->nface))) return fail(rc);
     if ((rc = dalloc(&h->d_design, h->ncell)) || (rc = dalloc(&h->d_phys, h->ncell)) || (rc = dalloc(&h->d_sens, h->ncell)) ||
         (rc = dalloc(&h->d_sens_design, h->ncell)) || (rc = dalloc(&h->d_vw, h->ncell)) || (rc = dalloc(&h->d_tmp, h->ncell)) ||
@@ -562,6 +537,7 @@ int stg_create(int dim, int n, const stg_opts* opts, stg_t** out) {
 int stg_destroy(stg_t* h) {
     if (!h) return STG_OK;
     if (h->st) cudaStreamSynchronize(h->st);
+    destroy2d(h);
     for (auto& L : h->lv) {
         cudaFree(L.m);
         cudaFree(L.P64);
@@ -592,9 +568,13 @@ int stg_destroy(stg_t* h) {
 }
 
 int stg_levels(const stg_t* h) { return h ? h->L : 0; }
-int stg_level_n(const stg_t* h, int level) { return (h && level >= 0 && level < h->L) ? h->lv[level].g.n : 0; }
+int stg_level_n(const stg_t* h, int level) {
+    if (!h || level < 0 || level >= h->L) return 0;
+    return h->dim == 2 ? level_n2d(h, level) : h->lv[level].g.n;
+}
 int64_t stg_level_dof(const stg_t* h, int level) {
     if (!h || level < 0 || level >= h->L) return 0;
+    if (h->dim == 2) return dof2d(h, level);
     Blocked B{h->lv[level].g.n};
     return B.size();
 }
@@ -605,6 +585,28 @@ int stg_set_boundary(stg_t* h, const double* cell_vol, const int32_t* cell_fixed
     if (!face_vol || !face_fixed) {
         set_error("face_vol and face_fixed are required");
         return STG_E_INVALID;
+    }
+    if (h->dim == 2) {
+        // the 2D kernels read every coefficient from the descriptor: any vol, fixed cells allowed
+        for (int d = 0; d < 2; d++)
+            if (!face_vol[d] || !face_fixed[d]) {
+                set_error("face arrays of axis %d missing", d);
+                return STG_E_INVALID;
+            }
+        const double* dc = nullptr;
+        const double* df[3] = {nullptr, nullptr, nullptr};
+        STG_TRY(upload_fields(h, cell_vol, face_vol, &dc, df));
+        int* ist = h->istage;
+        if (cell_fixed) STG_CK(cudaMemcpyAsync(ist, cell_fixed, sizeof(int) * h->ncell, cudaMemcpyHostToDevice, h->st));
+        for (int d = 0; d < 2; d++)
+            STG_CK(cudaMemcpyAsync(ist + h->ncell + d * h->nface, face_fixed[d], sizeof(int) * h->nface, cudaMemcpyHostToDevice,
+                                   h->st));
+        STG_TRY(set_boundary2d(h, dc, cell_fixed ? ist : nullptr, df[0], df[1], ist + h->ncell, ist + h->ncell + h->nface));
+        h->closed = closed != 0;
+        h->have_boundary = true;
+        h->updated = false;
+        STG_CK(cudaStreamSynchronize(h->st));
+        return STG_OK;
     }
     const int n = h->n;
     // the uniform-coefficient smoother needs one vol value on the free faces and no fixed cell
@@ -658,8 +660,12 @@ int stg_set_penalty(stg_t* h, const double* cell_penalty, const double* const* f
     const double* dc = nullptr;
     const double* df[3] = {nullptr, nullptr, nullptr};
     STG_TRY(upload_fields(h, cell_penalty, face_penalty, &dc, df));
-    Level& F = fine(h);
-    STG_TRY(penalty_from_field(h->st, F.g, dc, df[0], df[1], df[2], F.m, F.P64, F.P32));
+    if (h->dim == 2) {
+        STG_TRY(set_penalty2d(h, dc, df[0], df[1]));
+    } else {
+        Level& F = fine(h);
+        STG_TRY(penalty_from_field(h->st, F.g, dc, df[0], df[1], df[2], F.m, F.P64, F.P32));
+    }
     h->have_penalty = true;
     h->updated = false;
     h->phys_used = nullptr;
@@ -672,7 +678,7 @@ int stg_set_rhs(stg_t* h, const double* cell_b, const double* const* face_b) {
     const double* dc = nullptr;
     const double* df[3] = {nullptr, nullptr, nullptr};
     STG_TRY(upload_fields(h, cell_b, face_b, &dc, df));
-    STG_TRY(field_to_slots64(h->st, fine(h).g, dc, df[0], df[1], df[2], h->b64));
+    STG_TRY(fields_to_vec(h, dc, df, h->b64));
     h->have_rhs = true;
     STG_CK(cudaStreamSynchronize(h->st));
     return STG_OK;
@@ -714,7 +720,7 @@ static int energy_input(stg_t* h, const double* p, const double* const* vel, con
     const double* dc = nullptr;
     const double* df[3] = {nullptr, nullptr, nullptr};
     STG_TRY(upload_fields(h, p, vel, &dc, df));
-    STG_TRY(field_to_slots64(h->st, fine(h).g, dc, df[0], df[1], df[2], h->r64));
+    STG_TRY(fields_to_vec(h, dc, df, h->r64));
     *x = h->r64;
     return STG_OK;
 }
@@ -723,9 +729,8 @@ int stg_energy(stg_t* h, const double* p, const double* const* vel, double* J) {
     STG_TRY(check_handle(h));
     const d4* x;
     STG_TRY(energy_input(h, p, vel, &x));
-    Level& F = fine(h);
     int nb = 0;
-    STG_TRY(op64(h->st, F.g, F.vol, x, F.m, F.P64, nullptr, h->t64, 2, h->d_parts, &nb));
+    STG_TRY(energy_op(h, x, h->t64, h->d_parts, &nb));
     STG_TRY(reduce_parts(h->st, h->d_parts, nb, h->dnrm));
     double s = 0;
     STG_CK(cudaMemcpyAsync(&s, h->dnrm, sizeof(double), cudaMemcpyDeviceToHost, h->st));
@@ -738,8 +743,8 @@ int stg_energy_grad_x(stg_t* h, const double* p, const double* const* vel, doubl
     STG_TRY(check_handle(h));
     const d4* x;
     STG_TRY(energy_input(h, p, vel, &x));
-    Level& F = fine(h);
-    STG_TRY(op64(h->st, F.g, F.vol, x, F.m, F.P64, nullptr, h->t64, 2, nullptr, nullptr));
+    int nb = 0;
+    STG_TRY(energy_op(h, x, h->t64, nullptr, &nb));
     return download_fields(h, h->t64, p_grad, vel_grad);
 }
 
@@ -747,9 +752,8 @@ int stg_energy_grad_q(stg_t* h, const double* p, const double* const* vel, doubl
     STG_TRY(check_handle(h));
     const d4* x;
     STG_TRY(energy_input(h, p, vel, &x));
-    Level& F = fine(h);
     // 1/2 x^2 per unknown (fluid_topo/FluidEnergy3D.cpp:82-91)
-    STG_TRY(half_square64(h->st, F.g.nslot, x, h->t64));
+    STG_TRY(half_square64(h->st, h->n4, x, h->t64));
     return download_fields(h, h->t64, cell_q, face_q);
 }
 
@@ -761,8 +765,12 @@ int stg_set_density(stg_t* h, const double* rho, const stg_alpha* law) {
         return STG_E_INVALID;
     }
     if (rho) STG_CK(cudaMemcpyAsync(h->d_phys, rho, sizeof(double) * h->ncell, cudaMemcpyHostToDevice, h->st));
-    Level& F = fine(h);
-    STG_TRY(face_penalty_from_density(h->st, F.g, h->d_phys, *law, F.m, F.P64, F.P32));
+    if (h->dim == 2) {
+        STG_TRY(set_density2d(h, h->d_phys, *law));
+    } else {
+        Level& F = fine(h);
+        STG_TRY(face_penalty_from_density(h->st, F.g, h->d_phys, *law, F.m, F.P64, F.P32));
+    }
     h->have_penalty = true;
     h->updated = false;
     h->phys_used = h->d_phys;
@@ -776,12 +784,15 @@ int stg_adjoint_sensitivity(stg_t* h, const stg_alpha* law, double* dJ, stg_stat
         set_error("needs an alpha law, a prior stg_solve and a density set by stg_set_density");
         return STG_E_INVALID;
     }
-    Level& F = fine(h);
     // adjoint right-hand side E x, then A lambda = E x (A is symmetric)
-    STG_TRY(op64(h->st, F.g, F.vol, h->x64, F.m, F.P64, nullptr, h->t64, 2, nullptr, nullptr));
+    int nb = 0;
+    STG_TRY(energy_op(h, h->x64, h->t64, nullptr, &nb));
     int rc = solve_core(h, h->t64, h->lam64, stats);
     if (rc != STG_OK && rc != STG_E_NOT_CONVERGED) return rc;
-    STG_TRY(sensitivity(h->st, F.g, h->phys_used, *law, h->x64, h->lam64, h->d_sens));
+    if (h->dim == 2)
+        STG_TRY(sensitivity2d(h, h->phys_used, *law, h->x64, h->lam64, h->d_sens));
+    else
+        STG_TRY(sensitivity(h->st, fine(h).g, h->phys_used, *law, h->x64, h->lam64, h->d_sens));
     if (dJ) STG_CK(cudaMemcpyAsync(dJ, h->d_sens, sizeof(double) * h->ncell, cudaMemcpyDeviceToHost, h->st));
     STG_CK(cudaStreamSynchronize(h->st));
     return rc;
@@ -799,7 +810,7 @@ int stg_filter(stg_t* h, double rmin, const double* in, double* out, int transpo
         STG_CK(cudaMemcpyAsync(h->d_tmp, in, sizeof(double) * h->ncell, cudaMemcpyHostToDevice, h->st));
         src = h->d_tmp;
     }
-    STG_TRY(density_filter(h->st, h->n, rmin, src, dst, transpose));
+    STG_TRY(density_filter(h->st, h->dim, h->n, rmin, src, dst, transpose));
     if (out) STG_CK(cudaMemcpyAsync(out, dst, sizeof(double) * h->ncell, cudaMemcpyDeviceToHost, h->st));
     STG_CK(cudaStreamSynchronize(h->st));
     return STG_OK;
@@ -813,7 +824,7 @@ int stg_oc_update(stg_t* h, double rmin, const double* x, const double* dc, doub
         // vw_j = sum_i w_ij / W_i: the filtered volume is sum_j vw_j x_j
         std::vector<double> ones(h->ncell, 1.0);
         STG_CK(cudaMemcpyAsync(h->d_tmp, ones.data(), sizeof(double) * h->ncell, cudaMemcpyHostToDevice, h->st));
-        STG_TRY(density_filter(h->st, h->n, rmin, h->d_tmp, h->d_vw, 1));
+        STG_TRY(density_filter(h->st, h->dim, h->n, rmin, h->d_tmp, h->d_vw, 1));
         STG_CK(cudaStreamSynchronize(h->st));
         h->vw_rmin = rmin;
     }
@@ -863,7 +874,7 @@ int stg_density_noise(stg_t* h, uint64_t seed, double sigma, double* out) {
         for (auto& v : w) v /= s;
         STG_CK(cudaMemcpyAsync(h->d_gauss, w.data(), sizeof(double) * w.size(), cudaMemcpyHostToDevice, h->st));
     }
-    STG_TRY(density_noise(h->st, h->n, seed, h->d_gauss, R, h->d_design, h->d_tmp));
+    STG_TRY(density_noise(h->st, h->dim, h->n, seed, h->d_gauss, R, h->d_design, h->d_tmp));
     if (out) STG_CK(cudaMemcpyAsync(out, h->d_design, sizeof(double) * h->ncell, cudaMemcpyDeviceToHost, h->st));
     STG_CK(cudaStreamSynchronize(h->st));
     return STG_OK;
@@ -876,7 +887,12 @@ int stg_apply_A_device(stg_t* h, int level, double* d_Ap, const double* d_p) {
         set_error("bad level or pointer");
         return STG_E_INVALID;
     }
-    if (level < h->L - 1 && !h->updated) STG_TRY(update(h));
+    if (level < h->L - 1 && !h->updated) STG_TRY(h->setup(h));
+    if (h->dim == 2) {
+        STG_TRY(apply_A2d(h, level, d_Ap, d_p));
+        STG_CK(cudaStreamSynchronize(h->st));
+        return STG_OK;
+    }
     Level& L = h->lv[level];
     STG_TRY(ensure_adapter(L));
     STG_TRY(blocked_to_slots64(h->st, L.g, d_p, L.t0));
@@ -889,6 +905,11 @@ int stg_apply_A_device(stg_t* h, int level, double* d_Ap, const double* d_p) {
 
 int stg_apply_E_device(stg_t* h, double* d_Ap, const double* d_p) {
     STG_TRY(check_handle(h));
+    if (h->dim == 2) {
+        STG_TRY(apply_E2d(h, d_Ap, d_p));
+        STG_CK(cudaStreamSynchronize(h->st));
+        return STG_OK;
+    }
     Level& L = fine(h);
     STG_TRY(ensure_adapter(L));
     STG_TRY(blocked_to_slots64(h->st, L.g, d_p, L.t0));
@@ -900,14 +921,19 @@ int stg_apply_E_device(stg_t* h, double* d_Ap, const double* d_p) {
 
 int stg_update(stg_t* h) {
     STG_TRY(check_handle(h));
-    STG_TRY(update(h));
+    STG_TRY(h->setup(h));
     STG_CK(cudaStreamSynchronize(h->st));
     return STG_OK;
 }
 
 int stg_vcycle_device(stg_t* h, double* d_out, const double* d_in) {
     STG_TRY(check_handle(h));
-    if (!h->updated) STG_TRY(update(h));
+    if (!h->updated) STG_TRY(h->setup(h));
+    if (h->dim == 2) {
+        STG_TRY(vcycle2d(h, d_out, d_in));
+        STG_CK(cudaStreamSynchronize(h->st));
+        return STG_OK;
+    }
     Level& F = fine(h);
     STG_TRY(ensure_adapter(F));
     STG_TRY(blocked_to_slots64(h->st, F.g, d_in, F.t0));
@@ -925,7 +951,12 @@ int stg_apply_op_device(stg_t* h, int op, int level, double* d_out, const double
         set_error("bad level or pointer");
         return STG_E_INVALID;
     }
-    if (!h->updated) STG_TRY(update(h));
+    if (!h->updated) STG_TRY(h->setup(h));
+    if (h->dim == 2) {
+        STG_TRY(apply_op2d(h, op, level, d_out, d_in));
+        STG_CK(cudaStreamSynchronize(h->st));
+        return STG_OK;
+    }
     Level& L = h->lv[level];
     STG_TRY(ensure_adapter(L));
     switch (op) {
@@ -988,7 +1019,12 @@ int stg_level_descr_device(stg_t* h, int level, double* d_vol, double* d_penalty
         set_error("bad level");
         return STG_E_INVALID;
     }
-    if (!h->updated) STG_TRY(update(h));
+    if (!h->updated) STG_TRY(h->setup(h));
+    if (h->dim == 2) {
+        STG_TRY(level_descr2d(h, level, d_vol, d_penalty, d_fixed));
+        STG_CK(cudaStreamSynchronize(h->st));
+        return STG_OK;
+    }
     Level& L = h->lv[level];
     STG_TRY(ensure_adapter(L));
     if (d_penalty) STG_TRY(slots_to_blocked64(h->st, L.g, L.P64, d_penalty, nullptr));

@@ -2,9 +2,10 @@
 // the adjoint chain rule (FluidTopoOpt3D::Update_Grad), the density filter, the
 // optimality-criteria volume pass and the seeded density generator.
 //
-// Cell arrays are in the simplex Field order, (i*N + j)*N + k.
+// Cell arrays are in the simplex Field order: (i*N + j)*N + k in 3D, i*N + j in 2D.
 #include <math.h>
 
+#include "alpha.cuh"
 #include "kernels.h"
 #include "stencil.cuh"
 
@@ -13,23 +14,6 @@ namespace stg {
 namespace {
 
 constexpr int TPB = 256;
-
-__device__ __forceinline__ double alpha_of(double r, const stg_alpha& L) {
-    if (L.law == STG_ALPHA_REF) {
-        double s = r * r * r;
-        return L.alpha_os + (L.alpha_us - L.alpha_os) * s * (1 + L.q) / (s + L.q);
-    }
-    return L.amax * 0.1 * (1.0 - r) / (0.1 + r);
-}
-// d alpha / d rho including the rho^3 chain of the reference law (FluidTopoOpt3D.cpp:202-208, 273)
-__device__ __forceinline__ double dalpha_of(double r, const stg_alpha& L) {
-    if (L.law == STG_ALPHA_REF) {
-        double s = r * r * r;
-        double da = (L.alpha_us - L.alpha_os) * ((1 + L.q) / (s + L.q) - s * (1 + L.q) / ((s + L.q) * (s + L.q)));
-        return da * 3.0 * (r * r);
-    }
-    return -L.amax * 0.1 * 1.1 / ((0.1 + r) * (0.1 + r));
-}
 
 __device__ __forceinline__ long long cidx(int n, int i, int j, int k) { return ((long long)i * n + j) * n + k; }
 
@@ -77,17 +61,20 @@ __global__ void k_sensitivity(Geom g, const double* __restrict__ rho, stg_alpha 
 }
 
 // Linear hat filter: out_i = sum_j w_ij in_j / W_i (forward) or sum_j w_ji in_j / W_j (transpose).
-__global__ void k_filter(int n, double rmin, int R, const double* __restrict__ in, double* __restrict__ out, int transpose) {
+// dim 2 runs the same loops with a single k plane (nz = 1, no k offsets).
+__global__ void k_filter(int n, int nz, double rmin, int R, int Rz, const double* __restrict__ in, double* __restrict__ out,
+                         int transpose) {
     long long t = (long long)blockIdx.x * TPB + threadIdx.x;
-    if (t >= (long long)n * n * n) return;
-    int k = (int)(t % n), j = (int)((t / n) % n), i = (int)(t / ((long long)n * n));
+    if (t >= (long long)n * n * nz) return;
+    int k = (int)(t % nz), j = (int)((t / nz) % n), i = (int)(t / ((long long)n * nz));
+    auto at = [&](int a, int b, int c) { return ((long long)a * n + b) * nz + c; };
     auto wsum = [&](int a0, int b0, int c0) {
         double W = 0;
         for (int a = -R; a <= R; a++)
             for (int b = -R; b <= R; b++)
-                for (int c = -R; c <= R; c++) {
+                for (int c = -Rz; c <= Rz; c++) {
                     int ii = a0 + a, jj = b0 + b, kk = c0 + c;
-                    if (ii < 0 || jj < 0 || kk < 0 || ii >= n || jj >= n || kk >= n) continue;
+                    if (ii < 0 || jj < 0 || kk < 0 || ii >= n || jj >= n || kk >= nz) continue;
                     double w = rmin - sqrt((double)(a * a + b * b + c * c));
                     if (w > 0) W += w;
                 }
@@ -96,15 +83,15 @@ __global__ void k_filter(int n, double rmin, int R, const double* __restrict__ i
     double W = transpose ? 0.0 : wsum(i, j, k), s = 0;
     for (int a = -R; a <= R; a++)
         for (int b = -R; b <= R; b++)
-            for (int c = -R; c <= R; c++) {
+            for (int c = -Rz; c <= Rz; c++) {
                 int ii = i + a, jj = j + b, kk = k + c;
-                if (ii < 0 || jj < 0 || kk < 0 || ii >= n || jj >= n || kk >= n) continue;
+                if (ii < 0 || jj < 0 || kk < 0 || ii >= n || jj >= n || kk >= nz) continue;
                 double w = rmin - sqrt((double)(a * a + b * b + c * c));
                 if (w <= 0) continue;
                 if (transpose)
-                    s += w * in[cidx(n, ii, jj, kk)] / wsum(ii, jj, kk);
+                    s += w * in[at(ii, jj, kk)] / wsum(ii, jj, kk);
                 else
-                    s += w * in[cidx(n, ii, jj, kk)];
+                    s += w * in[at(ii, jj, kk)];
             }
     out[t] = transpose ? s : s / W;
 }
@@ -151,10 +138,9 @@ __global__ void k_uniform(long long nc, uint64_t seed, double* __restrict__ out)
 }
 
 // 1D Gaussian along one axis (stride), clamp-to-edge; clip after the last axis
-__global__ void k_blur(int n, long long stride, const double* __restrict__ w, int R, const double* __restrict__ in,
+__global__ void k_blur(int n, long long nc, long long stride, const double* __restrict__ w, int R, const double* __restrict__ in,
                        double* __restrict__ out, int clip) {
     long long t = (long long)blockIdx.x * TPB + threadIdx.x;
-    long long nc = (long long)n * n * n;
     if (t >= nc) return;
     int c = (int)((t / stride) % n);
     double acc = 0;
@@ -182,11 +168,12 @@ int sensitivity(cudaStream_t st, const Geom& g, const double* rho, const stg_alp
     return STG_OK;
 }
 
-int density_filter(cudaStream_t st, int n, double rmin, const double* in, double* out, int transpose) {
+int density_filter(cudaStream_t st, int dim, int n, double rmin, const double* in, double* out, int transpose) {
     int R = (int)ceil(rmin) - 1;
     if (R < 0) R = 0;
-    long long nc = (long long)n * n * n;
-    k_filter<<<grid_for(nc, TPB), TPB, 0, st>>>(n, rmin, R, in, out, transpose);
+    const int nz = dim == 3 ? n : 1;
+    long long nc = (long long)n * n * nz;
+    k_filter<<<grid_for(nc, TPB), TPB, 0, st>>>(n, nz, rmin, R, dim == 3 ? R : 0, in, out, transpose);
     STG_LAUNCH_CK();
     return STG_OK;
 }
@@ -202,24 +189,24 @@ int oc_volume(cudaStream_t st, int ncell, const double* x, const double* dc, con
     return STG_OK;
 }
 
-int density_noise(cudaStream_t st, int n, uint64_t seed, const double* w, int R, double* out, double* tmp) {
-    long long nc = (long long)n * n * n;
+int density_noise(cudaStream_t st, int dim, int n, uint64_t seed, const double* w, int R, double* out, double* tmp) {
+    long long nc = dim == 3 ? (long long)n * n * n : (long long)n * n;
     unsigned gb = grid_for(nc, TPB);
     k_uniform<<<gb, TPB, 0, st>>>(nc, seed, out);
     STG_LAUNCH_CK();
     if (R >= 0 && w) {
-        long long strides[3] = {(long long)n * n, n, 1};
+        const long long strides3[3] = {(long long)n * n, n, 1}, strides2[2] = {n, 1};
         double* a = out;
         double* b = tmp;
-        for (int ax = 0; ax < 3; ax++) {
-            k_blur<<<gb, TPB, 0, st>>>(n, strides[ax], w, R, a, b, ax == 2);
+        for (int ax = 0; ax < dim; ax++) {
+            k_blur<<<gb, TPB, 0, st>>>(n, nc, dim == 3 ? strides3[ax] : strides2[ax], w, R, a, b, ax == dim - 1);
             STG_LAUNCH_CK();
             double* c = a;
             a = b;
             b = c;
         }
-        // three passes leave the result in tmp
-        STG_CK(cudaMemcpyAsync(out, a, sizeof(double) * nc, cudaMemcpyDeviceToDevice, st));
+        // an odd number of passes leaves the result in tmp
+        if (a != out) STG_CK(cudaMemcpyAsync(out, a, sizeof(double) * nc, cudaMemcpyDeviceToDevice, st));
     }
     return STG_OK;
 }

@@ -6,8 +6,12 @@ ref_grid3d_index.npz   blocked-layout index tables produced by the reference's O
 oracle_n8.npz          oracle outputs on a seeded 8^3 problem (A x, E x, a V-cycle, the
                        solution to 1e-12) as a regression fixture for the oracle and
                        the GPU path.
+ref_grid2d_index.npz   the 2D blocked-layout tables produced by the reference's own grid2D
+                       host code (oracle/_ref/libref_grid2d.so).
+oracle2d_n16.npz       2D oracle outputs on a seeded 16^2 problem (same contents as the
+                       3D fixture).
 
-usage: python tests/golden/make_golden.py
+usage: python tests/golden/make_golden.py [3d] [2d]
 """
 import ctypes
 import os
@@ -73,7 +77,50 @@ def oracle_regression():
                         b=bb, vcycle_b=o.vcycle(bb), solution=sol, rel_true=st["rel_true"])
 
 
+def ref_index_tables_2d():
+    lib = ctypes.CDLL(os.path.join(ROOT, "oracle", "_ref", "libref_grid2d.so"))
+    out = {}
+    for n in (8, 16, 32):
+        out[f"cell_ind_{n}"] = np.array([[x, y, lib.ref2_cell_ind(n, x, y)] for x in range(n) for y in range(n)],
+                                        dtype=np.int32)
+        for d in range(2):
+            out[f"face_ind_{n}_{d}"] = np.array([[x, y, lib.ref2_face_ind(n, x, y, d)] for x in range(n + 8 * (d == 0))
+                                                 for y in range(n + 8 * (d == 1))], dtype=np.int32)
+            out[f"face_size_{n}_{d}"] = np.array([lib.ref2_face_size(n, d)], dtype=np.int32)
+        out[f"node_ind_{n}"] = np.array([[x, y, lib.ref2_node_ind(n, x, y)] for x in range(n + 8) for y in range(n + 8)],
+                                        dtype=np.int32)
+        xy = (ctypes.c_int * 2)()
+        inv = []
+        for i in range(lib.ref2_cell_size(n)):
+            lib.ref2_ind_cell(n, i, xy)
+            inv.append([i, xy[0], xy[1]])
+        out[f"ind_cell_{n}"] = np.array(inv, dtype=np.int32)
+    np.savez_compressed(os.path.join(HERE, "ref_grid2d_index.npz"), **out)
+
+
+def oracle_regression_2d():
+    from oracle import pyoracle as po
+    from tests.helpers import problem2
+
+    n = 16
+    b, rho, phys, fp = problem2(po, n, seed=11, sigma=2.0)
+    o = po.Steady2D(n)
+    o.init_boundary(b)
+    o.update_penalty(np.zeros((n, n)), fp)
+    o.update_b(b.cell_b, b.face_b)
+    x = np.random.default_rng(12).standard_normal(o.level_dof(o.levels - 1))
+    bb = po.field_to_blocked2(n, b.cell_b, b.face_b)
+    sol, st = o.solve(max_iter=60, abs_thr=0.0, rel_thr=1e-14, norm_thr=0.0, restarts=4, true_tol=1e-12)
+    np.savez_compressed(os.path.join(HERE, "oracle2d_n16.npz"), rho=rho, x=x, Ax=o.apply_A(x), Ex=o.apply_E(x), b=bb,
+                        vcycle_b=o.vcycle(bb), solution=sol, rel_true=st["rel_true"])
+
+
 if __name__ == "__main__":
-    ref_index_tables()
-    oracle_regression()
+    what = sys.argv[1:] or ["3d", "2d"]
+    if "3d" in what:
+        ref_index_tables()
+        oracle_regression()
+    if "2d" in what:
+        ref_index_tables_2d()
+        oracle_regression_2d()
     print("wrote", os.listdir(HERE))

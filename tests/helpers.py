@@ -17,6 +17,22 @@ def problem(po, n, seed=1, sigma=2.0, law="bp", bc="parabolic"):
     return b, rho, phys, fp
 
 
+def problem2(po, n, seed=1, sigma=2.0, law="bp", bc="parabolic"):
+    """2D counterpart of problem(): parabolic inlet on a centred n/4 segment (16 cells at
+    64^2) or the reference's 2D test 0, seeded density, BP or reference alpha law."""
+    b = po.bc_parabolic(n, 2, width=n // 4) if bc == "parabolic" else po.bc_test0_2d(n)
+    rho = po.density_noise(n, seed, sigma, dim=2)
+    if law == "bp":
+        rf = po.filt(rho, 1.5)
+        fp = po.face_penalty(rf, 1, [1e4], dim=2)
+        phys = rf
+    else:
+        prm = [5e2 / (n / 32.0), 1e-3, 0.014]
+        fp = po.face_penalty(rho, 0, prm, dim=2)
+        phys = rho
+    return b, rho, phys, fp
+
+
 def relerr(a, b):
     a = np.asarray(a, dtype=np.float64).ravel()
     b = np.asarray(b, dtype=np.float64).ravel()

@@ -1,0 +1,196 @@
+"""CPU tests of the 2D oracle: layout pinned against the reference's own grid2D code,
+regression against the committed fixture, and the structure the 2D GPU kernels rely on
+(A and E symmetric on the free unknowns, adjoint transfers, one smoother colour per box
+colour, the closed coarsest matrix, GMRES convergence, the adjoint gradient, 2D filter
+and noise)."""
+import os
+
+import numpy as np
+import pytest
+
+from tests.helpers import problem2, relerr
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def _setup(po, n, **kw):
+    b, rho, phys, fp = problem2(po, n, **kw)
+    o = po.Steady2D(n)
+    o.init_boundary(b)
+    o.update_penalty(np.zeros((n, n)), fp)
+    o.update_b(b.cell_b, b.face_b)
+    return b, o
+
+
+def test_layout_2d_matches_reference_index_tables(oracle):
+    """Blocked layout of common_cpx/form01mapping.cu:10-57, tables from the reference's code."""
+    L = oracle._lib2()
+    tab = np.load(os.path.join(GOLD, "ref_grid2d_index.npz"))
+    for n in (8, 16, 32):
+        for x, y, idx in tab[f"cell_ind_{n}"]:
+            assert L.orc2_index(n, 0, int(x), int(y), 0) == idx
+        for d in range(2):
+            for x, y, idx in tab[f"face_ind_{n}_{d}"]:
+                assert L.orc2_index(n, 1, int(x), int(y), d) == idx
+        for x, y, idx in tab[f"node_ind_{n}"]:
+            assert L.orc2_index(n, 2, int(x), int(y), 0) == idx
+        sizes = n * n + int(tab[f"face_size_{n}_0"][0]) + int(tab[f"face_size_{n}_1"][0])
+        assert oracle.dof2(n) == sizes
+        # ind_cell is the inverse of cell_ind
+        cells = {(int(x), int(y)): int(i) for x, y, i in tab[f"cell_ind_{n}"]}
+        for i, x, y in tab[f"ind_cell_{n}"]:
+            assert cells[(int(x), int(y))] == i
+
+
+def test_field_blocked_round_trip_2d(oracle):
+    n = 16
+    rng = np.random.default_rng(0)
+    c = rng.standard_normal((n, n))
+    f = [rng.standard_normal((n + 1, n)), rng.standard_normal((n, n + 1))]
+    v = oracle.field_to_blocked2(n, c, f)
+    c2, f2 = oracle.blocked_to_field2(n, v)
+    assert np.array_equal(c, c2) and all(np.array_equal(a, b) for a, b in zip(f, f2))
+
+
+def test_oracle2d_regression_fixture(oracle):
+    g = np.load(os.path.join(GOLD, "oracle2d_n16.npz"))
+    n = 16
+    b, o = _setup(oracle, n, seed=11, sigma=2.0)
+    _, rho, _, _ = problem2(oracle, n, seed=11, sigma=2.0)
+    assert np.array_equal(rho, g["rho"])
+    assert relerr(o.apply_A(g["x"]), g["Ax"]) < 1e-14
+    assert relerr(o.apply_E(g["x"]), g["Ex"]) < 1e-14
+    assert relerr(o.vcycle(g["b"]), g["vcycle_b"]) < 1e-12
+
+
+@pytest.mark.parametrize("bc", ["parabolic", "test0"])
+def test_operators_symmetric_2d(oracle, bc):
+    b, o = _setup(oracle, 32, bc=bc)
+    rng = np.random.default_rng(1)
+    for lvl in range(o.levels):
+        m = o.level_dof(lvl)
+        free = 1 - o.descr(lvl)[2]
+        # fixed rows are zero while the curl-curl reads fixed velocities (no definite fix in
+        # 2D), so A is symmetric on the free unknowns, where the solver works
+        x, y = rng.standard_normal(m) * free, rng.standard_normal(m) * free
+        a = y @ o.apply_A(x, lvl)
+        assert abs(a - x @ o.apply_A(y, lvl)) < 1e-12 * abs(a)
+    m = o.level_dof(o.levels - 1)
+    free = 1 - o.descr(o.levels - 1)[2]
+    x, y = rng.standard_normal(m) * free, rng.standard_normal(m) * free
+    e = y @ o.apply_E(x)
+    assert abs(e - x @ o.apply_E(y)) < 1e-12 * abs(e)
+    assert x @ o.apply_E(x) > 0
+
+
+def test_coarsening_doubles_lap_and_sums_penalty(oracle):
+    n = 32
+    b, o = _setup(oracle, n)
+    laps = [o.descr(l)[3] for l in range(o.levels)]
+    assert laps == [2.0 ** (o.levels - 1 - l) for l in range(o.levels)]
+    vol_f, pen_f, fix_f, _ = o.descr(o.levels - 1)
+    vol_c, pen_c, fix_c, _ = o.descr(o.levels - 2)
+    # total penalty is conserved on the faces that stay free
+    assert pen_c.sum() <= pen_f.sum() + 1e-9
+    assert np.all(vol_c[fix_c == 1] == 0) and np.all(pen_c[fix_c == 1] == 0)
+
+
+def test_transfers_are_adjoint_2d(oracle):
+    b, o = _setup(oracle, 32)
+    rng = np.random.default_rng(2)
+    for lvl in range(o.levels - 1):
+        ff = o.descr(lvl + 1)[2]
+        fc = o.descr(lvl)[2]
+        r = rng.standard_normal(o.level_dof(lvl + 1)) * (1 - ff)
+        xc = rng.standard_normal(o.level_dof(lvl)) * (1 - fc)
+        assert abs(o.restrict(lvl, r) @ xc - r @ o.prolong(lvl, xc)) < 1e-12 * np.linalg.norm(r) * np.linalg.norm(xc)
+
+
+def test_smoother_colour_touches_one_colour_of_boxes(oracle):
+    """One colour writes the 5 unknowns of every box of that colour and nothing else;
+    the two colours together cover every cell."""
+    n = 16
+    b, o = _setup(oracle, n)
+    lvl = o.levels - 1
+    m = o.level_dof(lvl)
+    r = np.random.default_rng(3).standard_normal(m)
+    d0 = o.smooth_colour(lvl, 0, r)
+    d1 = o.smooth_colour(lvl, 1, r)
+    cells0 = d0[: n * n] != 0
+    cells1 = d1[: n * n] != 0
+    assert not np.any(cells0 & cells1)
+    assert np.all(cells0 | cells1)
+    # smoothing is a contraction on the error for the preconditioned operator (sanity)
+    s = o.smooth(lvl, 0, r)
+    assert np.linalg.norm(r - o.apply_A(s, lvl)) < np.linalg.norm(r)
+
+
+def test_coarsest_solve_inverts_closed_matrix_2d(oracle):
+    n = 8  # single level: the coarsest matrix is the fine one
+    b, o = _setup(oracle, n)
+    assert o.levels == 1 and o.coarse_info() == 0
+    m = o.level_dof(0)
+    fixed = o.descr(0)[2]
+    r = np.random.default_rng(4).standard_normal(m) * (1 - fixed)
+    x = o.coarse_apply(r)
+    res = o.apply_A(x, 0) - r
+    # closed: every pressure row of the assembled matrix adds sum(p) (StokeFlowDirectSolve.cpp:45-48)
+    res[: n * n] += x[: n * n].sum()
+    assert np.linalg.norm(res) < 1e-10 * np.linalg.norm(r)
+
+
+@pytest.mark.parametrize("n,bc", [(32, "parabolic"), (64, "parabolic"), (64, "test0")])
+def test_gmres_2d_reaches_tight_tolerance(oracle, n, bc):
+    b, o = _setup(oracle, n, bc=bc)
+    x, st = o.solve(max_iter=60, abs_thr=0.0, rel_thr=1e-13, norm_thr=0.0, restarts=3, true_tol=1e-10)
+    assert st["rel_true"] < 1e-10
+
+
+def test_adjoint_gradient_2d_matches_central_differences(oracle):
+    """Central differences on the design (fluid_topo/FluidTopoOpt.cpp:201-216), reference law."""
+    n = 16
+    b = oracle.bc_parabolic(n, 2, width=4)
+    rho = 0.3 + 0.4 * oracle.density_noise(n, 3, 1.0, dim=2)
+    prm = [5e2 / (n / 32.0), 1e-3, 0.014]
+
+    def objective(r):
+        fp = oracle.face_penalty(r, 0, prm, dim=2)
+        o = oracle.Steady2D(n)
+        o.init_boundary(b)
+        o.update_penalty(np.zeros((n, n)), fp)
+        o.update_b(b.cell_b, b.face_b)
+        x, st = o.solve(max_iter=60, abs_thr=0.0, rel_thr=1e-14, norm_thr=0.0, restarts=4, true_tol=1e-13)
+        return o, x, o.energy(x)
+
+    o, x, J = objective(rho)
+    o.set_b_blocked(o.apply_E(x))
+    lam, _ = o.solve(max_iter=60, abs_thr=0.0, rel_thr=1e-14, norm_thr=0.0, restarts=4, true_tol=1e-13)
+    _, u = oracle.blocked_to_field2(n, x)
+    _, la = oracle.blocked_to_field2(n, lam)
+    g = oracle.sensitivity(rho, 0, prm, u, la, dim=2)
+    h = 1e-5
+    for c in [(1, 3), (8, 8), (12, 5)]:
+        rp, rm = rho.copy(), rho.copy()
+        rp[c] += h
+        rm[c] -= h
+        num = (objective(rp)[2] - objective(rm)[2]) / (2 * h)
+        assert abs(num - g[c]) <= 1e-4 * max(abs(num), 1e-3 * abs(J))
+
+
+def test_filter_and_noise_2d(oracle):
+    n = 16
+    one = np.ones((n, n))
+    assert np.allclose(oracle.filt(one, 1.5), 1.0)
+    rng = np.random.default_rng(5)
+    a, c = rng.random((n, n)), rng.random((n, n))
+    assert abs((oracle.filt(a, 1.5) * c).sum() - (a * oracle.filt(c, 1.5, transpose=True)).sum()) < 1e-12
+    # rmin 1.5 in 2D: weights 1.5 (centre), 0.5 (4 edge neighbours), 1.5 - sqrt(2) (4 corners)
+    wc = 1.5 - np.sqrt(2.0)
+    W = 1.5 + 4 * 0.5 + 4 * wc
+    i, j = 7, 9
+    man = (1.5 * a[i, j] + 0.5 * (a[i - 1, j] + a[i + 1, j] + a[i, j - 1] + a[i, j + 1]) +
+           wc * (a[i - 1, j - 1] + a[i - 1, j + 1] + a[i + 1, j - 1] + a[i + 1, j + 1])) / W
+    assert abs(oracle.filt(a, 1.5)[i, j] - man) < 1e-14
+    r = oracle.density_noise(32, 0, 3.0, dim=2)
+    assert r.shape == (32, 32) and r.min() >= 0 and r.max() <= 1
+    assert np.array_equal(r, oracle.density_noise(32, 0, 3.0, dim=2))
