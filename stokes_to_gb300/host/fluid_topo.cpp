@@ -1,0 +1,231 @@
+// fluid_topo: command-line driver of the flow topology optimization, drop-in for the
+// reference's fluid_topo (fluid_topo/main.cpp:14-59) on libstokes_gb300.
+//
+//   fluid_topo -driver {0,1} -test k -s N -o dir -frac f -lf iterations
+//
+// takes the reference's flags with the reference's defaults (-driver 1, -test 2, -s 64,
+// -lf 200, -o output; -frac has no usable default there and must be given in (0, 1]).
+// -driver 0 runs the 2D problem (FluidTopoOptDriver), 1 the 3D one (FluidTopoOptDriver3D).
+// Tests: 0 = the reference's test 0 (2D: one inlet, 16 outlets; 3D: the 64^3 patch case),
+// 1 = parabolic inlet on a centred N/4 segment / patch with a mirrored outlet,
+// 2 = the reference default (no boundary data; the solve returns zero).
+// The design update is the optimality-criteria step with a linear hat filter (the
+// reference runs MMA, simplex/src/optimization/OptimizerMma.h:96-128); extra flags:
+//   -rmin r     filter radius in cells (default 1.5; r <= 1 leaves the design unfiltered)
+//   -law ref|bp Brinkman law: the reference's alpha on rho^3 (FluidTopoOpt3D.cpp:110-123,
+//               default for test 0) or amax 0.1 (1 - rho)/(0.1 + rho) (default otherwise)
+//   -amax a     BP law maximum (1e4);  -move m  OC move limit (0.2)
+//   -tol t      FP64 relative residual of every solve (1e-8 in 3D, 1e-10 in 2D)
+//   -method plain|mixed   solver precision form (plain)
+//   -init uniform|noise   initial design: frac everywhere, or seeded smoothed noise
+//   -seed s -sigma g      noise seed and Gaussian width in cells (1, 4)
+//   -frames k   write the design every k iterations (0: final only)
+//   -dump_boundary dir   write the boundary arrays of the test to dir and exit (no GPU)
+// Output in -o: log.csv (iteration, objective, volume, change, V-cycles, solve times)
+// and, per written frame f, f/x.bin and f/velocity.bin (little-endian float64 in Field
+// order: the design, then the d face-velocity arrays) with f/info.txt giving N and d.
+#include <sys/stat.h>
+
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <iostream>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "stokes_gb300.hpp"
+
+namespace {
+
+struct Args {
+    std::map<std::string, std::string> kv;
+    std::string get(const std::string& k, const std::string& def) const {
+        auto it = kv.find(k);
+        return it == kv.end() ? def : it->second;
+    }
+    int geti(const std::string& k, int def) const { return std::stoi(get(k, std::to_string(def))); }
+    double getd(const std::string& k, double def) const {
+        auto it = kv.find(k);
+        return it == kv.end() ? def : std::stod(it->second);
+    }
+    bool has(const std::string& k) const { return kv.count(k) != 0; }
+};
+
+Args parse(int argc, char** argv) {
+    static const char* known[] = {"-o",   "-s",    "-test", "-driver", "-lf",  "-frac",   "-rmin",  "-law",   "-amax",
+                                  "-move", "-tol", "-method", "-init", "-seed", "-sigma", "-frames", "-verbose",
+                                  "-dump_boundary"};
+    Args a;
+    for (int i = 1; i < argc; i++) {
+        std::string k = argv[i];
+        bool ok = false;
+        for (const char* q : known) ok = ok || k == q;
+        if (!ok || i + 1 >= argc) throw stg::Error(STG_E_INVALID, "unknown flag or missing value: " + k);
+        a.kv[k] = argv[++i];
+    }
+    return a;
+}
+
+void make_dir(const std::string& d) {
+    std::string cur;
+    for (size_t i = 0; i <= d.size(); i++) {
+        if (i == d.size() || d[i] == '/') {
+            if (!cur.empty()) mkdir(cur.c_str(), 0755);
+        }
+        if (i < d.size()) cur += d[i];
+    }
+}
+
+void write_raw(const std::string& path, const std::vector<const std::vector<double>*>& arrays) {
+    std::ofstream f(path, std::ios::binary);
+    for (auto* a : arrays) f.write(reinterpret_cast<const char*>(a->data()), (std::streamsize)(a->size() * sizeof(double)));
+    if (!f) throw stg::Error(STG_E_INVALID, "cannot write " + path);
+}
+
+double now_ms() {
+    using namespace std::chrono;
+    return duration<double, std::milli>(steady_clock::now().time_since_epoch()).count();
+}
+
+template <int d>
+int run(const Args& a) {
+    const int n = a.geti("-s", 64);
+    const int test = a.geti("-test", 2);
+    const int iters = a.geti("-lf", 200);
+    const double frac = a.getd("-frac", -1.0);
+    if (!(frac > 0.0 && frac <= 1.0)) throw stg::Error(STG_E_INVALID, "-frac must be given in (0, 1]");
+    double rmin = a.getd("-rmin", 1.5);
+    if (rmin <= 1.0) rmin = 0.5;  // radius below one cell: the hat filter is the identity
+    const std::string law_s = a.get("-law", test == 0 ? "ref" : "bp");
+    const double move = a.getd("-move", 0.2);
+    const std::string out = a.get("-o", "output");
+    const int frames = a.geti("-frames", 0);
+
+    stg_opts opts;
+    stg_default_opts(&opts);
+    opts.tol = a.getd("-tol", d == 3 ? 1e-8 : 1e-10);
+    opts.method = a.get("-method", "plain") == "mixed" ? STG_METHOD_MIXED : STG_METHOD_PLAIN;
+    opts.verbose = a.geti("-verbose", 0);
+
+    stg_alpha law{};
+    if (law_s == "ref") {
+        // FluidTopoOpt3D.h:42-46 and Init (alpha_os scaled by 32/N); FluidTopoOpt.h:43-46 in 2D
+        law = stg_alpha{STG_ALPHA_REF, 5e2 / (n / 32.0), 1e-3, d == 3 ? 0.01 : 0.014, 0.0};
+    } else if (law_s == "bp") {
+        law = stg_alpha{STG_ALPHA_BP, 0.0, 0.0, 0.0, a.getd("-amax", 1e4)};
+    } else {
+        throw stg::Error(STG_E_INVALID, "-law must be ref or bp");
+    }
+
+    stg::Boundary<d> b;
+    if (test == 0)
+        b = stg::boundary_test0<d>(n);
+    else if (test == 1)
+        b = stg::boundary_parabolic<d>(n, n / 4);
+    else {
+        b.resize(n);  // reference default: empty boundary data
+        std::fill(b.cell_vol.begin(), b.cell_vol.end(), 1.0);
+        for (auto& f : b.face_vol) std::fill(f.begin(), f.end(), 1.0);
+    }
+
+    if (a.has("-dump_boundary")) {
+        // cell_vol, cell_b, face_vol[d], face_b[d] as float64, then cell_fixed, face_fixed[d] as int32
+        const std::string dir = a.get("-dump_boundary", ".");
+        make_dir(dir);
+        std::vector<const std::vector<double>*> dv = {&b.cell_vol, &b.cell_b};
+        for (int q = 0; q < d; q++) dv.push_back(&b.face_vol[q]);
+        for (int q = 0; q < d; q++) dv.push_back(&b.face_b[q]);
+        write_raw(dir + "/boundary_f64.bin", dv);
+        std::ofstream f(dir + "/boundary_i32.bin", std::ios::binary);
+        f.write(reinterpret_cast<const char*>(b.cell_fixed.data()), (std::streamsize)(b.cell_fixed.size() * 4));
+        for (int q = 0; q < d; q++)
+            f.write(reinterpret_cast<const char*>(b.face_fixed[q].data()), (std::streamsize)(b.face_fixed[q].size() * 4));
+        return 0;
+    }
+
+    stg::FluidSteadyState<d> fluid;
+    fluid.init(n, &opts);
+    fluid.init_boundary(b);
+    fluid.update_b(b);
+    stg::FluidEnergy<d> energy(fluid);
+    stg_t* h = fluid.handle();
+
+    const size_t nc = stg::cell_count(d, n);
+    std::vector<double> x(nc, frac), x_old(nc);
+    if (a.get("-init", "uniform") == "noise")
+        stg::check(stg_density_noise(h, (uint64_t)a.geti("-seed", 1), a.getd("-sigma", 4.0), x.data()));
+
+    make_dir(out);
+    std::ofstream log(out + "/log.csv");
+    log << "iteration,objective,volume,change,v_cycles_forward,v_cycles_adjoint,solve_ms,iteration_ms\n";
+    std::printf("fluid_topo %dD N=%d test %d: %s law, rmin %.2f, frac %.3f, %d iterations, tol %.1e, %s\n", d, n, test,
+                law_s.c_str(), rmin, frac, iters, opts.tol, stg_version());
+
+    auto write_frame = [&](int f) {
+        const std::string dir = out + "/" + std::to_string(f);
+        make_dir(dir);
+        fluid.download();
+        write_raw(dir + "/x.bin", {&x});
+        std::vector<const std::vector<double>*> v;
+        for (int q = 0; q < d; q++) v.push_back(&fluid.vel[q]);
+        write_raw(dir + "/velocity.bin", v);
+        std::ofstream info(dir + "/info.txt");
+        info << "dim " << d << "\nn " << n << "\nfield_order cell (i*N+j)" << (d == 3 ? "*N+k" : "")
+             << "; face axis q has N+1 entries along q\n";
+    };
+
+    double J = 0;
+    for (int it = 1; it <= iters; it++) {
+        const double t0 = now_ms();
+        x_old = x;
+        // physical density = H x (FluidTopoOpt3D::Update_Fluid with the filter in front)
+        stg::check(stg_filter(h, rmin, x.data(), nullptr, 0));
+        stg::check(stg_set_density(h, nullptr, &law));
+        const stg_stats& fs = fluid.solve(true);
+        const int vf = fs.inner_iters;
+        const double sms = fs.solve_ms;
+        J = energy.compute_energy();
+        // adjoint solve and chain rule (Update_Grad), then H^T for the filter
+        stg_stats as{};
+        stg::check(stg_adjoint_sensitivity(h, &law, nullptr, &as), true);
+        stg::check(stg_filter(h, rmin, nullptr, nullptr, 1));
+        double lam = 0;
+        stg::check(stg_oc_update(h, rmin, x.data(), nullptr, frac, move, 0.0, 1.0, x.data(), &lam));
+        double vol = 0, change = 0;
+        for (size_t q = 0; q < nc; q++) {
+            vol += x[q];
+            change = std::max(change, std::fabs(x[q] - x_old[q]));
+        }
+        vol /= (double)nc;
+        const double tms = now_ms() - t0;
+        log << it << "," << J << "," << vol << "," << change << "," << vf << "," << as.inner_iters << "," << sms + as.solve_ms
+            << "," << tms << "\n";
+        std::printf("iter %4d  J %.6e  vol %.4f  change %.3e  V-cycles %d+%d  %.1f ms\n", it, J, vol, change, vf,
+                    as.inner_iters, tms);
+        if (frames > 0 && it % frames == 0) write_frame(it);
+    }
+    write_frame(iters);
+    std::printf("final objective %.8e\n", J);
+    return 0;
+}
+
+}  // namespace
+
+int main(int argc, char** argv) {
+    try {
+        Args a = parse(argc, argv);
+        const int driver = a.geti("-driver", 1);
+        if (driver == 0) return run<2>(a);
+        if (driver == 1) return run<3>(a);
+        throw stg::Error(STG_E_INVALID, "-driver must be 0 (2D) or 1 (3D)");
+    } catch (const stg::Error& e) {
+        std::fprintf(stderr, "fluid_topo: %s\n", e.what());
+        return 2;
+    } catch (const std::exception& e) {
+        std::fprintf(stderr, "fluid_topo: %s\n", e.what());
+        return 2;
+    }
+}
