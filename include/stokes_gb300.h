@@ -14,7 +14,8 @@
  * 2D arrays follow the same rule with (i*N + j).
  *
  * "Blocked" device vectors use the reference solver layout
- * [cells | x-faces | y-faces | z-faces] of common_cpx/grid3D.cu:24-146, so the
+ * [cells | x-faces | y-faces | z-faces] of common_cpx/grid3D.cu:24-146 (3D) and
+ * [cells | x-faces | y-faces] of common_cpx/form01mapping.cu:10-57 (2D), so the
  * device-pointer entry points can sit behind the reference LinearMapping interface
  * (common_cpx/LinearMapping.h:4-14) unchanged.
  */
@@ -66,8 +67,10 @@ typedef struct stg_stats {
 int stg_set_stream(stg_t* h, void* cuda_stream);
 
 /* Kernel accounting: total kernels this library has launched in the process, and
- * per-kernel-class CUDA-event timing on the handle's stream (off by default). */
-#define STG_PROF_NCLASS 10
+ * per-kernel-class CUDA-event timing on the handle's stream (off by default). Classes:
+ * 0 resid32, 1 sweep32 (finest level), 2 restrict32, 3 prolong32, 4 apply32, 5 resid64,
+ * 6 krylov, 7 coarse, 8 setup, 9 other, 10 sweep32_coarse (coarser levels). */
+#define STG_PROF_NCLASS 11
 int64_t stg_kernel_launches(void);
 int stg_profile(stg_t* h, int enable); /* enabling also clears the counters */
 int stg_profile_read(stg_t* h, int cls, int64_t* launches, double* ms, double* bytes);
@@ -87,9 +90,10 @@ const char* stg_version(void);
  * (stoke/FluidSteadyState3D.h:11-38, stoke/FluidSteadyState.h).
  * -------------------------------------------------------------------------- */
 
-/* FluidSteadyState3D::init(N) (stoke/FluidSteadyState3D.cpp:12-90): builds the level
- * hierarchy with levels = log2(lowbit N) - 1. dim must be 3 (dim 2 is rejected with
- * STG_E_UNSUPPORTED in this build). N must be a multiple of 4 and >= 4. */
+/* FluidSteadyState3D::init(N) (stoke/FluidSteadyState3D.cpp:12-90), dim 3: levels =
+ * log2(lowbit N) - 1, N a multiple of 4 in [4, 1024]. FluidSteadyState::init(N)
+ * (stoke/FluidSteadyState.cpp:9-85), dim 2: levels = log2(lowbit N) - 2, N a multiple of
+ * 8 up to 16384 whose coarsest level has at most 8192 unknowns. */
 int stg_create(int dim, int n, const stg_opts* opts, stg_t** out);
 int stg_destroy(stg_t* h);
 
@@ -101,9 +105,12 @@ int64_t stg_level_dof(const stg_t* h, int level);
 
 /* FluidSteadyState3D::init_boundary(cell_vol, cell_fixed, face_vol, face_fixed, closed)
  * (stoke/FluidSteadyState3D.cpp:92-114) together with FluidEnergy3D::init_boundary
- * (fluid_topo/FluidEnergy3D.cpp:33-54). face_* point to dim arrays. Returns
+ * (fluid_topo/FluidEnergy3D.cpp:33-54); 2D: FluidSteadyState::init_boundary
+ * (stoke/FluidSteadyState.cpp:87-108). face_* point to dim arrays. In 3D, returns
  * STG_E_UNSUPPORTED when the free faces do not share one vol value or a cell is
- * fixed (this build implements the uniform-coefficient smoother only). */
+ * fixed (the 3D smoother is the uniform-coefficient one); when in addition every face
+ * on the domain boundary is fixed, as in every reference test, the 3D kernels use the
+ * 7-point Laplacian form of the operator (same matrix). 2D takes any vol and fixed cells. */
 int stg_set_boundary(stg_t* h, const double* cell_vol, const int32_t* cell_fixed, const double* const* face_vol,
                      const int32_t* const* face_fixed, int closed);
 

@@ -41,7 +41,7 @@ EXPORTS = [
     "stg_level_descr_device", "stg_density_noise", "stg_set_stream", "stg_kernel_launches", "stg_profile",
     "stg_profile_read", "stg_profile_name", "stg_oc_update_noalloc",
 ]
-STG_PROF_NCLASS = 10
+STG_PROF_NCLASS = 11
 
 
 class Opts(ctypes.Structure):

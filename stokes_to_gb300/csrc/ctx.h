@@ -17,6 +17,7 @@ struct Level {
     float4* P32 = nullptr;
     float4 *r = nullptr, *xa = nullptr, *xb = nullptr, *rr = nullptr;
     int cur = 0;  // which of xa/xb holds the current correction
+    bool lap = false;  // Laplacian-form operator valid on this level (stencil.cuh)
     __nv_bfloat16* xbf = nullptr;
     d4 *t0 = nullptr, *t1 = nullptr;  // FP64 adapter buffers (allocated on first use)
     float4* x() { return cur ? xb : xa; }
@@ -54,6 +55,10 @@ struct stg_ctx {
     std::vector<stg::Level> lv;  // lv[0] coarsest ... lv[L-1] finest (reference order)
     DenseCoarse dense;
     bool closed = true, have_boundary = false, have_penalty = false, have_rhs = false, updated = false, have_solution = false;
+    // lap_ok: the boundary admits the Laplacian form; general: force the masked general
+    // stencil (set while an adapter works on a vector that is nonzero on fixed unknowns)
+    bool lap_ok = false, general = false;
+    int* dflag = nullptr;
     // fine-level FP64
     stg::d4 *b64 = nullptr, *x64 = nullptr, *r64 = nullptr, *t64 = nullptr, *lam64 = nullptr;
     // Krylov (FP32)
@@ -67,7 +72,7 @@ struct stg_ctx {
     size_t ncell = 0, nface = 0;
     // design loop
     double *d_design = nullptr, *d_phys = nullptr, *d_sens = nullptr, *d_sens_design = nullptr, *d_vw = nullptr,
-           *d_tmp = nullptr, *d_gauss = nullptr, *d_parts = nullptr;
+           *d_tmp = nullptr, *d_gauss = nullptr, *d_parts = nullptr, *d_wsum = nullptr;
     double vw_rmin = -1.0;
     const double* phys_used = nullptr;
     // fine vector length in float4 / d4 units and the per-dimension hooks of solve_core
@@ -76,6 +81,7 @@ struct stg_ctx {
     int (*resid64)(stg_t*, const stg::d4* b, const stg::d4* x, stg::d4* r, double* nrm2_host) = nullptr;
     int (*precond)(stg_t*, const float4* rhs, float4* out) = nullptr;
     int (*apply32)(stg_t*, const float4* x, float4* y) = nullptr;
+    int (*finish)(stg_t*, const stg::d4* b, stg::d4* x) = nullptr;  // optional, after the refinement loop
     struct Ctx2* c2 = nullptr;  // 2D state (dim == 2)
 };
 

@@ -28,7 +28,10 @@ __device__ __forceinline__ T block_sum(T v) {
 }
 
 // ------------------------------------------------------------------ operators
-template <int MODE>
+// LAP: Laplacian form (stencil.cuh) for vectors zero on fixed unknowns; rows of fixed
+// unknowns come out 0 (MODE 1: b - A x is 0 there as well, the fixed part of the
+// solution being exactly b_f).
+template <int MODE, bool LAP>
 __global__ void __launch_bounds__(TPB) k_op64(Geom g, double vol, const d4* __restrict__ x, const uint8_t* __restrict__ m,
                                               const d4* __restrict__ P, const d4* __restrict__ b, d4* __restrict__ out,
                                               double* __restrict__ part) {
@@ -39,7 +42,9 @@ __global__ void __launch_bounds__(TPB) k_op64(Geom g, double vol, const d4* __re
         g.box_ijk(t, i, j, k);
         int s = g.slot(i, j, k);
         double o[4];
-        if (MODE == 2)
+        if (LAP)
+            lap_rows<double>(x, P, s, g.di(), g.dj(), vol, o);
+        else if (MODE == 2)
             apply_rows<double, true>(x, m, P, s, g.di(), g.dj(), vol, o);
         else
             apply_rows<double, false>(x, m, P, s, g.di(), g.dj(), vol, o);
@@ -50,6 +55,9 @@ __global__ void __launch_bounds__(TPB) k_op64(Geom g, double vol, const d4* __re
             o[1] = bu - o[1];
             o[2] = bv - o[2];
             o[3] = bw - o[3];
+        }
+        if (LAP) mask4<double>(__ldg(m + s), o);
+        if (MODE == 1) {
             acc = o[0] * o[0] + o[1] * o[1] + o[2] * o[2] + o[3] * o[3];
         } else if (MODE == 2) {
             double xp, xu, xv, xw;
@@ -64,7 +72,7 @@ __global__ void __launch_bounds__(TPB) k_op64(Geom g, double vol, const d4* __re
     }
 }
 
-template <bool HAS_X, bool RESID>
+template <bool HAS_X, bool RESID, bool LAP>
 __global__ void __launch_bounds__(TPB) k_op32(Geom g, float vol, const float4* __restrict__ r, const float4* __restrict__ x,
                                               const uint8_t* __restrict__ m, const float4* __restrict__ P,
                                               float4* __restrict__ out) {
@@ -74,13 +82,21 @@ __global__ void __launch_bounds__(TPB) k_op32(Geom g, float vol, const float4* _
     g.box_ijk(t, i, j, k);
     int s = g.slot(i, j, k);
     float o[4] = {0.f, 0.f, 0.f, 0.f};
-    if (HAS_X) apply_rows<float, false>(x, m, P, s, g.di(), g.dj(), vol, o);
+    if (HAS_X) {
+        if (LAP)
+            lap_rows<float>(x, P, s, g.di(), g.dj(), vol, o);
+        else
+            apply_rows<float, false>(x, m, P, s, g.di(), g.dj(), vol, o);
+    }
     if (RESID) {
         float4 rv = __ldg(r + s);
-        out[s] = make_float4(rv.x - o[0], rv.y - o[1], rv.z - o[2], rv.w - o[3]);
-    } else {
-        out[s] = make_float4(o[0], o[1], o[2], o[3]);
+        o[0] = rv.x - o[0];
+        o[1] = rv.y - o[1];
+        o[2] = rv.z - o[2];
+        o[3] = rv.w - o[3];
     }
+    if (LAP) mask4<float>(__ldg(m + s), o);
+    out[s] = make_float4(o[0], o[1], o[2], o[3]);
 }
 
 // ------------------------------------------------------------------ transfers
@@ -88,7 +104,7 @@ __global__ void __launch_bounds__(TPB) k_op32(Geom g, float vol, const float4* _
 // the coarse unknown of every kind at slot (I,J,K) sums the eight fine unknowns of the same
 // kind at slots (2I+a, 2J+b, 2K+c), then fixed coarse unknowns are zeroed. Fused with the
 // fine residual r - A x.
-template <bool HAS_X>
+template <bool HAS_X, bool LAP>
 __global__ void __launch_bounds__(TPB) k_restrict_res32(Geom gc, Geom gf, float volf, const float4* __restrict__ rf,
                                                         const float4* __restrict__ xf, const uint8_t* __restrict__ mf,
                                                         const float4* __restrict__ Pf, const uint8_t* __restrict__ mc,
@@ -107,11 +123,21 @@ __global__ void __launch_bounds__(TPB) k_restrict_res32(Geom gc, Geom gf, float 
         float4 r = __ldg(rf + s);
         if (HAS_X) {
             float o[4];
-            apply_rows<float, false>(xf, mf, Pf, s, gf.di(), gf.dj(), volf, o);
-            r.x -= o[0];
-            r.y -= o[1];
-            r.z -= o[2];
-            r.w -= o[3];
+            if (LAP) {
+                lap_rows<float>(xf, Pf, s, gf.di(), gf.dj(), volf, o);
+                o[0] = r.x - o[0];
+                o[1] = r.y - o[1];
+                o[2] = r.z - o[2];
+                o[3] = r.w - o[3];
+                mask4<float>(__ldg(mf + s), o);
+                r = make_float4(o[0], o[1], o[2], o[3]);
+            } else {
+                apply_rows<float, false>(xf, mf, Pf, s, gf.di(), gf.dj(), volf, o);
+                r.x -= o[0];
+                r.y -= o[1];
+                r.z -= o[2];
+                r.w -= o[3];
+            }
         }
         a0 += r.x;
         a1 += r.y;
@@ -372,11 +398,52 @@ __global__ void k_half_square64(long long n, const double* __restrict__ x, doubl
         out[t] = (0.5 * x[t]) * x[t];
 }
 
+__global__ void k_fixed_nonzero(Geom g, const d4* __restrict__ x, const uint8_t* __restrict__ m, int* __restrict__ flag) {
+    long long t = (long long)blockIdx.x * TPB + threadIdx.x;
+    if (t >= g.box()) return;
+    int i, j, k;
+    g.box_ijk(t, i, j, k);
+    int s = g.slot(i, j, k);
+    uint8_t mm = __ldg(m + s);
+    if (!mm) return;
+    double p, u, v, w;
+    load4(x, s, p, u, v, w);
+    if (((mm & MP) && p != 0.0) || ((mm & MU) && u != 0.0) || ((mm & MV) && v != 0.0) || ((mm & MW) && w != 0.0))
+        atomicOr(flag, 1);
+}
+
+__global__ void k_patch_fixed(Geom g, const d4* __restrict__ b, const uint8_t* __restrict__ m, d4* __restrict__ x) {
+    long long t = (long long)blockIdx.x * TPB + threadIdx.x;
+    if (t >= g.box()) return;
+    int i, j, k;
+    g.box_ijk(t, i, j, k);
+    int s = g.slot(i, j, k);
+    uint8_t mm = __ldg(m + s);
+    if (!mm) return;
+    double bp, bu, bv, bw, p, u, v, w;
+    load4(b, s, bp, bu, bv, bw);
+    load4(x, s, p, u, v, w);
+    store4(x, s, (mm & MP) ? bp : p, (mm & MU) ? bu : u, (mm & MV) ? bv : v, (mm & MW) ? bw : w);
+}
+
 }  // namespace
 
 // ------------------------------------------------------------------ launchers
 int vol_slots(cudaStream_t st, const Geom& g, const uint8_t* m, double cell_vol, double vol, d4* out) {
     k_vol_slots<<<grid_for(g.box(), TPB), TPB, 0, st>>>(g, m, cell_vol, vol, out);
+    STG_LAUNCH_CK();
+    return STG_OK;
+}
+
+int fixed_nonzero(cudaStream_t st, const Geom& g, const d4* x, const uint8_t* m, int* flag) {
+    STG_CK(cudaMemsetAsync(flag, 0, sizeof(int), st));
+    k_fixed_nonzero<<<grid_for(g.box(), TPB), TPB, 0, st>>>(g, x, m, flag);
+    STG_LAUNCH_CK();
+    return STG_OK;
+}
+
+int patch_fixed(cudaStream_t st, const Geom& g, const d4* b, const uint8_t* m, d4* x) {
+    k_patch_fixed<<<grid_for(g.box(), TPB), TPB, 0, st>>>(g, b, m, x);
     STG_LAUNCH_CK();
     return STG_OK;
 }
@@ -390,43 +457,54 @@ int half_square64(cudaStream_t st, long long n4, const d4* x, d4* out) {
 }
 
 int op64(cudaStream_t st, const Geom& g, double vol, const d4* x, const uint8_t* m, const d4* P, const d4* b, d4* out,
-         int mode, double* part, int* nblocks_out) {
+         int mode, double* part, int* nblocks_out, bool lap) {
     unsigned nb = grid_for(g.box(), TPB);
     if (nblocks_out) *nblocks_out = (int)nb;
-    if (mode == 0)
-        k_op64<0><<<nb, TPB, 0, st>>>(g, vol, x, m, P, b, out, part);
+    if (mode == 0 && lap)
+        k_op64<0, true><<<nb, TPB, 0, st>>>(g, vol, x, m, P, b, out, part);
+    else if (mode == 0)
+        k_op64<0, false><<<nb, TPB, 0, st>>>(g, vol, x, m, P, b, out, part);
+    else if (mode == 1 && lap)
+        k_op64<1, true><<<nb, TPB, 0, st>>>(g, vol, x, m, P, b, out, part);
     else if (mode == 1)
-        k_op64<1><<<nb, TPB, 0, st>>>(g, vol, x, m, P, b, out, part);
+        k_op64<1, false><<<nb, TPB, 0, st>>>(g, vol, x, m, P, b, out, part);
     else
-        k_op64<2><<<nb, TPB, 0, st>>>(g, vol, x, m, P, b, out, part);
+        k_op64<2, false><<<nb, TPB, 0, st>>>(g, vol, x, m, P, b, out, part);
     STG_LAUNCH_CK();
     return STG_OK;
 }
 
 int resid32(cudaStream_t st, const Geom& g, float vol, const float4* r, const float4* x, const uint8_t* m, const float4* P,
-            float4* rr) {
+            float4* rr, bool lap) {
     unsigned nb = grid_for(g.box(), TPB);
-    if (x)
-        k_op32<true, true><<<nb, TPB, 0, st>>>(g, vol, r, x, m, P, rr);
+    if (x && lap)
+        k_op32<true, true, true><<<nb, TPB, 0, st>>>(g, vol, r, x, m, P, rr);
+    else if (x)
+        k_op32<true, true, false><<<nb, TPB, 0, st>>>(g, vol, r, x, m, P, rr);
     else
-        k_op32<false, true><<<nb, TPB, 0, st>>>(g, vol, r, x, m, P, rr);
+        k_op32<false, true, false><<<nb, TPB, 0, st>>>(g, vol, r, x, m, P, rr);
     STG_LAUNCH_CK();
     return STG_OK;
 }
 
-int apply32(cudaStream_t st, const Geom& g, float vol, const float4* x, const uint8_t* m, const float4* P, float4* y) {
-    k_op32<true, false><<<grid_for(g.box(), TPB), TPB, 0, st>>>(g, vol, nullptr, x, m, P, y);
+int apply32(cudaStream_t st, const Geom& g, float vol, const float4* x, const uint8_t* m, const float4* P, float4* y, bool lap) {
+    if (lap)
+        k_op32<true, false, true><<<grid_for(g.box(), TPB), TPB, 0, st>>>(g, vol, nullptr, x, m, P, y);
+    else
+        k_op32<true, false, false><<<grid_for(g.box(), TPB), TPB, 0, st>>>(g, vol, nullptr, x, m, P, y);
     STG_LAUNCH_CK();
     return STG_OK;
 }
 
 int restrict_resid32(cudaStream_t st, const Geom& gc, const Geom& gf, float volf, const float4* rf, const float4* xf,
-                     const uint8_t* mf, const float4* Pf, const uint8_t* mc, float4* rc) {
+                     const uint8_t* mf, const float4* Pf, const uint8_t* mc, float4* rc, bool lap) {
     unsigned nb = grid_for(gc.box(), TPB);
-    if (xf)
-        k_restrict_res32<true><<<nb, TPB, 0, st>>>(gc, gf, volf, rf, xf, mf, Pf, mc, rc);
+    if (xf && lap)
+        k_restrict_res32<true, true><<<nb, TPB, 0, st>>>(gc, gf, volf, rf, xf, mf, Pf, mc, rc);
+    else if (xf)
+        k_restrict_res32<true, false><<<nb, TPB, 0, st>>>(gc, gf, volf, rf, xf, mf, Pf, mc, rc);
     else
-        k_restrict_res32<false><<<nb, TPB, 0, st>>>(gc, gf, volf, rf, xf, mf, Pf, mc, rc);
+        k_restrict_res32<false, false><<<nb, TPB, 0, st>>>(gc, gf, volf, rf, xf, mf, Pf, mc, rc);
     STG_LAUNCH_CK();
     return STG_OK;
 }

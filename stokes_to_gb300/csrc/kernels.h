@@ -10,20 +10,29 @@ namespace stg {
 // ---------------------------------------------------------------- operators (kernels.cu)
 // mode: 0 out = A x, 1 out = b - A x, 2 out = E x. If part != nullptr, each block writes
 // its partial sum of out.out (mode 1) or x.out (mode 2) to part[blockIdx.x] (FP64).
+// lap (modes 0 and 1): Laplacian form of A (stencil.cuh) for x zero on fixed unknowns,
+// rows of fixed unknowns 0. Every operator below takes the same switch; the solver sets
+// it when the level satisfies the Laplacian-form conditions and its vectors are zero on
+// fixed unknowns.
 int op64(cudaStream_t st, const Geom& g, double vol, const d4* x, const uint8_t* m, const d4* P, const d4* b, d4* out,
-         int mode, double* part, int* nblocks_out);
+         int mode, double* part, int* nblocks_out, bool lap = false);
 // rr = r - A x in FP32 (x == nullptr means x = 0, so rr = r)
 int resid32(cudaStream_t st, const Geom& g, float vol, const float4* r, const float4* x, const uint8_t* m, const float4* P,
-            float4* rr);
+            float4* rr, bool lap = false);
 // y = A x in FP32
-int apply32(cudaStream_t st, const Geom& g, float vol, const float4* x, const uint8_t* m, const float4* P, float4* y);
+int apply32(cudaStream_t st, const Geom& g, float vol, const float4* x, const uint8_t* m, const float4* P, float4* y,
+            bool lap = false);
 // One colour of the box-Vanka block-Jacobi step on the residual equation, fused with the
 // residual: xout = xin + SHATTER(B^-1 GATHER(r - A xin)) (sweep.cu). xin == nullptr: xin = 0.
 int sweep32(cudaStream_t st, const Geom& g, float vol, const float4* r, const float4* xin, float4* xout, const uint8_t* m,
-            const float4* P, int flag);
+            const float4* P, int flag, bool lap = false);
 // rc = R (rf - A xf) with R the 8-child sum masked by the coarse mask (xf == nullptr: rc = R rf).
 int restrict_resid32(cudaStream_t st, const Geom& gc, const Geom& gf, float volf, const float4* rf, const float4* xf,
-                     const uint8_t* mf, const float4* Pf, const uint8_t* mc, float4* rc);
+                     const uint8_t* mf, const float4* Pf, const uint8_t* mc, float4* rc, bool lap = false);
+// 1 in *flag (device) when x is nonzero on some fixed or absent unknown of the box, else 0
+int fixed_nonzero(cudaStream_t st, const Geom& g, const d4* x, const uint8_t* m, int* flag);
+// x_f = b_f on every fixed unknown of the box (the fixed rows of A are the identity)
+int patch_fixed(cudaStream_t st, const Geom& g, const d4* b, const uint8_t* m, d4* x);
 // xf += fix_f (injection of xc)
 int prolong_add32(cudaStream_t st, const Geom& gf, const Geom& gc, const float4* xc, const uint8_t* mf, float4* xf);
 // same with BF16-stored coarse correction
@@ -107,8 +116,9 @@ int face_penalty_from_density(cudaStream_t st, const Geom& g, const double* rho,
                               d4* P64, float4* P32);
 int sensitivity(cudaStream_t st, const Geom& g, const double* rho, const stg_alpha& law, const d4* x, const d4* lam,
                 double* grad);
-// dim 2: cells (i,j) -> i*n + j; dim 3: (i*n + j)*n + k
-int density_filter(cudaStream_t st, int dim, int n, double rmin, const double* in, double* out, int transpose);
+// dim 2: cells (i,j) -> i*n + j; dim 3: (i*n + j)*n + k. W: scratch of n^dim doubles
+// (receives the row sums W_i).
+int density_filter(cudaStream_t st, int dim, int n, double rmin, const double* in, double* out, int transpose, double* W);
 int oc_volume(cudaStream_t st, int ncell, const double* x, const double* dc, const double* vw, double lam, double move,
               double lo, double hi, double* xnew, double* parts, int* nparts);
 int density_noise(cudaStream_t st, int dim, int n, uint64_t seed, const double* w, int R, double* out, double* tmp);

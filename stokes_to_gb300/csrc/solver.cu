@@ -49,6 +49,10 @@ namespace stg {
 
 Level& fine(stg_t* h) { return h->lv[h->L - 1]; }
 
+// the Laplacian-form kernels apply: the level admits them and the vectors in flight are
+// zero on fixed unknowns (always inside solve_core; adapters check their input)
+bool fast(const stg_t* h, const Level& L) { return L.lap && !h->general; }
+
 int prof_flush(stg_t* h) {
     Prof& P = h->prof;
     if (P.pend.empty()) return STG_OK;
@@ -150,6 +154,8 @@ int update(stg_t* h) {
         c.vol = 4.0 * f.vol;
         c.cell_vol = 8.0 * f.cell_vol;
     }
+    // coarse boundary faces have fixed children, so the Laplacian form carries down
+    for (auto& L : h->lv) L.lap = h->lap_ok;
     PROF(h, 8, 0.0, dense_setup(h->st, h->dense, h->lv[0].g, h->lv[0].vol, h->lv[0].m, h->lv[0].P64, h->closed ? 1 : 0));
     h->updated = true;
     return STG_OK;
@@ -161,12 +167,14 @@ int update(stg_t* h) {
 // (common_cpx/DescentSmoother.cu:31-47), written in correction form x <- x + P_c(r - A x).
 int sweep(stg_t* h, Level& L, const float4* r, int flag, bool first) {
     float vol = (float)L.vol;
+    // profile class 1: sweeps of the finest level; 10: of the coarser levels
+    const int cls = &L == &fine(h) ? 1 : 10;
     if (first) {
         // x = 0: the residual is r itself
-        PROF(h, 1, 49.0 * L.g.box(), sweep32(h->st, L.g, vol, r, nullptr, L.x(), L.m, L.P32, flag));
+        PROF(h, cls, 49.0 * L.g.box(), sweep32(h->st, L.g, vol, r, nullptr, L.x(), L.m, L.P32, flag, fast(h, L)));
         return STG_OK;
     }
-    PROF(h, 1, 65.0 * L.g.box(), sweep32(h->st, L.g, vol, r, L.x(), L.other(), L.m, L.P32, flag));
+    PROF(h, cls, 65.0 * L.g.box(), sweep32(h->st, L.g, vol, r, L.x(), L.other(), L.m, L.P32, flag, fast(h, L)));
     L.cur ^= 1;
     return STG_OK;
 }
@@ -189,7 +197,7 @@ int vcycle(stg_t* h, const float4* rhs) {
         F.cur = 0;
         STG_TRY(smooth(h, F, r, false, true));
         Level& C = h->lv[i - 1];
-        PROF(h, 2, 49.0 * F.g.box() + 17.0 * C.g.box(), restrict_resid32(h->st, C.g, F.g, (float)F.vol, r, F.x(), F.m, F.P32, C.m, C.r));
+        PROF(h, 2, 49.0 * F.g.box() + 17.0 * C.g.box(), restrict_resid32(h->st, C.g, F.g, (float)F.vol, r, F.x(), F.m, F.P32, C.m, C.r, fast(h, F)));
     }
     Level& C0 = h->lv[0];
     C0.cur = 0;
@@ -213,7 +221,7 @@ int vcycle(stg_t* h, const float4* rhs) {
 int residual64(stg_t* h, const d4* b, const d4* x, d4* r, double* nrm2_host) {
     Level& F = fine(h);
     int nb = 0;
-    PROF(h, 5, 129.0 * F.g.box(), op64(h->st, F.g, F.vol, x, F.m, F.P64, b, r, 1, h->d_parts, &nb));
+    PROF(h, 5, 129.0 * F.g.box(), op64(h->st, F.g, F.vol, x, F.m, F.P64, b, r, 1, h->d_parts, &nb, fast(h, F)));
     STG_TRY(reduce_parts(h->st, h->d_parts, nb, h->dnrm));
     STG_CK(cudaMemcpyAsync(nrm2_host, h->dnrm, sizeof(double), cudaMemcpyDeviceToHost, h->st));
     STG_CK(cudaStreamSynchronize(h->st));
@@ -236,7 +244,15 @@ int precond3(stg_t* h, const float4* rhs, float4* out) {
 
 int apply3(stg_t* h, const float4* x, float4* y) {
     Level& F = fine(h);
-    PROF(h, 4, 49.0 * F.g.box(), apply32(h->st, F.g, (float)F.vol, x, F.m, F.P32, y));
+    PROF(h, 4, 49.0 * F.g.box(), apply32(h->st, F.g, (float)F.vol, x, F.m, F.P32, y, fast(h, F)));
+    return STG_OK;
+}
+
+// The Laplacian-form residual leaves the fixed rows at 0 and x at 0 there; the fixed
+// rows of A are the identity, so the fixed part of the solution is b_f exactly.
+int finish3(stg_t* h, const d4* b, d4* x) {
+    Level& F = fine(h);
+    if (fast(h, F)) STG_TRY(patch_fixed(h->st, F.g, b, F.m, x));
     return STG_OK;
 }
 
@@ -346,6 +362,7 @@ int solve_core(stg_t* h, const d4* b, d4* x, stg_stats* stats) {
         STG_CK(cudaMemcpyAsync(h->dy, y.data(), sizeof(double) * k, cudaMemcpyHostToDevice, h->st));
         PROF(h, 6, (16.0 * k + 64.0) * n4, axpy_multi_32to64(h->st, n4, h->Z.data(), h->dy, k, rn, x));
     }
+    if (h->finish) STG_TRY(h->finish(h, b, x));
     STG_CK(cudaEventRecord(h->e1, h->st));
     STG_CK(cudaEventSynchronize(h->e1));
     float ms = 0;
@@ -358,6 +375,24 @@ int solve_core(stg_t* h, const d4* b, d4* x, stg_stats* stats) {
     if (stats) *stats = S;
     if (status == STG_E_NOT_CONVERGED) set_error("tolerance %.1e not reached (%.3e after %d steps)", h->opts.tol, rel, S.outer_iters);
     return status;
+}
+
+// Adapters take any vector; the Laplacian form needs zero fixed entries, so a vector
+// that has nonzero fixed entries runs the general stencil for this call.
+struct PathGuard {
+    stg_t* h;
+    ~PathGuard() { h->general = false; }
+};
+
+int choose_path(stg_t* h, const Level& L, const d4* x) {
+    h->general = false;
+    if (!L.lap) return STG_OK;
+    int nz = 0;
+    STG_TRY(fixed_nonzero(h->st, L.g, x, L.m, h->dflag));
+    STG_CK(cudaMemcpyAsync(&nz, h->dflag, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+    STG_CK(cudaStreamSynchronize(h->st));
+    h->general = nz != 0;
+    return STG_OK;
 }
 
 int ensure_adapter(Level& L) {
@@ -427,8 +462,8 @@ int stg_profile_read(stg_t* h, int cls, int64_t* launches, double* ms, double* b
 }
 
 const char* stg_profile_name(int cls) {
-    static const char* names[STG_PROF_NCLASS] = {"resid32",  "sweep32", "restrict32", "prolong32", "apply32",
-                                                 "resid64",  "krylov",  "coarse",     "setup",     "other"};
+    static const char* names[STG_PROF_NCLASS] = {"resid32", "sweep32", "restrict32", "prolong32", "apply32", "resid64",
+                                                 "krylov",  "coarse",  "setup",      "other",     "sweep32_coarse"};
     return (cls >= 0 && cls < STG_PROF_NCLASS) ? names[cls] : "";
 }
 
@@ -505,6 +540,7 @@ int stg_create(int dim, int n, const stg_opts* opts, stg_t** out) {
         h->resid64 = residual64;
         h->precond = precond3;
         h->apply32 = apply3;
+        h->finish = finish3;
         h->ncell = (size_t)n * n * n;
         h->nface = (size_t)n * n * (n + 1);
         nparts = grid_for(F.g.box(), 256);
@@ -522,11 +558,12 @@ int stg_create(int dim, int n, const stg_opts* opts, stg_t** out) {
     for (auto& p : h->Z)
         if ((rc = dalloc(&p, ns))) return fail(rc);
     if ((rc = dalloc(&h->dscr, 1216 * 16)) || (rc = dalloc(&h->dh, 2 * (h->m + 2))) || (rc = dalloc(&h->dnrm, 8)) ||
-        (rc = dalloc(&h->dy, h->m + 1)) || (rc = dalloc(&h->d_parts, (size_t)nparts + 1216)))
+        (rc = dalloc(&h->dy, h->m + 1)) || (rc = dalloc(&h->d_parts, (size_t)nparts + 1216)) || (rc = dalloc(&h->dflag, 1)))
         return fail(rc);
     if ((rc = dalloc(&h->stage, h->ncell + 3 * h->nface)) || (rc = dalloc(&h->istage, h->ncell + 3 * h->nface))) return fail(rc);
     if ((rc = dalloc(&h->d_design, h->ncell)) || (rc = dalloc(&h->d_phys, h->ncell)) || (rc = dalloc(&h->d_sens, h->ncell)) ||
         (rc = dalloc(&h->d_sens_design, h->ncell)) || (rc = dalloc(&h->d_vw, h->ncell)) || (rc = dalloc(&h->d_tmp, h->ncell)) ||
+        (rc = dalloc(&h->d_wsum, h->ncell)) ||
         (rc = dalloc(&h->d_gauss, 512)))
         return fail(rc);
     if (cudaStreamSynchronize(h->st) != cudaSuccess) return fail(cuda_fail(cudaGetLastError(), "create", __FILE__, __LINE__));
@@ -556,9 +593,10 @@ int stg_destroy(stg_t* h) {
     for (auto p : h->V) cudaFree(p);
     for (auto p : h->Z) cudaFree(p);
     for (double* p : {h->dscr, h->dh, h->dnrm, h->dy, h->stage, h->d_design, h->d_phys, h->d_sens, h->d_sens_design, h->d_vw,
-                      h->d_tmp, h->d_gauss, h->d_parts})
+                      h->d_tmp, h->d_gauss, h->d_parts, h->d_wsum})
         cudaFree(p);
     cudaFree(h->istage);
+    cudaFree(h->dflag);
     if (h->e0) cudaEventDestroy(h->e0);
     if (h->e1) cudaEventDestroy(h->e1);
     for (auto e : h->prof.pool) cudaEventDestroy(e);
@@ -631,6 +669,21 @@ int stg_set_boundary(stg_t* h, const double* cell_vol, const int32_t* cell_fixed
                 set_error("fixed cells are not supported by this build");
                 return STG_E_UNSUPPORTED;
             }
+    // Laplacian form: every face on the domain boundary fixed (Field order, N+1 along d)
+    bool bnd_fixed = true;
+    for (int d = 0; d < 3 && bnd_fixed; d++)
+        for (int a = 0; a <= n && bnd_fixed; a++)
+            for (int b = 0; b < n && bnd_fixed; b++)
+                for (int c = 0; c < n && bnd_fixed; c++) {
+                    if (a != 0 && a != n) continue;
+                    int ijk[3];
+                    ijk[d] = a;
+                    ijk[(d + 1) % 3] = b;
+                    ijk[(d + 2) % 3] = c;
+                    const size_t q = ((size_t)ijk[0] * (n + (d == 1)) + ijk[1]) * (n + (d == 2)) + ijk[2];
+                    if (!face_fixed[d][q]) bnd_fixed = false;
+                }
+    h->lap_ok = bnd_fixed;
     double cv = cell_vol ? cell_vol[0] : 1.0;
     Level& F = fine(h);
     F.vol = std::isnan(v) ? 0.0 : v;
@@ -646,7 +699,6 @@ int stg_set_boundary(stg_t* h, const double* cell_vol, const int32_t* cell_fixed
     h->closed = closed != 0;
     h->have_boundary = true;
     h->updated = false;
-    (void)n;
     STG_CK(cudaStreamSynchronize(h->st));
     return STG_OK;
 }
@@ -810,7 +862,7 @@ int stg_filter(stg_t* h, double rmin, const double* in, double* out, int transpo
         STG_CK(cudaMemcpyAsync(h->d_tmp, in, sizeof(double) * h->ncell, cudaMemcpyHostToDevice, h->st));
         src = h->d_tmp;
     }
-    STG_TRY(density_filter(h->st, h->dim, h->n, rmin, src, dst, transpose));
+    STG_TRY(density_filter(h->st, h->dim, h->n, rmin, src, dst, transpose, h->d_wsum));
     if (out) STG_CK(cudaMemcpyAsync(out, dst, sizeof(double) * h->ncell, cudaMemcpyDeviceToHost, h->st));
     STG_CK(cudaStreamSynchronize(h->st));
     return STG_OK;
@@ -824,7 +876,7 @@ int stg_oc_update(stg_t* h, double rmin, const double* x, const double* dc, doub
         // vw_j = sum_i w_ij / W_i: the filtered volume is sum_j vw_j x_j
         std::vector<double> ones(h->ncell, 1.0);
         STG_CK(cudaMemcpyAsync(h->d_tmp, ones.data(), sizeof(double) * h->ncell, cudaMemcpyHostToDevice, h->st));
-        STG_TRY(density_filter(h->st, h->dim, h->n, rmin, h->d_tmp, h->d_vw, 1));
+        STG_TRY(density_filter(h->st, h->dim, h->n, rmin, h->d_tmp, h->d_vw, 1, h->d_wsum));
         STG_CK(cudaStreamSynchronize(h->st));
         h->vw_rmin = rmin;
     }
@@ -937,6 +989,8 @@ int stg_vcycle_device(stg_t* h, double* d_out, const double* d_in) {
     Level& F = fine(h);
     STG_TRY(ensure_adapter(F));
     STG_TRY(blocked_to_slots64(h->st, F.g, d_in, F.t0));
+    PathGuard guard{h};
+    STG_TRY(choose_path(h, F, F.t0));
     STG_TRY(f64_to_f32(h->st, F.g.nslot, F.t0, 1.0, h->w));
     STG_TRY(vcycle(h, h->w));
     STG_TRY(f32_to_f64(h->st, F.g.nslot, F.x(), F.t1));
@@ -986,13 +1040,16 @@ int stg_apply_op_device(stg_t* h, int op, int level, double* d_out, const double
         case STG_OP_VANKA_BLACK: {
             if (level == 0) break;
             STG_TRY(blocked_to_slots64(h->st, L.g, d_in, L.t0));
+            PathGuard guard{h};
+            STG_TRY(choose_path(h, L, L.t0));
             STG_TRY(f64_to_f32(h->st, L.g.nslot, L.t0, 1.0, L.r));
             L.cur = 0;
             if (op == STG_OP_SMOOTH_PRE || op == STG_OP_SMOOTH_POST) {
                 STG_CK(cudaMemsetAsync(L.x(), 0, sizeof(float4) * L.g.nslot, h->st));
                 STG_TRY(smooth(h, L, L.r, op == STG_OP_SMOOTH_POST, true));
             } else {
-                STG_TRY(sweep32(h->st, L.g, (float)L.vol, L.r, nullptr, L.x(), L.m, L.P32, op == STG_OP_VANKA_BLACK ? 1 : 0));
+                STG_TRY(sweep32(h->st, L.g, (float)L.vol, L.r, nullptr, L.x(), L.m, L.P32, op == STG_OP_VANKA_BLACK ? 1 : 0,
+                                fast(h, L)));
             }
             STG_TRY(f32_to_f64(h->st, L.g.nslot, L.x(), L.t1));
             STG_TRY(slots_to_blocked64(h->st, L.g, L.t1, d_out, nullptr));

@@ -140,6 +140,56 @@ __device__ __forceinline__ Nb<T> nb_make(T p, T u, T v, T w, uint8_t mm) {
     return r;
 }
 
+// ---------------------------------------------------------------- Laplacian form of A
+// Applies when (1) the free faces share one vol value and no cell is fixed, (2) every
+// face on the domain boundary is fixed, and (3) the vector is zero on every fixed or
+// absent unknown. Then each free face lies between two present cells, fix_f u = u, and
+// -fix_f G fix_c D (V u) + V D1 Cod1 (fix_f u) is exactly vol times the negative
+// 7-point face Laplacian of u: the edge-diagonal terms of the two parts cancel
+// identically (expanding ccx - (dv0 - dvx)/vol of stencil_core leaves
+// 6 u - sum of the six x-face neighbours), so a row reads the slot and its six face
+// neighbours. The rows of fixed and absent unknowns are masked by the caller (their
+// reference value, (P + F) x = x, is 0 under (3)).
+template <class T>
+struct Q4 {
+    T p, u, v, w;
+};
+
+template <class T>
+__device__ __forceinline__ void lap_core(const Q4<T>& c, const Q4<T>& xm, const Q4<T>& xp, const Q4<T>& ym, const Q4<T>& yp,
+                                         const Q4<T>& zm, const Q4<T>& zp, const Q4<T>& pen, T vol, T out[4]) {
+    const T div = (xp.u - c.u) + (yp.v - c.v) + (zp.w - c.w);
+    const T lu = T(6) * c.u - (xm.u + xp.u) - (ym.u + yp.u) - (zm.u + zp.u);
+    const T lv = T(6) * c.v - (xm.v + xp.v) - (ym.v + yp.v) - (zm.v + zp.v);
+    const T lw = T(6) * c.w - (xm.w + xp.w) - (ym.w + yp.w) - (zm.w + zp.w);
+    out[0] = vol * div + pen.p * c.p;
+    out[1] = vol * (lu - (c.p - xm.p)) + pen.u * c.u;
+    out[2] = vol * (lv - (c.p - ym.p)) + pen.v * c.v;
+    out[3] = vol * (lw - (c.p - zm.p)) + pen.w * c.w;
+}
+
+template <class T>
+__device__ __forceinline__ void mask4(uint8_t ms, T o[4]) {
+    if (ms & MP) o[0] = T(0);
+    if (ms & MU) o[1] = T(0);
+    if (ms & MV) o[2] = T(0);
+    if (ms & MW) o[3] = T(0);
+}
+
+template <class T, class V>
+__device__ __forceinline__ Q4<T> q4_load(const V* __restrict__ a, int s) {
+    Q4<T> r;
+    load4(a, s, r.p, r.u, r.v, r.w);
+    return r;
+}
+
+// Unmasked Laplacian-form rows of A x at slot s (global-memory operands).
+template <class T, class V>
+__device__ __forceinline__ void lap_rows(const V* __restrict__ x, const V* __restrict__ P, int s, int di, int dj, T vol, T out[4]) {
+    lap_core<T>(q4_load<T>(x, s), q4_load<T>(x, s - di), q4_load<T>(x, s + di), q4_load<T>(x, s - dj), q4_load<T>(x, s + dj),
+                q4_load<T>(x, s - 1), q4_load<T>(x, s + 1), q4_load<T>(P, s), vol, out);
+}
+
 // Full row values: A x (ENERGY false) or E x (ENERGY true) at slot s.
 template <class T, bool ENERGY, class V>
 __device__ __forceinline__ void apply_rows(const V* __restrict__ x, const uint8_t* __restrict__ m, const V* __restrict__ P,

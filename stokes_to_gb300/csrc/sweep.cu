@@ -85,7 +85,7 @@ __device__ __forceinline__ Elem make_elem(const Geom& g, int e, int nelem, int w
 
 __device__ __forceinline__ bool plane_ok(int n, int p) { return p >= -1 && p <= n + 1; }
 
-template <bool HAS_X>
+template <bool HAS_X, bool LAP>
 __device__ __forceinline__ void residual_plane(Smem& S, const Elem (&R)[2], int n, float vol, int p) {
     const bool pin = p >= 0 && p <= n;
     const int xa = rx(p - 1), xb = rx(p), xc = rx(p + 1);
@@ -97,7 +97,24 @@ __device__ __forceinline__ void residual_plane(Smem& S, const Elem (&R)[2], int 
         float4 out = make_float4(0.f, 0.f, 0.f, 0.f);
         if (pin && R[q].box) {
             float4 rv = S.r[r2(p)][e];
-            if (HAS_X) {
+            if (HAS_X && LAP) {
+                // Laplacian form (stencil.cuh): six face neighbours, own row masked
+                const int xi = e + (e / RK) * (XK - RK) + XK + 1;
+                auto q = [&](int pl, int o) {
+                    float4 v = S.x[pl][o];
+                    return Q4<float>{v.x, v.y, v.z, v.w};
+                };
+                const float4 pv = S.P[rp(p)][e];
+                float o[4];
+                lap_core<float>(q(xb, xi), q(xa, xi), q(xc, xi), q(xb, xi - XK), q(xb, xi + XK), q(xb, xi - 1), q(xb, xi + 1),
+                                Q4<float>{pv.x, pv.y, pv.z, pv.w}, vol, o);
+                o[0] = rv.x - o[0];
+                o[1] = rv.y - o[1];
+                o[2] = rv.z - o[2];
+                o[3] = rv.w - o[3];
+                mask4<float>(S.m[mb][xi], o);
+                out = make_float4(o[0], o[1], o[2], o[3]);
+            } else if (HAS_X) {
                 // rr region index e = rj*RK + rk  ->  x region index (rj+1)*XK + (rk+1)
                 const int xi = e + (e / RK) * (XK - RK) + XK + 1;
                 auto ld = [&](int a, int b, int c) {
@@ -125,7 +142,10 @@ __device__ __forceinline__ void residual_plane(Smem& S, const Elem (&R)[2], int 
     }
 }
 
-// pressure update of every red cell of plane p in the dp region, one thread per red cell
+// pressure update of every red cell of plane p in the dp region, one thread per red cell.
+// LAP: every present cell is free and every free face lies between two present cells, so a
+// free face's diagonal is 6 vol + P; fixed faces (residual 0) drop out through vL / vR = 0.
+template <bool LAP>
 __device__ __forceinline__ void pressure_plane(Smem& S, int n, float vol, int p, int j0, int k0, int flag, int tid) {
     if (tid >= DJ * DRED) return;
     const int dj = tid / DRED, q = tid % DRED;
@@ -139,7 +159,25 @@ __device__ __forceinline__ void pressure_plane(Smem& S, int n, float vol, int p,
     float4 pc = S.P[rp(p)][ri];
     uint8_t m0 = S.m[rm(p)][xi];
     float out;
-    if (m0 & MP) {
+    if (LAP) {
+        const float rL[3] = {rc.y, rc.z, rc.w};
+        const float pL[3] = {pc.y, pc.z, pc.w};
+        const uint8_t mhi[3] = {S.m[rm(p + 1)][xi], S.m[rm(p)][xi + XK], S.m[rm(p)][xi + 1]};
+        const float rh[3] = {S.rr[r2(p + 1)][ri].y, S.rr[r2(p)][ri + RK].z, S.rr[r2(p)][ri + 1].w};
+        const float ph[3] = {S.P[rp(p + 1)][ri].y, S.P[rp(p)][ri + RK].z, S.P[rp(p)][ri + 1].w};
+        const uint8_t bit[3] = {MU, MV, MW};
+        const float v6 = 6.f * vol;
+        float num = rc.x, den = 2.f * pc.x;
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+            float vL = (m0 & bit[d]) ? 0.f : vol, vR = (mhi[d] & bit[d]) ? 0.f : vol;
+            float iL = __fdividef(vL, v6 + pL[d]);
+            float iR = __fdividef(vR, v6 + ph[d]);
+            num += rL[d] * iL - rh[d] * iR;
+            den -= vL * iL + vR * iR;
+        }
+        out = den != 0.f ? __fdividef(num, den) : 0.f;
+    } else if (m0 & MP) {
         out = __fdividef(rc.x, 2.f * (pc.x + 1.f));
     } else {
         const float rL[3] = {rc.y, rc.z, rc.w};
@@ -164,7 +202,7 @@ __device__ __forceinline__ void pressure_plane(Smem& S, int n, float vol, int p,
     S.dp[dj * DK + dk] = out;
 }
 
-template <bool HAS_X>
+template <bool HAS_X, bool LAP>
 __global__ void __launch_bounds__(NT, 3) k_sweep(Geom g, float vol, const float4* __restrict__ r, const float4* __restrict__ xin,
                                                 float4* __restrict__ xout, const uint8_t* __restrict__ m,
                                                 const float4* __restrict__ P, int flag, int chunk) {
@@ -228,14 +266,14 @@ __global__ void __launch_bounds__(NT, 3) k_sweep(Geom g, float vol, const float4
     }
     cp_wait_all();
     __syncthreads();
-    residual_plane<HAS_X>(S, R, n, vol, i0 - 1);
+    residual_plane<HAS_X, LAP>(S, R, n, vol, i0 - 1);
     __syncthreads();
     if (HAS_X) issue_x(i0 + 2);       // replaces plane i0-2
     issue_r(S.r[r2(i0 + 1)], r, i0 + 1);  // replaces r of i0-1
     cp_commit();
-    residual_plane<HAS_X>(S, R, n, vol, i0);
+    residual_plane<HAS_X, LAP>(S, R, n, vol, i0);
     __syncthreads();
-    pressure_plane(S, n, vol, i0 - 1, j0, k0, flag, tid);
+    pressure_plane<LAP>(S, n, vol, i0 - 1, j0, k0, flag, tid);
     __syncthreads();
     S.dpp[tid] = S.dp[odi];
     cp_wait_all();
@@ -248,9 +286,9 @@ __global__ void __launch_bounds__(NT, 3) k_sweep(Geom g, float vol, const float4
         issue_r(S.r[r2(i + 2)], r, i + 2);
         cp_commit();
         fetch_m(i + 3);
-        residual_plane<HAS_X>(S, R, n, vol, i + 1);
+        residual_plane<HAS_X, LAP>(S, R, n, vol, i + 1);
         __syncthreads();
-        pressure_plane(S, n, vol, i, j0, k0, flag, tid);
+        pressure_plane<LAP>(S, n, vol, i, j0, k0, flag, tid);
         __syncthreads();
         if (out_ok) {
             float4 xo = HAS_X ? S.x[rx(i)][oxi] : make_float4(0.f, 0.f, 0.f, 0.f);
@@ -264,7 +302,12 @@ __global__ void __launch_bounds__(NT, 3) k_sweep(Geom g, float vol, const float4
             const float rf[3] = {rv.y, rv.z, rv.w};
             const float pf[3] = {pv.y, pv.z, pv.w};
             const uint8_t bit[3] = {MU, MV, MW};
-            const uint8_t mlo[3] = {S.m[rm(i - 1)][oxi], S.m[rm(i)][oxi - XK], S.m[rm(i)][oxi - 1]};
+            uint8_t mlo[3] = {0, 0, 0};
+            if (!LAP) {
+                mlo[0] = S.m[rm(i - 1)][oxi];
+                mlo[1] = S.m[rm(i)][oxi - XK];
+                mlo[2] = S.m[rm(i)][oxi - 1];
+            }
             const float dplo[3] = {S.dpp[tid], S.dp[odi - DK], S.dp[odi - 1]};
             float upd[3];
 #pragma unroll
@@ -276,7 +319,9 @@ __global__ void __launch_bounds__(NT, 3) k_sweep(Geom g, float vol, const float4
                 if (!own_red && !lower_red) continue;
                 bool fix = m0 & bit[d];
                 float v = fix ? 0.f : vol;
-                float D = v * (4.f + fc + ((mlo[d] & MP) ? 0.f : 1.f)) + pf[d] + (fix ? 1.f : 0.f);
+                // LAP: a free face has two present cells (fc = 1, lower cell present)
+                float D = LAP ? (fix ? 1.f : 6.f * vol + pf[d])
+                              : v * (4.f + fc + ((mlo[d] & MP) ? 0.f : 1.f)) + pf[d] + (fix ? 1.f : 0.f);
                 float dpo = own_red ? dpown : dplo[d];
                 float cf = own_red ? -v : v;
                 upd[d] = __fdividef(rf[d] - cf * dpo, D);
@@ -296,21 +341,28 @@ __global__ void __launch_bounds__(NT, 3) k_sweep(Geom g, float vol, const float4
 }  // namespace
 
 int sweep32(cudaStream_t st, const Geom& g, float vol, const float4* r, const float4* xin, float4* xout, const uint8_t* m,
-            const float4* P, int flag) {
+            const float4* P, int flag, bool lap) {
     static bool attr_set = false;
     const int smem = (int)sizeof(Smem);
     if (!attr_set) {
-        STG_CK(cudaFuncSetAttribute(k_sweep<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-        STG_CK(cudaFuncSetAttribute(k_sweep<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        STG_CK(cudaFuncSetAttribute(k_sweep<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        STG_CK(cudaFuncSetAttribute(k_sweep<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        STG_CK(cudaFuncSetAttribute(k_sweep<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        STG_CK(cudaFuncSetAttribute(k_sweep<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
         attr_set = true;
     }
-    // planes per block: long marches on big grids (prologue amortised), short ones on small
-    const int chunk = g.n >= 192 ? 32 : (g.n >= 96 ? 16 : 8);
+    // planes per block: long marches on big grids (prologue amortised), short ones on the
+    // coarse levels, where the sequential march, not bandwidth, sets the time
+    const int chunk = g.n >= 192 ? 32 : g.n >= 96 ? 16 : g.n >= 48 ? 8 : g.n >= 24 ? 4 : 2;
     dim3 grid((g.n + SK) / SK, (g.n + SJ) / SJ, (g.n + chunk) / chunk), block(SK, SJ);
-    if (xin)
-        k_sweep<true><<<grid, block, smem, st>>>(g, vol, r, xin, xout, m, P, flag, chunk);
+    if (xin && lap)
+        k_sweep<true, true><<<grid, block, smem, st>>>(g, vol, r, xin, xout, m, P, flag, chunk);
+    else if (xin)
+        k_sweep<true, false><<<grid, block, smem, st>>>(g, vol, r, xin, xout, m, P, flag, chunk);
+    else if (lap)
+        k_sweep<false, true><<<grid, block, smem, st>>>(g, vol, r, xin, xout, m, P, flag, chunk);
     else
-        k_sweep<false><<<grid, block, smem, st>>>(g, vol, r, xin, xout, m, P, flag, chunk);
+        k_sweep<false, false><<<grid, block, smem, st>>>(g, vol, r, xin, xout, m, P, flag, chunk);
     STG_LAUNCH_CK();
     return STG_OK;
 }

@@ -60,40 +60,50 @@ __global__ void k_sensitivity(Geom g, const double* __restrict__ rho, stg_alpha 
     grad[t] = sum * (0.5 * dalpha_of(r, L));
 }
 
-// Linear hat filter: out_i = sum_j w_ij in_j / W_i (forward) or sum_j w_ji in_j / W_j (transpose).
-// dim 2 runs the same loops with a single k plane (nz = 1, no k offsets).
-__global__ void k_filter(int n, int nz, double rmin, int R, int Rz, const double* __restrict__ in, double* __restrict__ out,
-                         int transpose) {
+// Linear hat filter: out_i = sum_j w_ij in_j / W_i (forward) or sum_j w_ji in_j / W_j
+// (transpose), w_ij = max(0, rmin - |c_i - c_j|) over cells inside the domain, W_i =
+// sum_j w_ij. W is computed once per call by k_filter_wsum, so the transpose reads it
+// instead of re-summing every neighbour's weights. dim 2 runs the same loops with a
+// single k plane (nz = 1, no k offsets). Loop order and arithmetic are the same in both
+// kernels, so W_i and the sums are identical wherever they are formed.
+__device__ __forceinline__ double hat_w(double rmin, int a, int b, int c) { return rmin - sqrt((double)(a * a + b * b + c * c)); }
+
+__global__ void k_filter_wsum(int n, int nz, double rmin, int R, int Rz, double* __restrict__ W) {
     long long t = (long long)blockIdx.x * TPB + threadIdx.x;
     if (t >= (long long)n * n * nz) return;
     int k = (int)(t % nz), j = (int)((t / nz) % n), i = (int)(t / ((long long)n * nz));
-    auto at = [&](int a, int b, int c) { return ((long long)a * n + b) * nz + c; };
-    auto wsum = [&](int a0, int b0, int c0) {
-        double W = 0;
-        for (int a = -R; a <= R; a++)
-            for (int b = -R; b <= R; b++)
-                for (int c = -Rz; c <= Rz; c++) {
-                    int ii = a0 + a, jj = b0 + b, kk = c0 + c;
-                    if (ii < 0 || jj < 0 || kk < 0 || ii >= n || jj >= n || kk >= nz) continue;
-                    double w = rmin - sqrt((double)(a * a + b * b + c * c));
-                    if (w > 0) W += w;
-                }
-        return W;
-    };
-    double W = transpose ? 0.0 : wsum(i, j, k), s = 0;
+    double s = 0;
     for (int a = -R; a <= R; a++)
         for (int b = -R; b <= R; b++)
             for (int c = -Rz; c <= Rz; c++) {
                 int ii = i + a, jj = j + b, kk = k + c;
                 if (ii < 0 || jj < 0 || kk < 0 || ii >= n || jj >= n || kk >= nz) continue;
-                double w = rmin - sqrt((double)(a * a + b * b + c * c));
-                if (w <= 0) continue;
-                if (transpose)
-                    s += w * in[at(ii, jj, kk)] / wsum(ii, jj, kk);
-                else
-                    s += w * in[at(ii, jj, kk)];
+                double w = hat_w(rmin, a, b, c);
+                if (w > 0) s += w;
             }
-    out[t] = transpose ? s : s / W;
+    W[t] = s;
+}
+
+__global__ void k_filter(int n, int nz, double rmin, int R, int Rz, const double* __restrict__ in, const double* __restrict__ W,
+                         double* __restrict__ out, int transpose) {
+    long long t = (long long)blockIdx.x * TPB + threadIdx.x;
+    if (t >= (long long)n * n * nz) return;
+    int k = (int)(t % nz), j = (int)((t / nz) % n), i = (int)(t / ((long long)n * nz));
+    double s = 0;
+    for (int a = -R; a <= R; a++)
+        for (int b = -R; b <= R; b++)
+            for (int c = -Rz; c <= Rz; c++) {
+                int ii = i + a, jj = j + b, kk = k + c;
+                if (ii < 0 || jj < 0 || kk < 0 || ii >= n || jj >= n || kk >= nz) continue;
+                double w = hat_w(rmin, a, b, c);
+                if (w <= 0) continue;
+                const long long q = ((long long)ii * n + jj) * nz + kk;
+                if (transpose)
+                    s += w * in[q] / W[q];
+                else
+                    s += w * in[q];
+            }
+    out[t] = transpose ? s : s / W[t];
 }
 
 __device__ __forceinline__ double warp_sum(double v) {
@@ -168,12 +178,14 @@ int sensitivity(cudaStream_t st, const Geom& g, const double* rho, const stg_alp
     return STG_OK;
 }
 
-int density_filter(cudaStream_t st, int dim, int n, double rmin, const double* in, double* out, int transpose) {
+int density_filter(cudaStream_t st, int dim, int n, double rmin, const double* in, double* out, int transpose, double* W) {
     int R = (int)ceil(rmin) - 1;
     if (R < 0) R = 0;
-    const int nz = dim == 3 ? n : 1;
+    const int nz = dim == 3 ? n : 1, Rz = dim == 3 ? R : 0;
     long long nc = (long long)n * n * nz;
-    k_filter<<<grid_for(nc, TPB), TPB, 0, st>>>(n, nz, rmin, R, dim == 3 ? R : 0, in, out, transpose);
+    k_filter_wsum<<<grid_for(nc, TPB), TPB, 0, st>>>(n, nz, rmin, R, Rz, W);
+    STG_LAUNCH_CK();
+    k_filter<<<grid_for(nc, TPB), TPB, 0, st>>>(n, nz, rmin, R, Rz, in, W, out, transpose);
     STG_LAUNCH_CK();
     return STG_OK;
 }

@@ -31,6 +31,7 @@
 #include <cstdio>
 #include <cstring>
 #include <fstream>
+#include <iomanip>
 #include <iostream>
 #include <map>
 #include <string>
@@ -160,6 +161,7 @@ int run(const Args& a) {
 
     make_dir(out);
     std::ofstream log(out + "/log.csv");
+    log.precision(17);
     log << "iteration,objective,volume,change,v_cycles_forward,v_cycles_adjoint,solve_ms,iteration_ms\n";
     std::printf("fluid_topo %dD N=%d test %d: %s law, rmin %.2f, frac %.3f, %d iterations, tol %.1e, %s\n", d, n, test,
                 law_s.c_str(), rmin, frac, iters, opts.tol, stg_version());
