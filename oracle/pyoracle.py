@@ -79,6 +79,11 @@ def lib():
         L.orc_density_noise.argtypes = [I, I, ctypes.c_uint64, D, DP]
         L.orc_bc_parabolic.argtypes = [I, I, I, DP, IP, DP, DP, DP, DP, IP, IP, IP, DP, DP, DP]
         L.orc_bc_test0_3d.argtypes = [I, DP, IP, DP, DP, DP, DP, IP, IP, IP, DP, DP, DP]
+        L.orc_mma_create.restype = P
+        L.orc_mma_create.argtypes = [I]
+        L.orc_mma_destroy.argtypes = [P]
+        L.orc_mma_update.restype = D
+        L.orc_mma_update.argtypes = [P, DP, DP, D, DP, DP, DP]
         _LIB = L
     return _LIB
 
@@ -463,3 +468,56 @@ class Steady2D:
 
     def vcycle(self, r):
         return self._op(self.L.orc2_vcycle, self.level_dof(self.levels - 1), r)
+
+
+# ------------------------------------------------------------------ MMA (one constraint)
+class Mma:
+    """The oracle's MMA restatement (oracle/mma_oracle.cpp): update(x, dfdx, g, dgdx,
+    xmin, xmax) replaces x in place by the next design and returns the dual variable."""
+
+    def __init__(self, n):
+        self.n = n
+        self.L = lib()
+        self.h = self.L.orc_mma_create(n)
+
+    def close(self):
+        if self.h:
+            self.L.orc_mma_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def update(self, x, dfdx, g, dgdx, xmin, xmax):
+        c = lambda a: np.ascontiguousarray(a, dtype=np.float64).ravel()
+        assert x.dtype == np.float64 and x.flags["C_CONTIGUOUS"]
+        d, dg, lo, hi = c(dfdx), c(dgdx), c(xmin), c(xmax)
+        return self.L.orc_mma_update(self.h, dp(x), dp(d), float(g), dp(dg), dp(lo), dp(hi))
+
+
+class RefMma:
+    """The reference's own MMASolver (simplex/ext/mma), built from the reference sources by
+    oracle/ref_build.sh into oracle/_ref (only where those sources are present)."""
+
+    def __init__(self, n, m=1):
+        path = os.path.join(_HERE, "_ref", "libref_mma.so")
+        self.L = ctypes.CDLL(path)
+        self.L.ref_mma_create.restype = P
+        self.L.ref_mma_create.argtypes = [I, I]
+        self.L.ref_mma_destroy.argtypes = [P]
+        self.L.ref_mma_update.argtypes = [P, DP, DP, DP, DP, DP, DP]
+        self.h = self.L.ref_mma_create(n, m)
+
+    def close(self):
+        if self.h:
+            self.L.ref_mma_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def update(self, x, dfdx, g, dgdx, xmin, xmax):
+        c = lambda a: np.ascontiguousarray(a, dtype=np.float64).ravel()
+        assert x.dtype == np.float64 and x.flags["C_CONTIGUOUS"]
+        d, gg, dg, lo, hi = c(dfdx), np.array([g], dtype=np.float64), c(dgdx), c(xmin), c(xmax)
+        self.L.ref_mma_update(self.h, dp(x), dp(d), dp(gg), dp(dg), dp(lo), dp(hi))

@@ -22,3 +22,8 @@ echo "built $OUT/libref_grid3d.so"
 "$NVCC" -std=c++14 -O2 -Xcompiler -fPIC -shared --extended-lambda -w -gencode arch=compute_103a,code=sm_103a \
   -I "$CC_DIR" "$HERE/ref_grid2d_wrap.cu" "$CC_DIR/form01mapping.cu" "$CC_DIR/gpuUtils.cu" -o "$OUT/libref_grid2d.so" -lcublas
 echo "built $OUT/libref_grid2d.so"
+# the vendored MMA solver (plain C++, no dependencies)
+MMA_DIR="$REF/simplex/ext/mma"
+"${CXX:-g++}" -std=c++14 -O2 -fPIC -shared -w -I "$MMA_DIR" "$HERE/ref_mma_wrap.cpp" "$MMA_DIR/MMASolver.cpp" \
+  -o "$OUT/libref_mma.so"
+echo "built $OUT/libref_mma.so"

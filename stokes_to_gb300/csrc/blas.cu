@@ -9,7 +9,7 @@ namespace {
 
 constexpr int TPB = 256;
 constexpr int RGRID = 1216;  // 8 x 152 SMs: reduction grid
-constexpr int MAXV = 8;      // vectors per multi-dot / multi-axpy pass
+constexpr int MAXV = 16;     // vectors per multi-dot / projection pass
 
 __device__ __forceinline__ double warp_sum(double v) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -116,6 +116,44 @@ __global__ void __launch_bounds__(TPB) k_multiaxpy32(long long n4, Tab v, const 
     if (want_norm) block_sums<1>(acc, part + blockIdx.x);
 }
 
+// Projection step of classical Gram-Schmidt on unnormalised basis vectors:
+// out = w - sum_q c_q v_q with c_q = sig2[q] * d[q] (d: the dot products <v_q, w> of the
+// previous pass, sig2[q] = 1/||v_q||^2), in one pass. DOTS: the same pass also returns
+// the dot products <v_q, out> (the re-orthogonalisation coefficients; the v_q are still
+// in registers) and <out, out> in column NV. out may alias w.
+template <int NV, bool DOTS>
+__global__ void __launch_bounds__(TPB) k_proj32(long long n4, Tab v, const double* __restrict__ d, const double* __restrict__ sig2,
+                                                const float4* w, float4* out, double* __restrict__ part) {
+    float c[NV];
+#pragma unroll
+    for (int q = 0; q < NV; q++) c[q] = (float)(sig2[q] * d[q]);
+    float acc[NV + 1];
+#pragma unroll
+    for (int q = 0; q <= NV; q++) acc[q] = 0.f;
+    for (long long t = (long long)blockIdx.x * TPB + threadIdx.x; t < n4; t += (long long)gridDim.x * TPB) {
+        float4 a = w[t];
+        float4 b[NV];
+#pragma unroll
+        for (int q = 0; q < NV; q++) {
+            b[q] = __ldg(v.p[q] + t);
+            a.x -= c[q] * b[q].x;
+            a.y -= c[q] * b[q].y;
+            a.z -= c[q] * b[q].z;
+            a.w -= c[q] * b[q].w;
+        }
+        out[t] = a;
+        if (DOTS) {
+#pragma unroll
+            for (int q = 0; q < NV; q++) acc[q] += a.x * b[q].x + a.y * b[q].y + a.z * b[q].z + a.w * b[q].w;
+        }
+        acc[NV] += a.x * a.x + a.y * a.y + a.z * a.z + a.w * a.w;
+    }
+    double dd[NV + 1];
+#pragma unroll
+    for (int q = 0; q <= NV; q++) dd[q] = acc[q];
+    block_sums<NV + 1>(dd, part + (long long)blockIdx.x * (MAXV + 1));
+}
+
 __global__ void k_scale32(long long n4, const float4* __restrict__ x, const double* __restrict__ nrm2, float4* __restrict__ out) {
     double s0 = *nrm2;
     float s = s0 > 0 ? (float)(1.0 / sqrt(s0)) : 0.f;
@@ -184,37 +222,64 @@ int reduce_parts(cudaStream_t st, const double* parts, int nparts, double* out) 
     return STG_OK;
 }
 
-template <int NV>
-static void launch_axpy(cudaStream_t st, long long n4, const Tab& t, const double* y, double alpha, d4* x) {
-    k_axpy_multi_32to64<NV><<<rgrid(n4), TPB, 0, st>>>(n4, t, y, alpha, x);
+// Calls K<NV>::run(args...) with NV = nb in [1, MAXV].
+template <template <int> class K, class... A>
+static void dispatch_nv(int nb, A&&... args) {
+    switch (nb) {
+        case 1: K<1>::run(args...); break;
+        case 2: K<2>::run(args...); break;
+        case 3: K<3>::run(args...); break;
+        case 4: K<4>::run(args...); break;
+        case 5: K<5>::run(args...); break;
+        case 6: K<6>::run(args...); break;
+        case 7: K<7>::run(args...); break;
+        case 8: K<8>::run(args...); break;
+        case 9: K<9>::run(args...); break;
+        case 10: K<10>::run(args...); break;
+        case 11: K<11>::run(args...); break;
+        case 12: K<12>::run(args...); break;
+        case 13: K<13>::run(args...); break;
+        case 14: K<14>::run(args...); break;
+        case 15: K<15>::run(args...); break;
+        default: K<16>::run(args...); break;
+    }
 }
+
+template <int NV>
+struct AxpyL {
+    static void run(cudaStream_t st, long long n4, const Tab& t, const double* y, double alpha, d4* x) {
+        k_axpy_multi_32to64<NV><<<rgrid(n4), TPB, 0, st>>>(n4, t, y, alpha, x);
+    }
+};
+template <int NV>
+struct DotL {
+    static void run(cudaStream_t st, long long n4, const Tab& t, const float4* w, double* part, bool ww) {
+        if (ww)
+            k_multidot32<NV, true><<<rgrid(n4), TPB, 0, st>>>(n4, t, w, part);
+        else
+            k_multidot32<NV, false><<<rgrid(n4), TPB, 0, st>>>(n4, t, w, part);
+    }
+};
+template <int NV>
+struct ProjL {
+    static void run(cudaStream_t st, long long n4, const Tab& t, const double* d, const double* sig2, const float4* w, float4* out,
+                    double* part, bool dots) {
+        if (dots)
+            k_proj32<NV, true><<<rgrid(n4), TPB, 0, st>>>(n4, t, d, sig2, w, out, part);
+        else
+            k_proj32<NV, false><<<rgrid(n4), TPB, 0, st>>>(n4, t, d, sig2, w, out, part);
+    }
+};
 
 int axpy_multi_32to64(cudaStream_t st, long long n4, const float4* const* z, const double* y, int nz, double alpha, d4* x) {
     for (int j0 = 0; j0 < nz; j0 += MAXV) {
         int nb = nz - j0 < MAXV ? nz - j0 : MAXV;
         Tab t{};
         for (int q = 0; q < nb; q++) t.p[q] = z[j0 + q];
-        switch (nb) {
-            case 1: launch_axpy<1>(st, n4, t, y + j0, alpha, x); break;
-            case 2: launch_axpy<2>(st, n4, t, y + j0, alpha, x); break;
-            case 3: launch_axpy<3>(st, n4, t, y + j0, alpha, x); break;
-            case 4: launch_axpy<4>(st, n4, t, y + j0, alpha, x); break;
-            case 5: launch_axpy<5>(st, n4, t, y + j0, alpha, x); break;
-            case 6: launch_axpy<6>(st, n4, t, y + j0, alpha, x); break;
-            case 7: launch_axpy<7>(st, n4, t, y + j0, alpha, x); break;
-            default: launch_axpy<8>(st, n4, t, y + j0, alpha, x); break;
-        }
+        dispatch_nv<AxpyL>(nb, st, n4, t, y + j0, alpha, x);
         STG_LAUNCH_CK();
     }
     return STG_OK;
-}
-
-template <int NV>
-static void launch_dot(cudaStream_t st, long long n4, const Tab& t, const float4* w, double* part, bool ww) {
-    if (ww)
-        k_multidot32<NV, true><<<rgrid(n4), TPB, 0, st>>>(n4, t, w, part);
-    else
-        k_multidot32<NV, false><<<rgrid(n4), TPB, 0, st>>>(n4, t, w, part);
 }
 
 int multidot32(cudaStream_t st, long long n4, const float4* const* v, int nv, const float4* w, double* h, double* scratch,
@@ -225,16 +290,7 @@ int multidot32(cudaStream_t st, long long n4, const float4* const* v, int nv, co
         bool want_ww = ww && j0 == 0;
         Tab t{};
         for (int q = 0; q < nb; q++) t.p[q] = v[j0 + q];
-        switch (nb) {
-            case 1: launch_dot<1>(st, n4, t, w, scratch, want_ww); break;
-            case 2: launch_dot<2>(st, n4, t, w, scratch, want_ww); break;
-            case 3: launch_dot<3>(st, n4, t, w, scratch, want_ww); break;
-            case 4: launch_dot<4>(st, n4, t, w, scratch, want_ww); break;
-            case 5: launch_dot<5>(st, n4, t, w, scratch, want_ww); break;
-            case 6: launch_dot<6>(st, n4, t, w, scratch, want_ww); break;
-            case 7: launch_dot<7>(st, n4, t, w, scratch, want_ww); break;
-            default: launch_dot<8>(st, n4, t, w, scratch, want_ww); break;
-        }
+        dispatch_nv<DotL>(nb, st, n4, t, w, scratch, want_ww);
         STG_LAUNCH_CK();
         k_reduce_cols<<<1, TPB, 0, st>>>(scratch, (int)g, MAXV + 1, nb, h + j0);
         STG_LAUNCH_CK();
@@ -247,9 +303,11 @@ int multidot32(cudaStream_t st, long long n4, const float4* const* v, int nv, co
 }
 
 template <int NV>
-static void launch_maxpy(cudaStream_t st, long long n4, const Tab& t, const double* h, float4* w, double* part, int want) {
-    k_multiaxpy32<NV><<<rgrid(n4), TPB, 0, st>>>(n4, t, h, w, part, want);
-}
+struct MaxpyL {
+    static void run(cudaStream_t st, long long n4, const Tab& t, const double* h, float4* w, double* part, int want) {
+        k_multiaxpy32<NV><<<rgrid(n4), TPB, 0, st>>>(n4, t, h, w, part, want);
+    }
+};
 
 int multiaxpy32_norm(cudaStream_t st, long long n4, const float4* const* v, int nv, const double* h, float4* w, double* nrm2,
                      double* scratch) {
@@ -263,19 +321,44 @@ int multiaxpy32_norm(cudaStream_t st, long long n4, const float4* const* v, int 
         int last = j0 + nb >= nv;
         Tab t{};
         for (int q = 0; q < nb; q++) t.p[q] = v[j0 + q];
-        switch (nb) {
-            case 1: launch_maxpy<1>(st, n4, t, h + j0, w, scratch, last); break;
-            case 2: launch_maxpy<2>(st, n4, t, h + j0, w, scratch, last); break;
-            case 3: launch_maxpy<3>(st, n4, t, h + j0, w, scratch, last); break;
-            case 4: launch_maxpy<4>(st, n4, t, h + j0, w, scratch, last); break;
-            case 5: launch_maxpy<5>(st, n4, t, h + j0, w, scratch, last); break;
-            case 6: launch_maxpy<6>(st, n4, t, h + j0, w, scratch, last); break;
-            case 7: launch_maxpy<7>(st, n4, t, h + j0, w, scratch, last); break;
-            default: launch_maxpy<8>(st, n4, t, h + j0, w, scratch, last); break;
-        }
+        dispatch_nv<MaxpyL>(nb, st, n4, t, h + j0, w, scratch, last);
         STG_LAUNCH_CK();
     }
     k_reduce_cols<<<1, TPB, 0, st>>>(scratch, (int)g, 1, 1, nrm2);
+    STG_LAUNCH_CK();
+    return STG_OK;
+}
+
+int project32(cudaStream_t st, long long n4, const float4* const* v, int nv, const double* d, const double* sig2, const float4* w,
+              float4* out, double* dots, double* nrm2, double* scratch) {
+    if (nv < 1) {
+        set_error("project32: empty basis");
+        return STG_E_INVALID;
+    }
+    unsigned g = rgrid(n4);
+    if (nv <= MAXV) {
+        Tab t{};
+        for (int q = 0; q < nv; q++) t.p[q] = v[q];
+        dispatch_nv<ProjL>(nv, st, n4, t, d, sig2, w, out, scratch, dots != nullptr);
+        STG_LAUNCH_CK();
+        if (dots) {
+            k_reduce_cols<<<1, TPB, 0, st>>>(scratch, (int)g, MAXV + 1, nv, dots);
+            STG_LAUNCH_CK();
+        }
+        k_reduce_cols<<<1, TPB, 0, st>>>(scratch + nv, (int)g, MAXV + 1, 1, nrm2);
+        STG_LAUNCH_CK();
+        return STG_OK;
+    }
+    // more vectors than one pass holds: subtract in chunks, then a separate dot pass
+    for (int j0 = 0; j0 < nv; j0 += MAXV) {
+        int nb = nv - j0 < MAXV ? nv - j0 : MAXV;
+        Tab t{};
+        for (int q = 0; q < nb; q++) t.p[q] = v[j0 + q];
+        dispatch_nv<ProjL>(nb, st, n4, t, d + j0, sig2 + j0, j0 == 0 ? w : out, out, scratch, false);
+        STG_LAUNCH_CK();
+    }
+    if (dots) return multidot32(st, n4, v, nv, out, dots, scratch, nrm2);
+    k_reduce_cols<<<1, TPB, 0, st>>>(scratch + (nv - ((nv - 1) / MAXV) * MAXV), (int)g, MAXV + 1, 1, nrm2);
     STG_LAUNCH_CK();
     return STG_OK;
 }

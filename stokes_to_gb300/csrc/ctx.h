@@ -65,7 +65,7 @@ struct stg_ctx {
     int m = 0;
     std::vector<float4*> V, Z;
     float4* w = nullptr;
-    double *dscr = nullptr, *dh = nullptr, *dnrm = nullptr, *dy = nullptr;
+    double *dscr = nullptr, *dh = nullptr, *dnrm = nullptr, *dy = nullptr, *dsig2 = nullptr;
     // host-order staging (cells + 3 face arrays)
     double* stage = nullptr;
     int* istage = nullptr;

@@ -78,6 +78,11 @@ int multidot32(cudaStream_t st, long long n4, const float4* const* v, int nv, co
 // w -= sum_j h[j] v_j ; then returns ||w||^2 into nrm2 (device)
 int multiaxpy32_norm(cudaStream_t st, long long n4, const float4* const* v, int nv, const double* h, float4* w, double* nrm2,
                      double* scratch);
+// Classical Gram-Schmidt projection on unnormalised basis vectors in one pass:
+// out = w - sum_q sig2[q] d[q] v_q (d, sig2 on the device; out may alias w); ||out||^2
+// into *nrm2 and, when dots != nullptr, <v_q, out> into dots[0..nv) (device).
+int project32(cudaStream_t st, long long n4, const float4* const* v, int nv, const double* d, const double* sig2, const float4* w,
+              float4* out, double* dots, double* nrm2, double* scratch);
 // out = x / sqrt(*nrm2)
 int scale32(cudaStream_t st, long long n4, float4* x, const double* nrm2, float4* out);
 // deterministic sum of nparts partials -> *out

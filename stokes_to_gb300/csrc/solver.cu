@@ -273,7 +273,7 @@ int solve_core(stg_t* h, const d4* b, d4* x, stg_stats* stats) {
     STG_CK(cudaStreamSynchronize(h->st));
     const double bn = std::sqrt(bn2);
     const int m = h->m;
-    std::vector<double> H((size_t)(m + 1) * m), cs(m), sn(m), g(m + 1), y(m), hcol(m + 2);
+    std::vector<double> H((size_t)(m + 1) * m), cs(m), sn(m), g(m + 1), y(m), hcol(m + 2), sig(m + 1);
     double rel = 0, rn = 0;
     int status = STG_E_NOT_CONVERGED;
     for (int outer = 0; outer <= h->opts.max_outer; outer++) {
@@ -301,37 +301,50 @@ int solve_core(stg_t* h, const d4* b, d4* x, stg_stats* stats) {
         std::fill(g.begin(), g.end(), 0.0);
         g[0] = beta;
         int k = 0;
+        // The basis is kept unnormalised: v_q = sig_q V_q with sig_q = 1/||V_q|| held on the
+        // host (and sig_q^2 on the device), z_q = sig_q Z_q with Z_q = M V_q. Arnoldi step:
+        // pass 1 d1 = V^T w; pass 2 V_{j+1} = w - sum sig^2 d1 V together with
+        // d2 = V^T V_{j+1}; pass 3 (classical Gram-Schmidt's second sweep, only when the
+        // first cancelled most of w: ||V_{j+1}|| < 0.7 ||w||) V_{j+1} -= sum sig^2 d2 V.
+        sig[0] = 1.0;
+        const double one = 1.0;
+        STG_CK(cudaMemcpyAsync(h->dsig2, &one, sizeof(double), cudaMemcpyHostToDevice, h->st));
         for (int j = 0; j < m; j++) {
             STG_TRY(h->precond(h, h->V[j], h->Z[j]));
             STG_TRY(h->apply32(h, h->Z[j], h->w));
-            // classical Gram-Schmidt; a second pass only when the first one cancelled most
-            // of w (||w_new|| < 0.7 ||w||, "twice is enough")
             PROF(h, 6, 16.0 * (j + 2) * n4, multidot32(h->st, n4, h->V.data(), j + 1, h->w, h->dh, h->dscr, h->dnrm + 1));
-            PROF(h, 6, 16.0 * (j + 3) * n4, multiaxpy32_norm(h->st, n4, h->V.data(), j + 1, h->dh, h->w, h->dnrm, h->dscr));
+            PROF(h, 6, 16.0 * (j + 3) * n4,
+                 project32(h->st, n4, h->V.data(), j + 1, h->dh, h->dsig2, h->w, h->V[j + 1], h->dh + m + 2, h->dnrm, h->dscr));
             std::vector<double> h1(j + 1), h2(j + 1, 0.0);
             double nrm[2] = {0, 0};
             STG_CK(cudaMemcpyAsync(h1.data(), h->dh, sizeof(double) * (j + 1), cudaMemcpyDeviceToHost, h->st));
+            STG_CK(cudaMemcpyAsync(h2.data(), h->dh + m + 2, sizeof(double) * (j + 1), cudaMemcpyDeviceToHost, h->st));
             STG_CK(cudaMemcpyAsync(nrm, h->dnrm, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->st));
             STG_CK(cudaStreamSynchronize(h->st));
             double nw2 = nrm[0];
             if (nrm[0] < 0.49 * nrm[1]) {
-                PROF(h, 6, 16.0 * (j + 2) * n4, multidot32(h->st, n4, h->V.data(), j + 1, h->w, h->dh + m + 2, h->dscr, nullptr));
                 PROF(h, 6, 16.0 * (j + 3) * n4,
-                     multiaxpy32_norm(h->st, n4, h->V.data(), j + 1, h->dh + m + 2, h->w, h->dnrm, h->dscr));
-                STG_CK(cudaMemcpyAsync(h2.data(), h->dh + m + 2, sizeof(double) * (j + 1), cudaMemcpyDeviceToHost, h->st));
+                     project32(h->st, n4, h->V.data(), j + 1, h->dh + m + 2, h->dsig2, h->V[j + 1], h->V[j + 1], nullptr, h->dnrm,
+                               h->dscr));
                 STG_CK(cudaMemcpyAsync(&nw2, h->dnrm, sizeof(double), cudaMemcpyDeviceToHost, h->st));
                 STG_CK(cudaStreamSynchronize(h->st));
+            } else {
+                std::fill(h2.begin(), h2.end(), 0.0);
             }
             S.inner_iters++;
-            double hn = std::sqrt(nw2);
-            for (int q = 0; q <= j; q++) hcol[q] = h1[q] + h2[q];
+            const double hn = sig[j] * std::sqrt(nw2);
+            for (int q = 0; q <= j; q++) hcol[q] = sig[q] * sig[j] * (h1[q] + h2[q]);
             hcol[j + 1] = hn;
             if (!std::isfinite(hn)) {
                 status = STG_E_NONFINITE;
                 set_error("non-finite Arnoldi norm");
                 break;
             }
-            if (hn > 0) PROF(h, 6, 32.0 * n4, scale32(h->st, n4, h->w, h->dnrm, h->V[j + 1]));
+            if (nw2 > 0) {
+                sig[j + 1] = 1.0 / std::sqrt(nw2);
+                const double s2 = 1.0 / nw2;
+                STG_CK(cudaMemcpyAsync(h->dsig2 + j + 1, &s2, sizeof(double), cudaMemcpyHostToDevice, h->st));
+            }
             // Givens rotations on the new Hessenberg column
             for (int q = 0; q < j; q++) {
                 double a = hcol[q], c = hcol[q + 1];
@@ -359,6 +372,7 @@ int solve_core(stg_t* h, const d4* b, d4* x, stg_stats* stats) {
             double d = H[q + (size_t)q * (m + 1)];
             y[q] = d != 0 ? s / d : 0.0;
         }
+        for (int q = 0; q < k; q++) y[q] *= sig[q];  // z_q = sig_q Z_q
         STG_CK(cudaMemcpyAsync(h->dy, y.data(), sizeof(double) * k, cudaMemcpyHostToDevice, h->st));
         PROF(h, 6, (16.0 * k + 64.0) * n4, axpy_multi_32to64(h->st, n4, h->Z.data(), h->dy, k, rn, x));
     }
@@ -557,7 +571,8 @@ int stg_create(int dim, int n, const stg_opts* opts, stg_t** out) {
         if ((rc = dalloc(&p, ns))) return fail(rc);
     for (auto& p : h->Z)
         if ((rc = dalloc(&p, ns))) return fail(rc);
-    if ((rc = dalloc(&h->dscr, 1216 * 16)) || (rc = dalloc(&h->dh, 2 * (h->m + 2))) || (rc = dalloc(&h->dnrm, 8)) ||
+    if ((rc = dalloc(&h->dscr, 1216 * 18)) || (rc = dalloc(&h->dh, 2 * (h->m + 2))) || (rc = dalloc(&h->dnrm, 8)) ||
+        (rc = dalloc(&h->dsig2, h->m + 2)) ||
         (rc = dalloc(&h->dy, h->m + 1)) || (rc = dalloc(&h->d_parts, (size_t)nparts + 1216)) || (rc = dalloc(&h->dflag, 1)))
         return fail(rc);
     if ((rc = dalloc(&h->stage, h->ncell + 3 * h->nface)) || (rc = dalloc(&h->istage, h->ncell + 3 * h->nface))) return fail(rc);
@@ -592,7 +607,7 @@ int stg_destroy(stg_t* h) {
     cudaFree(h->w);
     for (auto p : h->V) cudaFree(p);
     for (auto p : h->Z) cudaFree(p);
-    for (double* p : {h->dscr, h->dh, h->dnrm, h->dy, h->stage, h->d_design, h->d_phys, h->d_sens, h->d_sens_design, h->d_vw,
+    for (double* p : {h->dscr, h->dh, h->dnrm, h->dy, h->dsig2, h->stage, h->d_design, h->d_phys, h->d_sens, h->d_sens_design, h->d_vw,
                       h->d_tmp, h->d_gauss, h->d_parts, h->d_wsum})
         cudaFree(p);
     cudaFree(h->istage);

@@ -19,11 +19,12 @@
 //   -method plain|mixed   solver precision form (plain)
 //   -init uniform|noise   initial design: frac everywhere, or seeded smoothed noise
 //   -seed s -sigma g      noise seed and Gaussian width in cells (1, 4)
-//   -frames k   write the design every k iterations (0: final only)
+//   -frames k   write a frame every k iterations (0: the first and the last only)
 //   -dump_boundary dir   write the boundary arrays of the test to dir and exit (no GPU)
 // Output in -o: log.csv (iteration, objective, volume, change, V-cycles, solve times)
-// and, per written frame f, f/x.bin and f/velocity.bin (little-endian float64 in Field
-// order: the design, then the d face-velocity arrays) with f/info.txt giving N and d.
+// and frames in the reference drivers' layout and binary format (frame 0 = the initial
+// design; frame f = the design after iteration f with the velocity of its forward
+// solve): f/x, f/velocity, f/psi_D, f/psi_N, 0/grid, 0/last_frame.txt.
 #include <sys/stat.h>
 
 #include <chrono>
@@ -167,17 +168,10 @@ int run(const Args& a) {
                 law_s.c_str(), rmin, frac, iters, opts.tol, stg_version());
 
     auto write_frame = [&](int f) {
-        const std::string dir = out + "/" + std::to_string(f);
-        make_dir(dir);
-        fluid.download();
-        write_raw(dir + "/x.bin", {&x});
-        std::vector<const std::vector<double>*> v;
-        for (int q = 0; q < d; q++) v.push_back(&fluid.vel[q]);
-        write_raw(dir + "/velocity.bin", v);
-        std::ofstream info(dir + "/info.txt");
-        info << "dim " << d << "\nn " << n << "\nfield_order cell (i*N+j)" << (d == 3 ? "*N+k" : "")
-             << "; face axis q has N+1 entries along q\n";
+        if (f > 0) fluid.download();
+        stg::frames::write_frame<d>(out, f, b, x, fluid.vel, make_dir);
     };
+    write_frame(0);
 
     double J = 0;
     for (int it = 1; it <= iters; it++) {
@@ -207,9 +201,8 @@ int run(const Args& a) {
             << "," << tms << "\n";
         std::printf("iter %4d  J %.6e  vol %.4f  change %.3e  V-cycles %d+%d  %.1f ms\n", it, J, vol, change, vf,
                     as.inner_iters, tms);
-        if (frames > 0 && it % frames == 0) write_frame(it);
+        if ((frames > 0 && it % frames == 0) || it == iters) write_frame(it);
     }
-    write_frame(iters);
     std::printf("final objective %.8e\n", J);
     return 0;
 }

@@ -13,6 +13,7 @@
 #include <array>
 #include <cstdint>
 #include <cstdlib>
+#include <fstream>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -299,5 +300,126 @@ Boundary<d> boundary_parabolic(int n, int width) {
         }
     return b;
 }
+
+// ------------------------------------------------------------------ output frames
+// Frames in the layout and binary format of the reference drivers
+// (FluidTopoOptDriver{,3D}::Write_Output_Files, FT/FluidTopoOptDriver3D.cpp:35-92, with
+// simplex/src/common/Driver.h:57-70): <out>/<frame>/{grid (frame 0), velocity, x, psi_D,
+// psi_N} and <out>/0/last_frame.txt. Encodings (simplex File::Write_Binary, raw
+// little-endian values): Field<T,3> = int32 counts[3] + values; Grid<3> = int32
+// cell_counts[3] + double dx + double domain_min[3]; Particles<3> = int32 n + n x
+// {X[3], V[3], F[3]} doubles + n x {M, C} doubles + n x int32 I. 2D data go through the
+// reference's 3D conversion (counts (N, N, 1), Grid cell_counts (N, N, 0), vectors
+// padded with 0). Velocity is the face-to-cell average 0.5 (u(c) + u(c + e_axis))
+// (Interpolation::Interpolate_Faces_To_Cells). dx = 1, domain_min = 0, as the drivers'
+// grid.Initialize(N, 1.).
+namespace frames {
+
+template <class T>
+void put(std::ostream& o, const T& v) {
+    o.write(reinterpret_cast<const char*>(&v), sizeof(T));
+}
+
+inline void write_grid(const std::string& path, int dim, int n) {
+    std::ofstream o(path, std::ios::binary);
+    const int32_t c[3] = {n, n, dim == 3 ? n : 0};
+    for (int q = 0; q < 3; q++) put(o, c[q]);
+    put(o, 1.0);
+    for (int q = 0; q < 3; q++) put(o, 0.0);
+    if (!o) throw Error(STG_E_INVALID, "cannot write " + path);
+}
+
+// scalar cell field (Field order) as Field<double,3>
+inline void write_scalar(const std::string& path, int dim, int n, const std::vector<double>& a) {
+    std::ofstream o(path, std::ios::binary);
+    const int32_t c[3] = {n, n, dim == 3 ? n : 1};
+    for (int q = 0; q < 3; q++) put(o, c[q]);
+    o.write(reinterpret_cast<const char*>(a.data()), (std::streamsize)(a.size() * sizeof(double)));
+    if (!o) throw Error(STG_E_INVALID, "cannot write " + path);
+}
+
+// face velocity averaged to cells, as Field<Vector3d,3>
+template <int d>
+void write_velocity(const std::string& path, int n, const std::array<std::vector<double>, d>& vel) {
+    std::ofstream o(path, std::ios::binary);
+    const int32_t c[3] = {n, n, d == 3 ? n : 1};
+    for (int q = 0; q < 3; q++) put(o, c[q]);
+    const int nk = d == 3 ? n : 1;
+    std::vector<double> buf((size_t)n * n * nk * 3, 0.0);
+    for (int i = 0; i < n; i++)
+        for (int j = 0; j < n; j++)
+            for (int k = 0; k < nk; k++) {
+                const size_t cell = cidx(d, n, i, j, k);
+                for (int a = 0; a < d; a++) {
+                    const double lo = vel[a][fidx(d, n, a, i, j, k)];
+                    const double hi = vel[a][fidx(d, n, a, i + (a == 0), j + (a == 1), k + (a == 2))];
+                    buf[3 * cell + a] = 0.5 * (lo + hi);
+                }
+            }
+    o.write(reinterpret_cast<const char*>(buf.data()), (std::streamsize)(buf.size() * sizeof(double)));
+    if (!o) throw Error(STG_E_INVALID, "cannot write " + path);
+}
+
+inline void write_particles(const std::string& path, const std::vector<std::array<double, 3>>& X) {
+    std::ofstream o(path, std::ios::binary);
+    const int32_t np = (int32_t)X.size();
+    put(o, np);
+    if (np > 0) {
+        for (auto& x : X)
+            for (int q = 0; q < 3; q++) put(o, x[q]);
+        const std::vector<double> zeros((size_t)np * 3, 0.0);
+        o.write(reinterpret_cast<const char*>(zeros.data()), (std::streamsize)(zeros.size() * sizeof(double)));  // V
+        o.write(reinterpret_cast<const char*>(zeros.data()), (std::streamsize)(zeros.size() * sizeof(double)));  // F
+        o.write(reinterpret_cast<const char*>(zeros.data()), (std::streamsize)(np * sizeof(double)));           // M
+        o.write(reinterpret_cast<const char*>(zeros.data()), (std::streamsize)(np * sizeof(double)));           // C
+        const std::vector<int32_t> izero((size_t)np, 0);
+        o.write(reinterpret_cast<const char*>(izero.data()), (std::streamsize)(np * sizeof(int32_t)));          // I
+    }
+    if (!o) throw Error(STG_E_INVALID, "cannot write " + path);
+}
+
+// One frame of a run: the design, the face velocity and the boundary markers (psi_D:
+// centres of fixed cells; psi_N: centres of fixed faces, x-faces first).
+template <int d>
+void write_frame(const std::string& out, int frame, const Boundary<d>& b, const std::vector<double>& design,
+                 const std::array<std::vector<double>, d>& vel, void (*mkdir_p)(const std::string&)) {
+    const int n = b.n;
+    const std::string dir = out + "/" + std::to_string(frame);
+    mkdir_p(dir);
+    {
+        mkdir_p(out + "/0");
+        std::ofstream t(out + "/0/last_frame.txt");
+        t << frame;
+    }
+    if (frame == 0) write_grid(dir + "/grid", d, n);
+    write_velocity<d>(dir + "/velocity", n, vel);
+    write_scalar(dir + "/x", d, n, design);
+    const int nk = d == 3 ? n : 1;
+    std::vector<std::array<double, 3>> pd, pn;
+    for (int i = 0; i < n; i++)
+        for (int j = 0; j < n; j++)
+            for (int k = 0; k < nk; k++)
+                if (b.cell_fixed[cidx(d, n, i, j, k)]) pd.push_back({i + 0.5, j + 0.5, d == 3 ? k + 0.5 : 0.0});
+    write_particles(dir + "/psi_D", pd);
+    for (int a = 0; a < d; a++) {
+        const int ni = n + (a == 0), nj = n + (a == 1), nkk = d == 3 ? n + (a == 2) : 1;
+        // the 2D driver walks y-faces with j outermost (FluidTopoOptDriver.cpp Write_Output_Files)
+        if (d == 2 && a == 1) {
+            for (int j = 0; j < nj; j++)
+                for (int i = 0; i < ni; i++)
+                    if (b.face_fixed[a][fidx(d, n, a, i, j, 0)]) pn.push_back({i + 0.5, (double)j, 0.0});
+            continue;
+        }
+        for (int i = 0; i < ni; i++)
+            for (int j = 0; j < nj; j++)
+                for (int k = 0; k < nkk; k++)
+                    if (b.face_fixed[a][fidx(d, n, a, i, j, k)])
+                        pn.push_back({a == 0 ? (double)i : i + 0.5, a == 1 ? (double)j : j + 0.5,
+                                      d == 3 ? (a == 2 ? (double)k : k + 0.5) : 0.0});
+    }
+    write_particles(dir + "/psi_N", pn);
+}
+
+}  // namespace frames
 
 }  // namespace stg

@@ -10,8 +10,12 @@ ref_grid2d_index.npz   the 2D blocked-layout tables produced by the reference's 
                        host code (oracle/_ref/libref_grid2d.so).
 oracle2d_n16.npz       2D oracle outputs on a seeded 16^2 problem (same contents as the
                        3D fixture).
+ref_mma.npz            six updates of the reference's own MMA solver (oracle/_ref/libref_mma.so,
+                       built from simplex/ext/mma by oracle/ref_build.sh) on a seeded problem
+                       with the reference optimizer's settings (one volume constraint with
+                       coefficient 1e4, move limit 0.2, bounds [0.01, 1]).
 
-usage: python tests/golden/make_golden.py [3d] [2d]
+usage: python tests/golden/make_golden.py [3d] [2d] [mma]
 """
 import ctypes
 import os
@@ -115,12 +119,42 @@ def oracle_regression_2d():
                         vcycle_b=o.vcycle(bb), solution=sol, rel_true=st["rel_true"])
 
 
+def mma_problem(n=2000, iters=6, seed=0):
+    """Seeded inputs of the MMA fixture: per update a negative sensitivity, the volume
+    constraint g = 1e4 (mean x - 0.3) with gradient 1e4 / n, and bounds
+    [max(0.01, x - 0.2), min(1, x + 0.2)] (simplex/src/optimization/OptimizerMma.h:96-128)."""
+    rng = np.random.default_rng(seed)
+    return [-np.abs(rng.standard_normal(n)) * (1 + 3 * rng.random(n)) for _ in range(iters)]
+
+
+def mma_run(solver, n, dfs, frac=0.3):
+    x = np.full(n, frac)
+    xs = []
+    for df in dfs:
+        g = 1e4 * (x.mean() - frac)
+        dg = np.full(n, 1e4 / n)
+        solver.update(x, df, g, dg, np.maximum(0.01, x - 0.2), np.minimum(1.0, x + 0.2))
+        xs.append(x.copy())
+    return np.array(xs)
+
+
+def ref_mma():
+    from oracle import pyoracle as po
+
+    n = 2000
+    dfs = mma_problem(n)
+    xs = mma_run(po.RefMma(n), n, dfs)
+    np.savez_compressed(os.path.join(HERE, "ref_mma.npz"), dfdx=np.array(dfs), x=xs)
+
+
 if __name__ == "__main__":
-    what = sys.argv[1:] or ["3d", "2d"]
+    what = sys.argv[1:] or ["3d", "2d", "mma"]
     if "3d" in what:
         ref_index_tables()
         oracle_regression()
     if "2d" in what:
         ref_index_tables_2d()
         oracle_regression_2d()
+    if "mma" in what:
+        ref_mma()
     print("wrote", os.listdir(HERE))

@@ -19,6 +19,14 @@ def driver(stg):
     return DRIVER
 
 
+def read_field(path, n, dim):
+    """A scalar Field<double,3> file of the reference frame format: int32 counts[3] + values."""
+    raw = open(path, "rb").read()
+    counts = np.frombuffer(raw[:12], dtype=np.int32)
+    assert tuple(counts) == (n, n, n if dim == 3 else 1)
+    return np.frombuffer(raw[12:], dtype=np.float64).reshape((n,) * dim)
+
+
 def _dump(driver, tmp_path, dim, test, n):
     out = tmp_path / f"b{dim}_{test}_{n}"
     subprocess.run([driver, "-driver", "0" if dim == 2 else "1", "-test", str(test), "-s", str(n), "-frac", "0.3",
@@ -76,7 +84,14 @@ def test_driver_2d_optimization_matches_oracle(oracle, driver, tmp_path):
     subprocess.run([driver, "-driver", "0", "-test", "1", "-s", str(n), "-frac", str(frac), "-lf", str(iters), "-o",
                     str(out)], check=True)
     log = np.genfromtxt(out / "log.csv", delimiter=",", names=True)
-    x_gpu = np.fromfile(out / str(iters) / "x.bin", dtype=np.float64).reshape(n, n)
+    x_gpu = read_field(out / str(iters) / "x", n, 2)
+    # reference frame layout: grid at frame 0, last_frame.txt, velocity as cell vectors,
+    # psi_N holding the 4N fixed boundary faces
+    assert np.array_equal(read_field(out / "0" / "x", n, 2), np.full((n, n), frac))
+    assert (out / "0" / "grid").stat().st_size == 3 * 4 + 8 + 3 * 8
+    assert (out / "0" / "last_frame.txt").read_text().strip() == str(iters)
+    assert (out / str(iters) / "velocity").stat().st_size == 3 * 4 + n * n * 3 * 8
+    assert int(np.fromfile(out / str(iters) / "psi_N", dtype=np.int32, count=1)[0]) == 4 * n
 
     b = oracle.bc_parabolic(n, 2, width=n // 4)
     x = np.full((n, n), frac)
