@@ -184,6 +184,22 @@ int stg_filter(stg_t* h, double rmin, const double* in, double* out, int transpo
 int stg_oc_update(stg_t* h, double rmin, const double* x, const double* dc, double frac, double move, double lo, double hi,
                   double* x_new, double* lambda_out);
 
+/* One design update of the reference optimizer: the loop body of
+ * OptimizerMMA::Optimize_MMA (simplex/src/optimization/OptimizerMma.h:96-128), i.e. the
+ * Method of Moving Asymptotes of simplex/ext/mma/MMASolver.cpp (dual interior point), with
+ * the volume constraint of FluidTopoOpt3D::Compute_Constraint(_Grad)
+ * (fluid_topo/FluidTopoOpt3D.cpp:19-39): g = coef (mean x - frac), dg/dx = coef / ncell,
+ * and per-cell bounds [max(lo, x - move), min(hi, x + move)] (the reference: coef 1e4,
+ * lo 0.01, hi 1, move 0.2). The asymptotes carry over between calls (stg_mma_reset starts
+ * a new run, as a new MMASolver does). x: host design, or NULL for the device-resident
+ * design; dfdx: host gradient, or NULL for the device sensitivity left by
+ * stg_filter(..., transpose = 1). x_new (host, may alias x, or NULL) receives the new
+ * design, which also stays on the device; change: max |x_new - x|, the reference's
+ * stopping quantity. */
+int stg_mma_update(stg_t* h, const double* x, const double* dfdx, double frac, double coef, double lo, double hi, double move,
+                   double* x_new, double* change);
+int stg_mma_reset(stg_t* h);
+
 /* The optimality-criteria update of stg_oc_update for callers that cannot allocate
  * device memory: applications that reserve the whole GPU for their own pool, plugins
  * running under another framework's allocator budget, and latency-sensitive loops that

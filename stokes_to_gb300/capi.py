@@ -39,7 +39,7 @@ EXPORTS = [
     "stg_energy_grad_x", "stg_energy_grad_q", "stg_set_density", "stg_adjoint_sensitivity", "stg_filter", "stg_oc_update",
     "stg_apply_A_device", "stg_apply_E_device", "stg_update", "stg_vcycle_device", "stg_apply_op_device",
     "stg_level_descr_device", "stg_density_noise", "stg_set_stream", "stg_kernel_launches", "stg_profile",
-    "stg_profile_read", "stg_profile_name", "stg_oc_update_noalloc",
+    "stg_profile_read", "stg_profile_name", "stg_oc_update_noalloc", "stg_mma_update", "stg_mma_reset",
 ]
 STG_PROF_NCLASS = 11
 
@@ -108,6 +108,8 @@ def lib():
         L.stg_adjoint_sensitivity.argtypes = [P, ctypes.POINTER(Alpha), DP, ctypes.POINTER(Stats)]
         L.stg_filter.argtypes = [P, D, DP, DP, I]
         L.stg_oc_update.argtypes = [P, D, DP, DP, D, D, D, D, DP, DP]
+        L.stg_mma_update.argtypes = [P, DP, DP, D, D, D, D, D, DP, DP]
+        L.stg_mma_reset.argtypes = [P]
         L.stg_apply_A_device.argtypes = [P, I, P, P]
         L.stg_apply_E_device.argtypes = [P, P, P]
         L.stg_update.argtypes = [P]
@@ -283,6 +285,16 @@ class Solver:
         lam = np.zeros(1)
         check(self.L.stg_oc_update(self.h, rmin, dp(_c64(x)), dp(_c64(dc)), frac, move, lo, hi, dp(out), dp(lam)))
         return out, float(lam[0])
+
+    def mma_update(self, x, dfdx, frac, coef=1e4, lo=0.01, hi=1.0, move=0.2, want=True):
+        """One MMA design update (reference optimizer); returns (x_new, change)."""
+        out = np.zeros((self.n,) * self.dim) if want else None
+        ch = np.zeros(1)
+        check(self.L.stg_mma_update(self.h, dp(_c64(x)), dp(_c64(dfdx)), frac, coef, lo, hi, move, dp(out), dp(ch)))
+        return out, float(ch[0])
+
+    def mma_reset(self):
+        return check(self.L.stg_mma_reset(self.h))
 
     def density_noise(self, seed, sigma, want=True):
         out = np.zeros((self.n,) * self.dim) if want else None

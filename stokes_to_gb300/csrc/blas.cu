@@ -46,6 +46,8 @@ struct Tab {
     const float4* p[MAXV];
 };
 
+// x64 += sum_q (alpha y_q) z_q, accumulated in FP64 (an FP32 sum of the basis loses
+// the outer refinement step's accuracy to cancellation among the terms)
 template <int NV>
 __global__ void __launch_bounds__(TPB) k_axpy_multi_32to64(long long n4, Tab z, const double* __restrict__ y, double alpha,
                                                            d4* __restrict__ x) {

@@ -82,7 +82,8 @@ struct stg_ctx {
     int (*precond)(stg_t*, const float4* rhs, float4* out) = nullptr;
     int (*apply32)(stg_t*, const float4* x, float4* y) = nullptr;
     int (*finish)(stg_t*, const stg::d4* b, stg::d4* x) = nullptr;  // optional, after the refinement loop
-    struct Ctx2* c2 = nullptr;  // 2D state (dim == 2)
+    struct Ctx2* c2 = nullptr;        // 2D state (dim == 2)
+    struct MmaState* mma = nullptr;   // MMA optimizer state (mma.cu), created on first use
 };
 
 
@@ -111,6 +112,12 @@ int apply_E2d(stg_t* h, double* out, const double* in);
 int vcycle2d(stg_t* h, double* out, const double* in);
 int apply_op2d(stg_t* h, int op, int level, double* out, const double* in);
 int level_descr2d(stg_t* h, int level, double* vol, double* pen, uint8_t* fixed);
+
+// MMA design update (mma.cu) on device cell arrays; d_xout may alias d_x
+int mma_update(stg_t* h, const double* d_x, const double* d_df, double frac, double coef, double lo, double hi, double movlim,
+               double* d_xout, double* change);
+int mma_reset(stg_t* h);
+void mma_free(stg_t* h);
 
 template <class T>
 int dalloc(T** p, size_t count) {

@@ -590,6 +590,7 @@ int stg_destroy(stg_t* h) {
     if (!h) return STG_OK;
     if (h->st) cudaStreamSynchronize(h->st);
     destroy2d(h);
+    mma_free(h);
     for (auto& L : h->lv) {
         cudaFree(L.m);
         cudaFree(L.P64);
@@ -924,6 +925,33 @@ int stg_oc_update(stg_t* h, double rmin, const double* x, const double* dc, doub
     STG_CK(cudaStreamSynchronize(h->st));
     if (lambda_out) *lambda_out = lmid;
     return STG_OK;
+}
+
+int stg_mma_update(stg_t* h, const double* x, const double* dfdx, double frac, double coef, double lo, double hi, double move,
+                   double* x_new, double* change) {
+    STG_TRY(check_handle(h));
+    if (!(hi > lo) || !(move > 0)) {
+        set_error("MMA bounds need hi > lo and move > 0");
+        return STG_E_INVALID;
+    }
+    if (x) STG_CK(cudaMemcpyAsync(h->d_design, x, sizeof(double) * h->ncell, cudaMemcpyHostToDevice, h->st));
+    const double* ddf = h->d_sens_design;
+    if (dfdx) {
+        STG_CK(cudaMemcpyAsync(h->d_sens, dfdx, sizeof(double) * h->ncell, cudaMemcpyHostToDevice, h->st));
+        ddf = h->d_sens;
+    }
+    double ch = 0;
+    STG_TRY(mma_update(h, h->d_design, ddf, frac, coef, lo, hi, move, h->d_tmp, &ch));
+    STG_CK(cudaMemcpyAsync(h->d_design, h->d_tmp, sizeof(double) * h->ncell, cudaMemcpyDeviceToDevice, h->st));
+    if (x_new) STG_CK(cudaMemcpyAsync(x_new, h->d_design, sizeof(double) * h->ncell, cudaMemcpyDeviceToHost, h->st));
+    STG_CK(cudaStreamSynchronize(h->st));
+    if (change) *change = ch;
+    return STG_OK;
+}
+
+int stg_mma_reset(stg_t* h) {
+    STG_TRY(check_handle(h));
+    return mma_reset(h);
 }
 
 int stg_density_noise(stg_t* h, uint64_t seed, double sigma, double* out) {

@@ -338,17 +338,317 @@ __global__ void __launch_bounds__(NT, 3) k_sweep(Geom g, float vol, const float4
     }
 }
 
+// ---------------------------------------------------------------- Laplacian-form sweep
+// The same march and algebra in the Laplacian form (stencil.cuh), written so that the
+// plane loop does little besides the arithmetic: ring slots are rotated element offsets
+// into flat shared arrays (no modular ring indices), every per-thread index, validity
+// flag and global offset is formed once before the march, global plane pointers advance
+// by one plane per step, and the mask ring holds 4 planes (the Laplacian form reads no
+// mask of the plane below).
+struct SmemL {
+    float4 x[4 * XN];
+    float4 P[3 * RN];
+    float4 r[2 * RN];
+    float4 rr[2 * RN];
+    float dp[DJ * DK];
+    float dpp[SJ * SK];
+    uint8_t m[4 * XN];
+};
+
+struct Stage {
+    int s;   // shared index in the plane (-1: none)
+    int jk;  // global offset in the plane
+};
+
+__device__ __forceinline__ Stage make_stage(const Geom& g, int e, int nelem, int w, int j_org, int k_org) {
+    Stage st;
+    int j = j_org + e / w, k = k_org + e % w;
+    bool ok = e < nelem && j >= -1 && j <= g.n + 1 && k >= -1 && k <= g.n + 2;
+    st.s = e < nelem ? e : -1;
+    st.jk = ok ? (j + 1) * g.sz + (k + 1) : -1;  // -1: outside the allocation (zero fill)
+    return st;
+}
+
+__device__ __forceinline__ void cp16s(unsigned dst, const void* src, bool ok) {
+    int n = ok ? 16 : 0;
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(dst), "l"(src), "r"(n) : "memory");
+}
+
+template <bool HAS_X>
+__global__ void __launch_bounds__(NT, 3) k_sweep_lap(Geom g, float vol, const float4* __restrict__ r, const float4* __restrict__ xin,
+                                                    float4* __restrict__ xout, const uint8_t* __restrict__ m,
+                                                    const float4* __restrict__ P, int flag, int chunk) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    SmemL& S = *reinterpret_cast<SmemL*>(smem_raw);
+    const int n = g.n;
+    const int tk = threadIdx.x, tj = threadIdx.y, tid = tj * SK + tk;
+    const int k0 = blockIdx.x * SK, j0 = blockIdx.y * SJ, i0 = blockIdx.z * chunk;
+    const int i1 = min(i0 + chunk, n + 1);
+    const int j = j0 + tj, k = k0 + tk;
+    const long long plane = (long long)g.sy * g.sz;
+    const float v6 = 6.f * vol;
+
+    // staging elements: x / mask region (X) and P / r region (R), two per thread
+    const Stage X0 = make_stage(g, tid, XN, XK, j0 - 2, k0 - 2), X1 = make_stage(g, tid + NT, XN, XK, j0 - 2, k0 - 2);
+    const Stage R0 = make_stage(g, tid, RN, RK, j0 - 1, k0 - 1), R1 = make_stage(g, tid + NT, RN, RK, j0 - 1, k0 - 1);
+    const unsigned sx = (unsigned)__cvta_generic_to_shared(S.x), sP = (unsigned)__cvta_generic_to_shared(S.P),
+                   sr = (unsigned)__cvta_generic_to_shared(S.r);
+
+    // residual elements: rr/P index e and x/mask index xi, and whether (j,k) lies in [0,n]^2
+    const int re0 = tid, re1 = tid + NT;
+    const int rx0 = re0 + (re0 / RK) * (XK - RK) + XK + 1, rx1 = re1 + (re1 / RK) * (XK - RK) + XK + 1;
+    auto in_box = [&](int e) {
+        int jj = j0 - 1 + e / RK, kk = k0 - 1 + e % RK;
+        return e < RN && jj >= 0 && jj <= n && kk >= 0 && kk <= n;
+    };
+    const bool rb0 = in_box(re0), rb1 = in_box(re1);
+
+    // pressure-phase cell of this thread for the two plane parities
+    const int pdj = tid / DRED, pq = tid % DRED, pj = j0 - 1 + pdj;
+    const bool p_thread = tid < DJ * DRED;
+    const int ppar0 = (pj + flag - (k0 - 1)) & 1;  // dk = ((p & 1) ^ ppar0) + 2 pq
+    // (the two parities as scalars: a runtime-indexed array would live in local memory)
+    const int pdk0 = 2 * pq, pdk1 = 2 * pq + 1;
+    const bool pok0 = p_thread && pdk0 < DK && pj >= 0 && k0 - 1 + pdk0 >= 0 && pj < n && k0 - 1 + pdk0 < n;
+    const bool pok1 = p_thread && pdk1 < DK && pj >= 0 && k0 - 1 + pdk1 >= 0 && pj < n && k0 - 1 + pdk1 < n;
+
+    // update-phase slot
+    const bool out_ok = j <= n && k <= n;
+    const long long out_jk = (long long)(j + 1) * g.sz + (k + 1);
+    const int oxi = (tj + 2) * XK + (tk + 2), ori = (tj + 1) * RK + (tk + 1), odi = (tj + 1) * DK + (tk + 1);
+    const bool jk_cell = j < n && k < n;
+    const int opar = (j + k + flag) & 1;  // own colour is red when ((i & 1) ^ opar) == 0
+    const bool lo_j_ok = j >= 1 && k < n, lo_k_ok = k >= 1 && j < n;
+
+    auto issue_x = [&](int slot, int p, const float4* src) {  // plane p of x into ring slot
+        const bool pok = p >= -1 && p <= n + 1;
+        if (X0.s >= 0) cp16s(sx + 16u * (slot + X0.s), (pok && X0.jk >= 0) ? (const void*)(src + X0.jk) : (const void*)xin, pok && X0.jk >= 0);
+        if (X1.s >= 0) cp16s(sx + 16u * (slot + X1.s), (pok && X1.jk >= 0) ? (const void*)(src + X1.jk) : (const void*)xin, pok && X1.jk >= 0);
+    };
+    auto issue_r = [&](unsigned base, int slot, int p, const float4* src, const float4* any) {
+        const bool pok = p >= -1 && p <= n + 1;
+        if (R0.s >= 0) cp16s(base + 16u * (slot + R0.s), (pok && R0.jk >= 0) ? (const void*)(src + R0.jk) : (const void*)any, pok && R0.jk >= 0);
+        if (R1.s >= 0) cp16s(base + 16u * (slot + R1.s), (pok && R1.jk >= 0) ? (const void*)(src + R1.jk) : (const void*)any, pok && R1.jk >= 0);
+    };
+    uint8_t mr0 = MALL, mr1 = MALL;
+    auto fetch_m = [&](int p, const uint8_t* src) {
+        const bool pok = p >= -1 && p <= n + 1;
+        mr0 = (pok && X0.jk >= 0) ? __ldg(src + X0.jk) : (uint8_t)MALL;
+        mr1 = (pok && X1.jk >= 0) ? __ldg(src + X1.jk) : (uint8_t)MALL;
+    };
+    auto store_m = [&](int slot) {
+        if (X0.s >= 0) S.m[slot + X0.s] = mr0;
+        if (X1.s >= 0) S.m[slot + X1.s] = mr1;
+    };
+
+    // residual of plane p: x slots (p-1, p, p+1), r / P / mask slots of p, into rr slot
+    auto residual = [&](int p, int xa, int xb, int xc, int rs, int ps, int ms, int rrs) {
+        const bool pin = p >= 0 && p <= n;
+        auto one = [&](int e, int xi, bool box) {
+            float4 out = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (pin && box) {
+                const float4 rv = S.r[rs + e];
+                if (HAS_X) {
+                    auto q = [&](int idx) {
+                        const float4 v = S.x[idx];
+                        return Q4<float>{v.x, v.y, v.z, v.w};
+                    };
+                    const float4 pv = S.P[ps + e];
+                    float o[4];
+                    lap_core<float>(q(xb + xi), q(xa + xi), q(xc + xi), q(xb + xi - XK), q(xb + xi + XK), q(xb + xi - 1),
+                                    q(xb + xi + 1), Q4<float>{pv.x, pv.y, pv.z, pv.w}, vol, o);
+                    o[0] = rv.x - o[0];
+                    o[1] = rv.y - o[1];
+                    o[2] = rv.z - o[2];
+                    o[3] = rv.w - o[3];
+                    mask4<float>(S.m[ms + xi], o);
+                    out = make_float4(o[0], o[1], o[2], o[3]);
+                } else {
+                    out = rv;  // r is zero on fixed unknowns
+                }
+            }
+            S.rr[rrs + e] = out;
+        };
+        one(re0, rx0, rb0);
+        if (re1 < RN) one(re1, rx1, rb1);
+    };
+
+    // pressure update of the red cells of plane p (rr slots p, p+1; P slots p, p+1; mask slots p, p+1)
+    auto pressure = [&](int p, int rr0, int rr1, int p0, int p1, int m0s, int m1s) {
+        const int b = (p & 1) ^ ppar0;
+        if (!(b ? pok1 : pok0) || p < 0 || p >= n) return;
+        const int dk = b ? pdk1 : pdk0;
+        const int ri = pdj * RK + dk, xi = (pdj + 1) * XK + (dk + 1);
+        const float4 rc = S.rr[rr0 + ri], pc = S.P[p0 + ri];
+        const uint8_t mo = S.m[m0s + xi];
+        const float rL[3] = {rc.y, rc.z, rc.w}, pL[3] = {pc.y, pc.z, pc.w};
+        const uint8_t mhi[3] = {S.m[m1s + xi], S.m[m0s + xi + XK], S.m[m0s + xi + 1]};
+        const float rh[3] = {S.rr[rr1 + ri].y, S.rr[rr0 + ri + RK].z, S.rr[rr0 + ri + 1].w};
+        const float ph[3] = {S.P[p1 + ri].y, S.P[p0 + ri + RK].z, S.P[p0 + ri + 1].w};
+        const uint8_t bit[3] = {MU, MV, MW};
+        float num = rc.x, den = 2.f * pc.x;
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+            const float vL = (mo & bit[d]) ? 0.f : vol, vR = (mhi[d] & bit[d]) ? 0.f : vol;
+            const float iL = __fdividef(vL, v6 + pL[d]), iR = __fdividef(vR, v6 + ph[d]);
+            num += rL[d] * iL - rh[d] * iR;
+            den -= vL * iL + vR * iR;
+        }
+        S.dp[pdj * DK + dk] = den != 0.f ? __fdividef(num, den) : 0.f;
+    };
+
+    // ring slots as element offsets (rotated each plane)
+    int xm1 = 0 * XN, x0 = 1 * XN, x1 = 2 * XN, x2 = 3 * XN;  // x(i-1), x(i), x(i+1), x(i+2)
+    int pm1 = 0 * RN, p0 = 1 * RN, p1 = 2 * RN;               // P(i-1), P(i), P(i+1)
+    int r0 = 0 * RN, r1 = 1 * RN;                             // r(i), r(i+1)
+    int rrm1 = 0 * RN, rr0 = 1 * RN;                          // rr(i-1), rr(i)
+    int mm1 = 0 * XN, m0 = 1 * XN, m1 = 2 * XN, m2 = 3 * XN;  // masks of planes i-1 .. i+2
+
+    // prologue: planes i0-2 .. i0+1 of x, i0-1 .. i0+1 of P, i0-1 and i0 of r, masks i0-1 .. i0+2
+    const float4* gx = xin + (i0 - 1) * plane;  // plane p lives at (p + 1) * plane: this is plane i0-2
+    if (HAS_X) {
+        issue_x(xm1, i0 - 2, gx);
+        issue_x(x0, i0 - 1, gx + plane);
+        issue_x(x1, i0, gx + 2 * plane);
+        issue_x(x2, i0 + 1, gx + 3 * plane);
+    }
+    const float4* gP = P + i0 * plane;
+    issue_r(sP, pm1, i0 - 1, gP, P);
+    issue_r(sP, p0, i0, gP + plane, P);
+    issue_r(sP, p1, i0 + 1, gP + 2 * plane, P);
+    const float4* gr = r + i0 * plane;
+    issue_r(sr, r0, i0 - 1, gr, r);
+    issue_r(sr, r1, i0, gr + plane, r);
+    cp_commit();
+    const uint8_t* gm = m + i0 * plane;  // plane i0-1
+    fetch_m(i0 - 1, gm);
+    store_m(mm1);
+    fetch_m(i0, gm + plane);
+    store_m(m0);
+    fetch_m(i0 + 1, gm + 2 * plane);
+    store_m(m1);
+    fetch_m(i0 + 2, gm + 3 * plane);
+    store_m(m2);
+    cp_wait_all();
+    __syncthreads();
+    // residual of i0-1: x(i0-2, i0-1, i0) = slots (xm1, x0, x1), r(i0-1) = r0, P(i0-1) = pm1, mask(i0-1) = mm1
+    residual(i0 - 1, xm1, x0, x1, r0, pm1, mm1, rrm1);
+    __syncthreads();
+    if (HAS_X) issue_x(xm1, i0 + 2, gx + 4 * plane);  // x(i0+2) replaces x(i0-2)
+    issue_r(sr, r0, i0 + 1, gr + 2 * plane, r);       // r(i0+1) replaces r(i0-1)
+    cp_commit();
+    // residual of i0: x(i0-1, i0, i0+1) = (x0, x1, x2), r(i0) = r1, P(i0) = p0, mask(i0) = m0
+    residual(i0, x0, x1, x2, r1, p0, m0, rr0);
+    __syncthreads();
+    pressure(i0 - 1, rrm1, rr0, pm1, p0, mm1, m0);
+    __syncthreads();
+    S.dpp[tid] = S.dp[odi];
+    cp_wait_all();
+    __syncthreads();
+    // rotate to the loop's view at i = i0: x(i0-1..i0+2) = (x0, x1, x2, xm1), r(i0) = r1,
+    // r(i0+1) = r0, rr(i0-1) = rrm1, rr(i0) = rr0, P(i0-1) = pm1, masks i0-1 .. i0+2 unchanged
+    {
+        int t = xm1;
+        xm1 = x0;
+        x0 = x1;
+        x1 = x2;
+        x2 = t;
+        t = r0;
+        r0 = r1;
+        r1 = t;
+    }
+    gx += 5 * plane;  // plane i0+3
+    gP += 3 * plane;  // plane i0+2
+    gr += 3 * plane;  // plane i0+2
+    gm += 4 * plane;  // plane i0+3
+    float4* gout = xout + (i0 + 1) * plane + out_jk;
+
+    for (int i = i0; i < i1; i++) {
+        // stream x(i+3) into the slot of x(i-1), P(i+2) into P(i-1), r(i+2) into r(i)
+        if (HAS_X) issue_x(xm1, i + 3, gx);
+        issue_r(sP, pm1, i + 2, gP, P);
+        issue_r(sr, r0, i + 2, gr, r);
+        cp_commit();
+        fetch_m(i + 3, gm);
+        residual(i + 1, x0, x1, x2, r1, p1, m1, rrm1);
+        __syncthreads();
+        pressure(i, rr0, rrm1, p0, p1, m0, m1);
+        __syncthreads();
+        if (out_ok) {
+            float4 xo = HAS_X ? S.x[x0 + oxi] : make_float4(0.f, 0.f, 0.f, 0.f);
+            const float4 rv = S.rr[rr0 + ori], pv = S.P[p0 + ori];
+            const uint8_t mo = S.m[m0 + oxi];
+            const bool cell = jk_cell && i < n;
+            const bool own_col = ((i & 1) ^ opar) == 0;  // (i + j + k + flag) even
+            const bool own_red = cell && own_col;
+            const float dpown = S.dp[odi];
+            if (own_red) xo.x += dpown;
+            // the lower cells have the other colour: red exactly when the own colour is black
+            const bool lo_ok[3] = {!own_col && i >= 1 && jk_cell, !own_col && lo_j_ok && i < n, !own_col && lo_k_ok && i < n};
+            const float dplo[3] = {S.dpp[tid], S.dp[odi - DK], S.dp[odi - 1]};
+            const float rf[3] = {rv.y, rv.z, rv.w}, pf[3] = {pv.y, pv.z, pv.w};
+            const uint8_t bit[3] = {MU, MV, MW};
+            float upd[3];
+#pragma unroll
+            for (int d = 0; d < 3; d++) {
+                upd[d] = 0.f;
+                if (!own_red && !lo_ok[d]) continue;
+                const bool fix = mo & bit[d];
+                const float v = fix ? 0.f : vol;
+                const float D = fix ? 1.f : v6 + pf[d];
+                upd[d] = __fdividef(rf[d] - (own_red ? -v : v) * (own_red ? dpown : dplo[d]), D);
+            }
+            xo.y += upd[0];
+            xo.z += upd[1];
+            xo.w += upd[2];
+            *gout = xo;
+        }
+        store_m(mm1);  // mask (i+3) into the slot of mask (i-1)
+        cp_wait_all();
+        __syncthreads();
+        S.dpp[tid] = S.dp[odi];
+        // rotate the rings and advance the plane pointers
+        {
+            int t = xm1;
+            xm1 = x0;
+            x0 = x1;
+            x1 = x2;
+            x2 = t;
+            t = pm1;
+            pm1 = p0;
+            p0 = p1;
+            p1 = t;
+            t = r0;
+            r0 = r1;
+            r1 = t;
+            t = rrm1;
+            rrm1 = rr0;
+            rr0 = t;
+            t = mm1;
+            mm1 = m0;
+            m0 = m1;
+            m1 = m2;
+            m2 = t;
+        }
+        gx += plane;
+        gP += plane;
+        gr += plane;
+        gm += plane;
+        gout += plane;
+    }
+}
+
 }  // namespace
 
 int sweep32(cudaStream_t st, const Geom& g, float vol, const float4* r, const float4* xin, float4* xout, const uint8_t* m,
             const float4* P, int flag, bool lap) {
     static bool attr_set = false;
-    const int smem = (int)sizeof(Smem);
+    const int smem = (int)sizeof(Smem), smem_l = (int)sizeof(SmemL);
     if (!attr_set) {
         STG_CK(cudaFuncSetAttribute(k_sweep<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
         STG_CK(cudaFuncSetAttribute(k_sweep<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-        STG_CK(cudaFuncSetAttribute(k_sweep<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-        STG_CK(cudaFuncSetAttribute(k_sweep<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        STG_CK(cudaFuncSetAttribute(k_sweep_lap<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_l));
+        STG_CK(cudaFuncSetAttribute(k_sweep_lap<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_l));
         attr_set = true;
     }
     // planes per block: long marches on big grids (prologue amortised), short ones on the
@@ -356,11 +656,11 @@ int sweep32(cudaStream_t st, const Geom& g, float vol, const float4* r, const fl
     const int chunk = g.n >= 192 ? 32 : g.n >= 96 ? 16 : g.n >= 48 ? 8 : g.n >= 24 ? 4 : 2;
     dim3 grid((g.n + SK) / SK, (g.n + SJ) / SJ, (g.n + chunk) / chunk), block(SK, SJ);
     if (xin && lap)
-        k_sweep<true, true><<<grid, block, smem, st>>>(g, vol, r, xin, xout, m, P, flag, chunk);
+        k_sweep_lap<true><<<grid, block, smem_l, st>>>(g, vol, r, xin, xout, m, P, flag, chunk);
     else if (xin)
         k_sweep<true, false><<<grid, block, smem, st>>>(g, vol, r, xin, xout, m, P, flag, chunk);
     else if (lap)
-        k_sweep<false, true><<<grid, block, smem, st>>>(g, vol, r, xin, xout, m, P, flag, chunk);
+        k_sweep_lap<false><<<grid, block, smem_l, st>>>(g, vol, r, xin, xout, m, P, flag, chunk);
     else
         k_sweep<false, false><<<grid, block, smem, st>>>(g, vol, r, xin, xout, m, P, flag, chunk);
     STG_LAUNCH_CK();

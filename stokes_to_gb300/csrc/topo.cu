@@ -68,7 +68,20 @@ __global__ void k_sensitivity(Geom g, const double* __restrict__ rho, stg_alpha 
 // kernels, so W_i and the sums are identical wherever they are formed.
 __device__ __forceinline__ double hat_w(double rmin, int a, int b, int c) { return rmin - sqrt((double)(a * a + b * b + c * c)); }
 
-__global__ void k_filter_wsum(int n, int nz, double rmin, int R, int Rz, double* __restrict__ W) {
+// the weights rmin - |o| of every offset o, computed once on the host (IEEE sqrt, so the
+// same values as hat_w); used when the stencil fits (radius R <= 3)
+constexpr int WTAB_MAX = 343;
+struct WTab {
+    double w[WTAB_MAX];
+};
+template <bool TAB>
+__device__ __forceinline__ double weight(const WTab& T, double rmin, int R, int Rz, int a, int b, int c) {
+    if (TAB) return T.w[((a + R) * (2 * R + 1) + (b + R)) * (2 * Rz + 1) + (c + Rz)];
+    return hat_w(rmin, a, b, c);
+}
+
+template <bool TAB>
+__global__ void k_filter_wsum(int n, int nz, double rmin, int R, int Rz, WTab T, double* __restrict__ W) {
     long long t = (long long)blockIdx.x * TPB + threadIdx.x;
     if (t >= (long long)n * n * nz) return;
     int k = (int)(t % nz), j = (int)((t / nz) % n), i = (int)(t / ((long long)n * nz));
@@ -78,14 +91,15 @@ __global__ void k_filter_wsum(int n, int nz, double rmin, int R, int Rz, double*
             for (int c = -Rz; c <= Rz; c++) {
                 int ii = i + a, jj = j + b, kk = k + c;
                 if (ii < 0 || jj < 0 || kk < 0 || ii >= n || jj >= n || kk >= nz) continue;
-                double w = hat_w(rmin, a, b, c);
+                double w = weight<TAB>(T, rmin, R, Rz, a, b, c);
                 if (w > 0) s += w;
             }
     W[t] = s;
 }
 
-__global__ void k_filter(int n, int nz, double rmin, int R, int Rz, const double* __restrict__ in, const double* __restrict__ W,
-                         double* __restrict__ out, int transpose) {
+template <bool TAB>
+__global__ void k_filter(int n, int nz, double rmin, int R, int Rz, WTab T, const double* __restrict__ in,
+                         const double* __restrict__ W, double* __restrict__ out, int transpose) {
     long long t = (long long)blockIdx.x * TPB + threadIdx.x;
     if (t >= (long long)n * n * nz) return;
     int k = (int)(t % nz), j = (int)((t / nz) % n), i = (int)(t / ((long long)n * nz));
@@ -95,7 +109,7 @@ __global__ void k_filter(int n, int nz, double rmin, int R, int Rz, const double
             for (int c = -Rz; c <= Rz; c++) {
                 int ii = i + a, jj = j + b, kk = k + c;
                 if (ii < 0 || jj < 0 || kk < 0 || ii >= n || jj >= n || kk >= nz) continue;
-                double w = hat_w(rmin, a, b, c);
+                double w = weight<TAB>(T, rmin, R, Rz, a, b, c);
                 if (w <= 0) continue;
                 const long long q = ((long long)ii * n + jj) * nz + kk;
                 if (transpose)
@@ -183,9 +197,23 @@ int density_filter(cudaStream_t st, int dim, int n, double rmin, const double* i
     if (R < 0) R = 0;
     const int nz = dim == 3 ? n : 1, Rz = dim == 3 ? R : 0;
     long long nc = (long long)n * n * nz;
-    k_filter_wsum<<<grid_for(nc, TPB), TPB, 0, st>>>(n, nz, rmin, R, Rz, W);
+    WTab T{};
+    const int nt = (2 * R + 1) * (2 * R + 1) * (2 * Rz + 1);
+    const bool tab = nt <= WTAB_MAX;
+    if (tab)
+        for (int a = -R; a <= R; a++)
+            for (int b = -R; b <= R; b++)
+                for (int c = -Rz; c <= Rz; c++)
+                    T.w[((a + R) * (2 * R + 1) + (b + R)) * (2 * Rz + 1) + (c + Rz)] = rmin - sqrt((double)(a * a + b * b + c * c));
+    if (tab)
+        k_filter_wsum<true><<<grid_for(nc, TPB), TPB, 0, st>>>(n, nz, rmin, R, Rz, T, W);
+    else
+        k_filter_wsum<false><<<grid_for(nc, TPB), TPB, 0, st>>>(n, nz, rmin, R, Rz, T, W);
     STG_LAUNCH_CK();
-    k_filter<<<grid_for(nc, TPB), TPB, 0, st>>>(n, nz, rmin, R, Rz, in, W, out, transpose);
+    if (tab)
+        k_filter<true><<<grid_for(nc, TPB), TPB, 0, st>>>(n, nz, rmin, R, Rz, T, in, W, out, transpose);
+    else
+        k_filter<false><<<grid_for(nc, TPB), TPB, 0, st>>>(n, nz, rmin, R, Rz, T, in, W, out, transpose);
     STG_LAUNCH_CK();
     return STG_OK;
 }

@@ -9,9 +9,14 @@
 // Tests: 0 = the reference's test 0 (2D: one inlet, 16 outlets; 3D: the 64^3 patch case),
 // 1 = parabolic inlet on a centred N/4 segment / patch with a mirrored outlet,
 // 2 = the reference default (no boundary data; the solve returns zero).
-// The design update is the optimality-criteria step with a linear hat filter (the
-// reference runs MMA, simplex/src/optimization/OptimizerMma.h:96-128); extra flags:
-//   -rmin r     filter radius in cells (default 1.5; r <= 1 leaves the design unfiltered)
+// The loop follows OptimizerMMA::Optimize_MMA (simplex/src/optimization/OptimizerMma.h:96-128):
+// iteration k evaluates the objective and its gradient at design k, writes frame k, then
+// updates the design; MMA stops once the largest change is <= 1e-3 or after -lf iterations.
+// Extra flags:
+//   -opt mma|oc the reference's MMA (default for test 0: reference law, no filter) or an
+//               optimality-criteria step with a hat filter (default otherwise)
+//   -rmin r     filter radius in cells (default 1.5 with oc, none with mma; r <= 1 leaves
+//               the design unfiltered)
 //   -law ref|bp Brinkman law: the reference's alpha on rho^3 (FluidTopoOpt3D.cpp:110-123,
 //               default for test 0) or amax 0.1 (1 - rho)/(0.1 + rho) (default otherwise)
 //   -amax a     BP law maximum (1e4);  -move m  OC move limit (0.2)
@@ -19,12 +24,12 @@
 //   -method plain|mixed   solver precision form (plain)
 //   -init uniform|noise   initial design: frac everywhere, or seeded smoothed noise
 //   -seed s -sigma g      noise seed and Gaussian width in cells (1, 4)
-//   -frames k   write a frame every k iterations (0: the first and the last only)
+//   -frames k   write a frame every k iterations (default 1, as the reference; 0: none)
 //   -dump_boundary dir   write the boundary arrays of the test to dir and exit (no GPU)
 // Output in -o: log.csv (iteration, objective, volume, change, V-cycles, solve times)
-// and frames in the reference drivers' layout and binary format (frame 0 = the initial
-// design; frame f = the design after iteration f with the velocity of its forward
-// solve): f/x, f/velocity, f/psi_D, f/psi_N, 0/grid, 0/last_frame.txt.
+// and frames in the reference drivers' layout and binary format (frame k = design k
+// with the velocity of its forward solve): k/x, k/velocity, k/psi_D, k/psi_N, 0/grid,
+// 0/last_frame.txt.
 #include <sys/stat.h>
 
 #include <chrono>
@@ -59,7 +64,7 @@ struct Args {
 Args parse(int argc, char** argv) {
     static const char* known[] = {"-o",   "-s",    "-test", "-driver", "-lf",  "-frac",   "-rmin",  "-law",   "-amax",
                                   "-move", "-tol", "-method", "-init", "-seed", "-sigma", "-frames", "-verbose",
-                                  "-dump_boundary"};
+                                  "-dump_boundary", "-opt"};
     Args a;
     for (int i = 1; i < argc; i++) {
         std::string k = argv[i];
@@ -99,12 +104,14 @@ int run(const Args& a) {
     const int iters = a.geti("-lf", 200);
     const double frac = a.getd("-frac", -1.0);
     if (!(frac > 0.0 && frac <= 1.0)) throw stg::Error(STG_E_INVALID, "-frac must be given in (0, 1]");
-    double rmin = a.getd("-rmin", 1.5);
+    const std::string opt = a.get("-opt", test == 0 ? "mma" : "oc");
+    if (opt != "mma" && opt != "oc") throw stg::Error(STG_E_INVALID, "-opt must be mma or oc");
+    double rmin = a.getd("-rmin", opt == "oc" ? 1.5 : 0.0);
     if (rmin <= 1.0) rmin = 0.5;  // radius below one cell: the hat filter is the identity
     const std::string law_s = a.get("-law", test == 0 ? "ref" : "bp");
     const double move = a.getd("-move", 0.2);
     const std::string out = a.get("-o", "output");
-    const int frames = a.geti("-frames", 0);
+    const int frames = a.geti("-frames", 1);
 
     stg_opts opts;
     stg_default_opts(&opts);
@@ -164,17 +171,11 @@ int run(const Args& a) {
     std::ofstream log(out + "/log.csv");
     log.precision(17);
     log << "iteration,objective,volume,change,v_cycles_forward,v_cycles_adjoint,solve_ms,iteration_ms\n";
-    std::printf("fluid_topo %dD N=%d test %d: %s law, rmin %.2f, frac %.3f, %d iterations, tol %.1e, %s\n", d, n, test,
-                law_s.c_str(), rmin, frac, iters, opts.tol, stg_version());
-
-    auto write_frame = [&](int f) {
-        if (f > 0) fluid.download();
-        stg::frames::write_frame<d>(out, f, b, x, fluid.vel, make_dir);
-    };
-    write_frame(0);
+    std::printf("fluid_topo %dD N=%d test %d: %s, %s law, rmin %.2f, frac %.3f, %d iterations, tol %.1e, %s\n", d, n, test,
+                opt.c_str(), law_s.c_str(), rmin, frac, iters, opts.tol, stg_version());
 
     double J = 0;
-    for (int it = 1; it <= iters; it++) {
+    for (int it = 0; it < iters; it++) {
         const double t0 = now_ms();
         x_old = x;
         // physical density = H x (FluidTopoOpt3D::Update_Fluid with the filter in front)
@@ -188,8 +189,15 @@ int run(const Args& a) {
         stg_stats as{};
         stg::check(stg_adjoint_sensitivity(h, &law, nullptr, &as), true);
         stg::check(stg_filter(h, rmin, nullptr, nullptr, 1));
-        double lam = 0;
-        stg::check(stg_oc_update(h, rmin, x.data(), nullptr, frac, move, 0.0, 1.0, x.data(), &lam));
+        if (frames > 0 && it % frames == 0) {
+            fluid.download();
+            stg::frames::write_frame<d>(out, it, b, x, fluid.vel, make_dir);
+        }
+        double lam = 0, mma_change = 0;
+        if (opt == "oc")
+            stg::check(stg_oc_update(h, rmin, x.data(), nullptr, frac, move, 0.0, 1.0, x.data(), &lam));
+        else  // the reference optimizer: coef 1e4, bounds [0.01, 1], move 0.2 (FluidTopoOpt3D::Init_MMA)
+            stg::check(stg_mma_update(h, x.data(), nullptr, frac, 1e4, 0.01, 1.0, move, x.data(), &mma_change));
         double vol = 0, change = 0;
         for (size_t q = 0; q < nc; q++) {
             vol += x[q];
@@ -201,7 +209,7 @@ int run(const Args& a) {
             << "," << tms << "\n";
         std::printf("iter %4d  J %.6e  vol %.4f  change %.3e  V-cycles %d+%d  %.1f ms\n", it, J, vol, change, vf,
                     as.inner_iters, tms);
-        if ((frames > 0 && it % frames == 0) || it == iters) write_frame(it);
+        if (opt == "mma" && change <= 1e-3) break;  // Optimize_MMA's stopping test (tol 1e-3)
     }
     std::printf("final objective %.8e\n", J);
     return 0;

@@ -119,7 +119,7 @@ def oracle_regression_2d():
                         vcycle_b=o.vcycle(bb), solution=sol, rel_true=st["rel_true"])
 
 
-def mma_problem(n=2000, iters=6, seed=0):
+def mma_problem(n=4096, iters=6, seed=0):
     """Seeded inputs of the MMA fixture: per update a negative sensitivity, the volume
     constraint g = 1e4 (mean x - 0.3) with gradient 1e4 / n, and bounds
     [max(0.01, x - 0.2), min(1, x + 0.2)] (simplex/src/optimization/OptimizerMma.h:96-128)."""
@@ -141,7 +141,7 @@ def mma_run(solver, n, dfs, frac=0.3):
 def ref_mma():
     from oracle import pyoracle as po
 
-    n = 2000
+    n = 4096  # the cells of a 64^2 (or 16^3) design
     dfs = mma_problem(n)
     xs = mma_run(po.RefMma(n), n, dfs)
     np.savez_compressed(os.path.join(HERE, "ref_mma.npz"), dfdx=np.array(dfs), x=xs)

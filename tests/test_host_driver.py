@@ -74,44 +74,81 @@ def test_driver_fails_loudly_without_gpu(driver, tmp_path):
     assert r.returncode == 2 and "stokes_gb300" in r.stderr
 
 
-@pytest.mark.gpu
-def test_driver_2d_optimization_matches_oracle(oracle, driver, tmp_path):
-    """fluid_topo -driver 0 -test 1 -s 64 -frac 0.3: uniform 0.3 start, BP law, filter
-    1.5, OC move 0.2, solves to 1e-10; objective history and final design against the
-    oracle's loop."""
-    n, iters, frac, rmin = 64, 4, 0.3, 1.5
-    out = tmp_path / "run"
-    subprocess.run([driver, "-driver", "0", "-test", "1", "-s", str(n), "-frac", str(frac), "-lf", str(iters), "-o",
-                    str(out)], check=True)
-    log = np.genfromtxt(out / "log.csv", delimiter=",", names=True)
-    x_gpu = read_field(out / str(iters) / "x", n, 2)
-    # reference frame layout: grid at frame 0, last_frame.txt, velocity as cell vectors,
-    # psi_N holding the 4N fixed boundary faces
-    assert np.array_equal(read_field(out / "0" / "x", n, 2), np.full((n, n), frac))
-    assert (out / "0" / "grid").stat().st_size == 3 * 4 + 8 + 3 * 8
-    assert (out / "0" / "last_frame.txt").read_text().strip() == str(iters)
-    assert (out / str(iters) / "velocity").stat().st_size == 3 * 4 + n * n * 3 * 8
-    assert int(np.fromfile(out / str(iters) / "psi_N", dtype=np.int32, count=1)[0]) == 4 * n
-
-    b = oracle.bc_parabolic(n, 2, width=n // 4)
+def _oracle_loop(oracle, b, n, iters, frac, update, law, prm, rmin):
+    """The design loop on the oracle: per iteration the objective at design k, the
+    adjoint sensitivity, then the design update; returns objectives and designs."""
     x = np.full((n, n), frac)
-    vw = oracle.filt(np.ones((n, n)), rmin, transpose=True)
-    J = []
+    Js, xs = [], []
     for it in range(iters):
-        phys = oracle.filt(x, rmin)
-        fp = oracle.face_penalty(phys, 1, [1e4], dim=2)
+        xs.append(x.copy())
+        phys = oracle.filt(x, rmin) if rmin > 1 else x
+        fp = oracle.face_penalty(phys, law, prm, dim=2)
         o = oracle.Steady2D(n)
         o.init_boundary(b)
         o.update_penalty(np.zeros((n, n)), fp)
         o.update_b(b.cell_b, b.face_b)
         u_ref, _ = o.solve(max_iter=60, abs_thr=0.0, rel_thr=1e-13, norm_thr=0.0, restarts=4, true_tol=1e-11)
-        J.append(o.energy(u_ref))
+        Js.append(o.energy(u_ref))
         o.set_b_blocked(o.apply_E(u_ref))
         lam_ref, _ = o.solve(max_iter=60, abs_thr=0.0, rel_thr=1e-13, norm_thr=0.0, restarts=4, true_tol=1e-11)
         _, u = oracle.blocked_to_field2(n, u_ref)
         _, lam = oracle.blocked_to_field2(n, lam_ref)
-        dc = oracle.filt(oracle.sensitivity(phys, 1, [1e4], u, lam, dim=2), rmin, transpose=True)
-        x, _, _ = oracle.oc_update(x, dc, vw / n ** 2, vw, frac)
-        x = x.reshape(n, n)
+        sens = oracle.sensitivity(phys, law, prm, u, lam, dim=2)
+        dc = oracle.filt(sens, rmin, transpose=True) if rmin > 1 else sens
+        x = update(x, dc)
+    return np.array(Js), xs
+
+
+@pytest.mark.gpu
+def test_driver_2d_optimization_matches_oracle(oracle, driver, tmp_path):
+    """fluid_topo -driver 0 -test 1 -s 64 -frac 0.3 (OC): uniform 0.3 start, BP law,
+    filter 1.5, move 0.2, solves to 1e-10; objective history and designs against the
+    oracle's loop, plus the reference frame layout."""
+    n, iters, frac, rmin = 64, 4, 0.3, 1.5
+    out = tmp_path / "run"
+    subprocess.run([driver, "-driver", "0", "-test", "1", "-s", str(n), "-frac", str(frac), "-lf", str(iters), "-o",
+                    str(out)], check=True)
+    log = np.genfromtxt(out / "log.csv", delimiter=",", names=True)
+    b = oracle.bc_parabolic(n, 2, width=n // 4)
+    vw = oracle.filt(np.ones((n, n)), rmin, transpose=True)
+
+    def oc(x, dc):
+        return oracle.oc_update(x, dc, vw / n ** 2, vw, frac)[0].reshape(n, n)
+
+    J, xs = _oracle_loop(oracle, b, n, iters, frac, oc, 1, [1e4], rmin)
     assert np.allclose(log["objective"], J, rtol=1e-6, atol=0)
-    assert relerr(x_gpu, x) < 1e-5
+    for k in range(iters):
+        assert relerr(read_field(out / str(k) / "x", n, 2), xs[k]) < 1e-5, k
+    # reference frame layout: grid at frame 0, last_frame.txt, velocity as cell vectors,
+    # psi_N holding the 4N fixed boundary faces
+    assert (out / "0" / "grid").stat().st_size == 3 * 4 + 8 + 3 * 8
+    assert (out / "0" / "last_frame.txt").read_text().strip() == str(iters - 1)
+    assert (out / "1" / "velocity").stat().st_size == 3 * 4 + n * n * 3 * 8
+    assert int(np.fromfile(out / "1" / "psi_N", dtype=np.int32, count=1)[0]) == 4 * n
+
+
+@pytest.mark.gpu
+def test_driver_2d_reference_test0_mma_matches_oracle(oracle, driver, tmp_path):
+    """fluid_topo -driver 0 -test 0 -s 64 -frac 0.3: the reference's own configuration
+    (test 0 boundary, reference alpha law on rho^3, unfiltered design, MMA with the
+    reference settings) against the oracle's loop with the oracle MMA (which is pinned to
+    the reference MMA solver)."""
+    n, iters, frac = 64, 3, 0.3
+    out = tmp_path / "run"
+    subprocess.run([driver, "-driver", "0", "-test", "0", "-s", str(n), "-frac", str(frac), "-lf", str(iters), "-o",
+                    str(out)], check=True)
+    log = np.genfromtxt(out / "log.csv", delimiter=",", names=True)
+    b = oracle.bc_test0_2d(n)
+    prm = [5e2 / (n / 32.0), 1e-3, 0.014]
+    mma = oracle.Mma(n * n)
+
+    def mma_step(x, dc):
+        x = np.ascontiguousarray(x, dtype=np.float64).ravel().copy()
+        g = 1e4 * (x.mean() - frac)
+        mma.update(x, dc, g, np.full(x.size, 1e4 / x.size), np.maximum(0.01, x - 0.2), np.minimum(1.0, x + 0.2))
+        return x.reshape(n, n)
+
+    J, xs = _oracle_loop(oracle, b, n, iters, frac, mma_step, 0, prm, 0.0)
+    assert np.allclose(log["objective"], J, rtol=1e-6, atol=0)
+    for k in range(iters):
+        assert relerr(read_field(out / str(k) / "x", n, 2), xs[k]) < 1e-6, k
