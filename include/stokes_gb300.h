@@ -49,6 +49,13 @@ typedef struct stg_opts {
     int inner_max;       /* FGMRES basis size of one refinement step */
     double inner_tol;    /* relative reduction asked of one refinement step */
     int verbose;         /* print per-iteration residuals to stderr */
+    int smooth_sweeps;   /* sweeps per colour in the solver's smoother: 2 = the reference's
+                            DescentSmoother (default); 1 halves the smoothing work. The
+                            LinearMapping adapters always run the reference smoother. */
+    int warm_start;      /* 1: start each solve from the previous solution of the same
+                            equation (the forward one for stg_solve, the adjoint one for
+                            stg_adjoint_sensitivity) instead of zero; 0 (default): zero, as
+                            the reference */
 } stg_opts;
 
 typedef struct stg_stats {
@@ -76,7 +83,7 @@ int stg_profile(stg_t* h, int enable); /* enabling also clears the counters */
 int stg_profile_read(stg_t* h, int cls, int64_t* launches, double* ms, double* bytes);
 const char* stg_profile_name(int cls);
 
-/* Fills *o with the defaults (PLAIN, tol 1e-8, 20 outer, 30 inner, 1e-4). */
+/* Fills *o with the defaults (PLAIN, tol 1e-8, 20 outer, 30 inner, 1e-4, 2 sweeps). */
 void stg_default_opts(stg_opts* o);
 
 /* Message of the last failure on this thread ("" if none). */

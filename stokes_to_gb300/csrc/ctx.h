@@ -57,7 +57,9 @@ struct stg_ctx {
     bool closed = true, have_boundary = false, have_penalty = false, have_rhs = false, updated = false, have_solution = false;
     // lap_ok: the boundary admits the Laplacian form; general: force the masked general
     // stencil (set while an adapter works on a vector that is nonzero on fixed unknowns)
-    bool lap_ok = false, general = false;
+    bool lap_ok = false, general = false, reference_cycle = false;
+    bool x0_valid[2] = {false, false};  // x64 / lam64 hold a previous solution (warm start)
+    bool has_x0(const stg::d4* x) const { return (x == x64 && x0_valid[0]) || (x == lam64 && x0_valid[1]); }
     int* dflag = nullptr;
     // fine-level FP64
     stg::d4 *b64 = nullptr, *x64 = nullptr, *r64 = nullptr, *t64 = nullptr, *lam64 = nullptr;

@@ -420,8 +420,8 @@ __global__ void k_patch_fixed(Geom g, const d4* __restrict__ b, const uint8_t* _
     int s = g.slot(i, j, k);
     uint8_t mm = __ldg(m + s);
     if (!mm) return;
-    double bp, bu, bv, bw, p, u, v, w;
-    load4(b, s, bp, bu, bv, bw);
+    double bp = 0, bu = 0, bv = 0, bw = 0, p, u, v, w;
+    if (b) load4(b, s, bp, bu, bv, bw);
     load4(x, s, p, u, v, w);
     store4(x, s, (mm & MP) ? bp : p, (mm & MU) ? bu : u, (mm & MV) ? bv : v, (mm & MW) ? bw : w);
 }
@@ -438,6 +438,12 @@ int vol_slots(cudaStream_t st, const Geom& g, const uint8_t* m, double cell_vol,
 int fixed_nonzero(cudaStream_t st, const Geom& g, const d4* x, const uint8_t* m, int* flag) {
     STG_CK(cudaMemsetAsync(flag, 0, sizeof(int), st));
     k_fixed_nonzero<<<grid_for(g.box(), TPB), TPB, 0, st>>>(g, x, m, flag);
+    STG_LAUNCH_CK();
+    return STG_OK;
+}
+
+int zero_fixed(cudaStream_t st, const Geom& g, const uint8_t* m, d4* x) {
+    k_patch_fixed<<<grid_for(g.box(), TPB), TPB, 0, st>>>(g, nullptr, m, x);
     STG_LAUNCH_CK();
     return STG_OK;
 }

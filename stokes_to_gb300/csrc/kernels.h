@@ -31,6 +31,8 @@ int restrict_resid32(cudaStream_t st, const Geom& gc, const Geom& gf, float volf
                      const uint8_t* mf, const float4* Pf, const uint8_t* mc, float4* rc, bool lap = false);
 // 1 in *flag (device) when x is nonzero on some fixed or absent unknown of the box, else 0
 int fixed_nonzero(cudaStream_t st, const Geom& g, const d4* x, const uint8_t* m, int* flag);
+// x_f = 0 on every fixed or absent unknown of the box
+int zero_fixed(cudaStream_t st, const Geom& g, const uint8_t* m, d4* x);
 // x_f = b_f on every fixed unknown of the box (the fixed rows of A are the identity)
 int patch_fixed(cudaStream_t st, const Geom& g, const d4* b, const uint8_t* m, d4* x);
 // xf += fix_f (injection of xc)

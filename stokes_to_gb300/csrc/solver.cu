@@ -180,9 +180,13 @@ int sweep(stg_t* h, Level& L, const float4* r, int flag, bool first) {
 }
 
 int smooth(stg_t* h, Level& L, const float4* r, bool post, bool x_is_zero) {
-    const int flags_pre[4] = {0, 0, 1, 1}, flags_post[4] = {1, 1, 0, 0};
-    const int* f = post ? flags_post : flags_pre;
-    for (int s = 0; s < 4; s++) STG_TRY(sweep(h, L, r, f[s], s == 0 && x_is_zero));
+    // sweeps per colour: the reference's 2, or the solver option (adapters keep the reference)
+    const int per = h->reference_cycle ? 2 : std::max(1, std::min(4, h->opts.smooth_sweeps));
+    int s = 0;
+    for (int c = 0; c < 2; c++) {
+        const int flag = post ? 1 - c : c;
+        for (int q = 0; q < per; q++, s++) STG_TRY(sweep(h, L, r, flag, s == 0 && x_is_zero));
+    }
     return STG_OK;
 }
 
@@ -266,7 +270,12 @@ int solve_core(stg_t* h, const d4* b, d4* x, stg_stats* stats) {
         S.setup_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     }
     STG_CK(cudaEventRecord(h->e0, h->st));
-    STG_CK(cudaMemsetAsync(x, 0, sizeof(d4) * n4, h->st));
+    // zero initial guess as the reference, or the previous solution of this equation
+    if (h->opts.warm_start && h->has_x0(x)) {
+        if (h->dim == 3 && fast(h, fine(h))) STG_TRY(zero_fixed(h->st, fine(h).g, fine(h).m, x));
+    } else {
+        STG_CK(cudaMemsetAsync(x, 0, sizeof(d4) * n4, h->st));
+    }
     double bn2 = 0;
     STG_TRY(dot64(h->st, n4, b, b, h->dnrm, h->dscr));
     STG_CK(cudaMemcpyAsync(&bn2, h->dnrm, sizeof(double), cudaMemcpyDeviceToHost, h->st));
@@ -395,11 +404,15 @@ int solve_core(stg_t* h, const d4* b, d4* x, stg_stats* stats) {
 // that has nonzero fixed entries runs the general stencil for this call.
 struct PathGuard {
     stg_t* h;
-    ~PathGuard() { h->general = false; }
+    ~PathGuard() {
+        h->general = false;
+        h->reference_cycle = false;
+    }
 };
 
 int choose_path(stg_t* h, const Level& L, const d4* x) {
     h->general = false;
+    h->reference_cycle = true;  // adapters reproduce the reference's V-cycle and smoother
     if (!L.lap) return STG_OK;
     int nz = 0;
     STG_TRY(fixed_nonzero(h->st, L.g, x, L.m, h->dflag));
@@ -436,6 +449,8 @@ void stg_default_opts(stg_opts* o) {
     o->inner_max = 30;
     o->inner_tol = 1e-4;
     o->verbose = 0;
+    o->smooth_sweeps = 2;
+    o->warm_start = 0;
 }
 
 const char* stg_last_error(void) { return g_err; }
@@ -517,6 +532,7 @@ int stg_create(int dim, int n, const stg_opts* opts, stg_t** out) {
     else
         stg_default_opts(&h->opts);
     if (h->opts.inner_max < 1) h->opts.inner_max = 1;
+    if (h->opts.smooth_sweeps < 1) h->opts.smooth_sweeps = 2;  // unset: the reference smoother
     h->m = h->opts.inner_max;
     h->L = dim == 3 ? level_count(n) : 0;
     int rc = STG_OK;
@@ -762,6 +778,7 @@ int stg_solve(stg_t* h, double* p_out, double* const* vel_out, stg_stats* stats)
     int rc = solve_core(h, h->b64, h->x64, stats);
     if (rc != STG_OK && rc != STG_E_NOT_CONVERGED) return rc;
     h->have_solution = true;
+    h->x0_valid[0] = true;
     if (p_out || vel_out) STG_TRY(download_fields(h, h->x64, p_out, vel_out));
     return rc;
 }
@@ -856,6 +873,7 @@ int stg_adjoint_sensitivity(stg_t* h, const stg_alpha* law, double* dJ, stg_stat
     int nb = 0;
     STG_TRY(energy_op(h, h->x64, h->t64, nullptr, &nb));
     int rc = solve_core(h, h->t64, h->lam64, stats);
+    if (rc == STG_OK || rc == STG_E_NOT_CONVERGED) h->x0_valid[1] = true;
     if (rc != STG_OK && rc != STG_E_NOT_CONVERGED) return rc;
     if (h->dim == 2)
         STG_TRY(sensitivity2d(h, h->phys_used, *law, h->x64, h->lam64, h->d_sens));

@@ -22,6 +22,8 @@
 //   -amax a     BP law maximum (1e4);  -move m  OC move limit (0.2)
 //   -tol t      FP64 relative residual of every solve (1e-8 in 3D, 1e-10 in 2D)
 //   -method plain|mixed   solver precision form (plain)
+//   -warm 0|1   start each forward / adjoint solve from the previous one (default 1; the
+//               reference starts from zero, which -warm 0 reproduces)
 //   -init uniform|noise   initial design: frac everywhere, or seeded smoothed noise
 //   -seed s -sigma g      noise seed and Gaussian width in cells (1, 4)
 //   -frames k   write a frame every k iterations (default 1, as the reference; 0: none)
@@ -64,7 +66,7 @@ struct Args {
 Args parse(int argc, char** argv) {
     static const char* known[] = {"-o",   "-s",    "-test", "-driver", "-lf",  "-frac",   "-rmin",  "-law",   "-amax",
                                   "-move", "-tol", "-method", "-init", "-seed", "-sigma", "-frames", "-verbose",
-                                  "-dump_boundary", "-opt"};
+                                  "-dump_boundary", "-opt", "-warm"};
     Args a;
     for (int i = 1; i < argc; i++) {
         std::string k = argv[i];
@@ -118,6 +120,7 @@ int run(const Args& a) {
     opts.tol = a.getd("-tol", d == 3 ? 1e-8 : 1e-10);
     opts.method = a.get("-method", "plain") == "mixed" ? STG_METHOD_MIXED : STG_METHOD_PLAIN;
     opts.verbose = a.geti("-verbose", 0);
+    opts.warm_start = a.geti("-warm", 1);
 
     stg_alpha law{};
     if (law_s == "ref") {
