@@ -41,6 +41,9 @@ typedef struct stg_ctx stg_t;
 /* Solver method of stg_solve. */
 #define STG_METHOD_PLAIN 0 /* FP32 V-cycle preconditioned FGMRES inside FP64 refinement */
 #define STG_METHOD_MIXED 1 /* as PLAIN with BF16-stored coarse-level corrections */
+#define STG_METHOD_LEARNED 2 /* as PLAIN with the learned correction of stg_net_* added to every
+                                V-cycle; falls back to PLAIN for the rest of a solve when a
+                                Krylov step reduces the residual estimate by less than 20% */
 
 typedef struct stg_opts {
     int method;          /* STG_METHOD_* */
@@ -49,9 +52,11 @@ typedef struct stg_opts {
     int inner_max;       /* FGMRES basis size of one refinement step */
     double inner_tol;    /* relative reduction asked of one refinement step */
     int verbose;         /* print per-iteration residuals to stderr */
-    int smooth_sweeps;   /* sweeps per colour in the solver's smoother: 2 = the reference's
-                            DescentSmoother (default); 1 halves the smoothing work. The
-                            LinearMapping adapters always run the reference smoother. */
+    int smooth_sweeps;   /* sweeps per colour in the solver's smoother: 1 (default; 0 means
+                            1) or 2, the reference's DescentSmoother. At 256^3 one sweep per
+                            colour reaches the same FP64 tolerance in as many V-cycles at
+                            2/3 of the time. The LinearMapping adapters always run the
+                            reference smoother. */
     int warm_start;      /* 1: start each solve from the previous solution of the same
                             equation (the forward one for stg_solve, the adjoint one for
                             stg_adjoint_sensitivity) instead of zero; 0 (default): zero, as
@@ -66,6 +71,8 @@ typedef struct stg_stats {
     double setup_ms;     /* hierarchy + coarsest-inverse set-up time */
     double solve_ms;     /* device time of the Krylov solve */
     int status;          /* 0 converged, STG_E_* otherwise */
+    int learned_iters;   /* FGMRES iterations whose preconditioner added the learned correction */
+    int fallbacks;       /* refinement steps that fell back from LEARNED to PLAIN after a stall */
 } stg_stats;
 
 /* Runs the handle's work on a caller-owned CUDA stream (a cudaStream_t passed as void*);
@@ -76,8 +83,9 @@ int stg_set_stream(stg_t* h, void* cuda_stream);
 /* Kernel accounting: total kernels this library has launched in the process, and
  * per-kernel-class CUDA-event timing on the handle's stream (off by default). Classes:
  * 0 resid32, 1 sweep32 (finest level), 2 restrict32, 3 prolong32, 4 apply32, 5 resid64,
- * 6 krylov, 7 coarse, 8 setup, 9 other, 10 sweep32_coarse (coarser levels). */
-#define STG_PROF_NCLASS 11
+ * 6 krylov, 7 coarse, 8 setup, 9 other, 10 sweep32_coarse (coarser levels), 11 net
+ * (the learned correction's network). */
+#define STG_PROF_NCLASS 12
 int64_t stg_kernel_launches(void);
 int stg_profile(stg_t* h, int enable); /* enabling also clears the counters */
 int stg_profile_read(stg_t* h, int cls, int64_t* launches, double* ms, double* bytes);
@@ -105,6 +113,8 @@ int stg_create(int dim, int n, const stg_opts* opts, stg_t** out);
 int stg_destroy(stg_t* h);
 
 /* Number of levels and cells per axis of a level (level 0 = coarsest, as the reference). */
+/* Switches the solver method of a handle (STG_METHOD_*; LEARNED needs dim 3). */
+int stg_set_method(stg_t* h, int method);
 int stg_levels(const stg_t* h);
 int stg_level_n(const stg_t* h, int level);
 /* LinearMapping::xDoF()/yDoF() of the reference operator at a level (blocked layout size). */
@@ -261,6 +271,35 @@ int stg_apply_op_device(stg_t* h, int op, int level, double* d_out, const double
 /* Coarse descriptor of a level after stg_update (StokeFlowDescriptor3D d_vol,
  * d_penalty, d_fixed; stoke/StokeFlowDescriptor3D.h:5-30), blocked layout, device pointers. */
 int stg_level_descr_device(stg_t* h, int level, double* d_vol, double* d_penalty, uint8_t* d_fixed);
+
+/* ----------------------------------------------------------------------------
+ * Learned preconditioner (not part of the reference): a 3-level 3D U-Net (16/32/64
+ * channels, 3x3x3 convolutions, BF16 weights and activations, FP32 accumulation on the
+ * tensor cores) that maps (density, face penalties, residual after a V-cycle) to a
+ * correction. STG_METHOD_LEARNED uses it inside FGMRES as z = M(v) + NN(v - A M(v)).
+ * Parameters are one FP32 vector: per convolution l = 0..9 the weights [27][C_out][C_in]
+ * (tap 9 (di+1) + 3 (dj+1) + (dk+1)) then the biases [C_out]; the 1x1 head [4][16] and its
+ * biases [4]; last, the output scale kappa (set by the first training pair, not trained).
+ * -------------------------------------------------------------------------- */
+
+/* Creates the handle's network (or re-initialises it) with seeded He-uniform weights. */
+int stg_net_init(stg_t* h, uint64_t seed);
+int stg_net_num_params(const stg_t* h, int64_t* count);
+int stg_net_get_params(stg_t* h, float* out, int64_t count);
+/* Loads parameters and resets the Adam state. */
+int stg_net_set_params(stg_t* h, const float* in, int64_t count);
+/* One forward pass on host data of an n^3 grid (n >= 8, n % 4 == 0), independent of the
+ * handle's grid: in [n^3][8] channels (density, p, u, v, w, three penalty shares), cell
+ * v = (i n + j) n + k. out [n^3][4] (may be NULL). With target [n^3][4] non-NULL, also the
+ * mean-squared-error loss and its gradient with respect to every parameter (grad may be
+ * NULL), kept for stg_net_adam_step. */
+int stg_net_forward_backward(stg_t* h, int n, const float* in, const float* target, float* out, float* grad, double* loss);
+/* One Adam step (beta 0.9 / 0.999, eps 1e-8) with the last computed gradient. */
+int stg_net_adam_step(stg_t* h, double lr);
+/* Trains on the handle's current operator (3D; boundary and penalty or density set):
+ * each step draws a pair from seeded noise (e = M(noise), r = A e, z = M(r); input
+ * r1 = r - A z, target e - z), runs forward, backward and Adam. losses: steps entries or NULL. */
+int stg_net_train(stg_t* h, int steps, double lr, uint64_t seed, float* losses);
 
 /* ----------------------------------------------------------------------------
  * Input generators used by the benchmarks (not part of the reference).

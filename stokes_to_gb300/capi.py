@@ -21,6 +21,7 @@ STG_E_NONFINITE = -6
 
 STG_METHOD_PLAIN = 0
 STG_METHOD_MIXED = 1
+STG_METHOD_LEARNED = 2
 STG_ALPHA_REF = 0
 STG_ALPHA_BP = 1
 
@@ -40,8 +41,10 @@ EXPORTS = [
     "stg_apply_A_device", "stg_apply_E_device", "stg_update", "stg_vcycle_device", "stg_apply_op_device",
     "stg_level_descr_device", "stg_density_noise", "stg_set_stream", "stg_kernel_launches", "stg_profile",
     "stg_profile_read", "stg_profile_name", "stg_oc_update_noalloc", "stg_mma_update", "stg_mma_reset",
+    "stg_set_method", "stg_net_init", "stg_net_num_params", "stg_net_get_params", "stg_net_set_params",
+    "stg_net_forward_backward", "stg_net_adam_step", "stg_net_train",
 ]
-STG_PROF_NCLASS = 11
+STG_PROF_NCLASS = 12
 
 
 class Opts(ctypes.Structure):
@@ -53,7 +56,7 @@ class Opts(ctypes.Structure):
 class Stats(ctypes.Structure):
     _fields_ = [("outer_iters", ctypes.c_int), ("inner_iters", ctypes.c_int), ("rel_residual", ctypes.c_double),
                 ("abs_residual", ctypes.c_double), ("setup_ms", ctypes.c_double), ("solve_ms", ctypes.c_double),
-                ("status", ctypes.c_int)]
+                ("status", ctypes.c_int), ("learned_iters", ctypes.c_int), ("fallbacks", ctypes.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -126,6 +129,15 @@ def lib():
         L.stg_profile_name.restype = ctypes.c_char_p
         L.stg_profile_name.argtypes = [I]
         L.stg_oc_update_noalloc.argtypes = [I, D, P, P, D, D, D, D, P, DP, P]
+        FP = ctypes.POINTER(ctypes.c_float)
+        L.stg_set_method.argtypes = [P, I]
+        L.stg_net_init.argtypes = [P, ctypes.c_uint64]
+        L.stg_net_num_params.argtypes = [P, ctypes.POINTER(ctypes.c_int64)]
+        L.stg_net_get_params.argtypes = [P, FP, ctypes.c_int64]
+        L.stg_net_set_params.argtypes = [P, FP, ctypes.c_int64]
+        L.stg_net_forward_backward.argtypes = [P, I, FP, FP, FP, FP, DP]
+        L.stg_net_adam_step.argtypes = [P, D]
+        L.stg_net_train.argtypes = [P, I, D, ctypes.c_uint64, FP]
         _LIB = L
     return _LIB
 
@@ -138,6 +150,10 @@ def check(rc, allow=()):
 
 def dp(a):
     return None if a is None else a.ctypes.data_as(DP)
+
+
+def fp(a):
+    return None if a is None else a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
 
 
 def _c64(a):
@@ -301,6 +317,45 @@ class Solver:
         out = np.zeros((self.n,) * self.dim) if want else None
         check(self.L.stg_density_noise(self.h, seed, sigma, dp(out)))
         return out
+
+    def set_method(self, method):
+        return check(self.L.stg_set_method(self.h, method))
+
+    # ---- learned preconditioner
+    def net_init(self, seed=0):
+        return check(self.L.stg_net_init(self.h, seed))
+
+    def net_num_params(self):
+        c = ctypes.c_int64()
+        check(self.L.stg_net_num_params(self.h, ctypes.byref(c)))
+        return int(c.value)
+
+    def net_params(self):
+        out = np.zeros(self.net_num_params(), dtype=np.float32)
+        check(self.L.stg_net_get_params(self.h, fp(out), out.size))
+        return out
+
+    def net_set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        return check(self.L.stg_net_set_params(self.h, fp(p), p.size))
+
+    def net_forward_backward(self, n, inp, target=None):
+        """inp [n^3][8], target [n^3][4] or None -> (out, loss, grad)."""
+        inp = np.ascontiguousarray(inp, dtype=np.float32)
+        tgt = None if target is None else np.ascontiguousarray(target, dtype=np.float32)
+        out = np.zeros((n ** 3, 4), dtype=np.float32)
+        grad = np.zeros(self.net_num_params(), dtype=np.float32) if tgt is not None else None
+        loss = np.zeros(1)
+        check(self.L.stg_net_forward_backward(self.h, n, fp(inp), fp(tgt), fp(out), fp(grad), dp(loss)))
+        return out, (float(loss[0]) if tgt is not None else None), grad
+
+    def net_adam_step(self, lr):
+        return check(self.L.stg_net_adam_step(self.h, lr))
+
+    def net_train(self, steps, lr=1e-3, seed=0):
+        losses = np.zeros(max(steps, 1), dtype=np.float32)
+        check(self.L.stg_net_train(self.h, steps, lr, seed, fp(losses)))
+        return losses[:steps]
 
     # ---- device-pointer LinearMapping adapters (pointers are ints from torch.Tensor.data_ptr())
     def apply_A_device(self, level, out_ptr, in_ptr):

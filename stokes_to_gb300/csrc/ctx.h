@@ -86,6 +86,8 @@ struct stg_ctx {
     int (*finish)(stg_t*, const stg::d4* b, stg::d4* x) = nullptr;  // optional, after the refinement loop
     struct Ctx2* c2 = nullptr;        // 2D state (dim == 2)
     struct MmaState* mma = nullptr;   // MMA optimizer state (mma.cu), created on first use
+    struct NetState* net = nullptr;   // learned preconditioner (unet.cu), stg_net_init
+    bool net_on = false;              // LEARNED: the network is in use in the current refinement step
 };
 
 
@@ -114,6 +116,15 @@ int apply_E2d(stg_t* h, double* out, const double* in);
 int vcycle2d(stg_t* h, double* out, const double* in);
 int apply_op2d(stg_t* h, int op, int level, double* out, const double* in);
 int level_descr2d(stg_t* h, int level, double* vol, double* pen, uint8_t* fixed);
+
+Level& fine(stg_t* h);
+bool fast(const stg_t* h, const Level& L);
+// one V-cycle out = M(rhs) and y = A x on the finest level (FP32, solver.cu)
+int precond3(stg_t* h, const float4* rhs, float4* out);
+int apply3(stg_t* h, const float4* x, float4* y);
+// z += NN(r1): the learned correction (unet.cu); net_free releases the network
+int net_correct(stg_t* h, const float4* r1, float4* z);
+void net_free(stg_t* h);
 
 // MMA design update (mma.cu) on device cell arrays; d_xout may alias d_x
 int mma_update(stg_t* h, const double* d_x, const double* d_df, double frac, double coef, double lo, double hi, double movlim,

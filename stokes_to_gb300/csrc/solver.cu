@@ -246,6 +246,17 @@ int precond3(stg_t* h, const float4* rhs, float4* out) {
     return STG_OK;
 }
 
+// STG_METHOD_LEARNED: out = M(rhs) + NN(rhs - A M(rhs)) while the network is in use.
+// h->w is free here: the Arnoldi step overwrites it with A out next.
+int precond_learned(stg_t* h, const float4* rhs, float4* out) {
+    STG_TRY(precond3(h, rhs, out));
+    if (!h->net_on) return STG_OK;
+    Level& F = fine(h);
+    PROF(h, 4, 49.0 * F.g.box(), resid32(h->st, F.g, (float)F.vol, rhs, out, F.m, F.P32, h->w, fast(h, F)));
+    PROF(h, 11, 0.0, net_correct(h, h->w, out));
+    return STG_OK;
+}
+
 int apply3(stg_t* h, const float4* x, float4* y) {
     Level& F = fine(h);
     PROF(h, 4, 49.0 * F.g.box(), apply32(h->st, F.g, (float)F.vol, x, F.m, F.P32, y, fast(h, F)));
@@ -276,6 +287,11 @@ int solve_core(stg_t* h, const d4* b, d4* x, stg_stats* stats) {
     } else {
         STG_CK(cudaMemsetAsync(x, 0, sizeof(d4) * n4, h->st));
     }
+    if (h->opts.method == STG_METHOD_LEARNED && !h->net) {
+        set_error("STG_METHOD_LEARNED needs a network (stg_net_init, then stg_net_train or stg_net_set_params)");
+        return STG_E_INVALID;
+    }
+    h->net_on = h->opts.method == STG_METHOD_LEARNED;
     double bn2 = 0;
     STG_TRY(dot64(h->st, n4, b, b, h->dnrm, h->dscr));
     STG_CK(cudaMemcpyAsync(&bn2, h->dnrm, sizeof(double), cudaMemcpyDeviceToHost, h->st));
@@ -318,7 +334,9 @@ int solve_core(stg_t* h, const d4* b, d4* x, stg_stats* stats) {
         sig[0] = 1.0;
         const double one = 1.0;
         STG_CK(cudaMemcpyAsync(h->dsig2, &one, sizeof(double), cudaMemcpyHostToDevice, h->st));
+        double prev_est = beta;
         for (int j = 0; j < m; j++) {
+            if (h->net_on) S.learned_iters++;
             STG_TRY(h->precond(h, h->V[j], h->Z[j]));
             STG_TRY(h->apply32(h, h->Z[j], h->w));
             PROF(h, 6, 16.0 * (j + 2) * n4, multidot32(h->st, n4, h->V.data(), j + 1, h->w, h->dh, h->dscr, h->dnrm + 1));
@@ -372,6 +390,13 @@ int solve_core(stg_t* h, const d4* b, d4* x, stg_stats* stats) {
             k = j + 1;
             double est = std::fabs(g[j + 1]);
             if (h->opts.verbose > 1) fprintf(stderr, "[stg]   inner %d  est %.3e\n", j, est);
+            // a learned step that cut the estimate by less than 20% ends the network's use in
+            // this solve (FGMRES is flexible, so the basis built so far stays valid)
+            if (h->net_on && est > 0.8 * prev_est) {
+                h->net_on = false;
+                S.fallbacks++;
+            }
+            prev_est = est;
             if (est <= itol * beta || hn == 0.0) break;
         }
         if (status == STG_E_NONFINITE) break;
@@ -449,7 +474,7 @@ void stg_default_opts(stg_opts* o) {
     o->inner_max = 30;
     o->inner_tol = 1e-4;
     o->verbose = 0;
-    o->smooth_sweeps = 2;
+    o->smooth_sweeps = 1;
     o->warm_start = 0;
 }
 
@@ -492,7 +517,7 @@ int stg_profile_read(stg_t* h, int cls, int64_t* launches, double* ms, double* b
 
 const char* stg_profile_name(int cls) {
     static const char* names[STG_PROF_NCLASS] = {"resid32", "sweep32", "restrict32", "prolong32", "apply32", "resid64",
-                                                 "krylov",  "coarse",  "setup",      "other",     "sweep32_coarse"};
+                                                 "krylov",  "coarse",  "setup",      "other",     "sweep32_coarse", "net"};
     return (cls >= 0 && cls < STG_PROF_NCLASS) ? names[cls] : "";
 }
 
@@ -532,7 +557,7 @@ int stg_create(int dim, int n, const stg_opts* opts, stg_t** out) {
     else
         stg_default_opts(&h->opts);
     if (h->opts.inner_max < 1) h->opts.inner_max = 1;
-    if (h->opts.smooth_sweeps < 1) h->opts.smooth_sweeps = 2;  // unset: the reference smoother
+    if (h->opts.smooth_sweeps < 1) h->opts.smooth_sweeps = 1;  // unset: the default
     h->m = h->opts.inner_max;
     h->L = dim == 3 ? level_count(n) : 0;
     int rc = STG_OK;
@@ -562,13 +587,17 @@ int stg_create(int dim, int n, const stg_opts* opts, stg_t** out) {
         if ((rc = mask_from_field(h->st, L.g, nullptr, nullptr, nullptr, nullptr, L.m))) return fail(rc);
     }
     long long nparts = 0;
+    if (dim == 2 && h->opts.method == STG_METHOD_LEARNED) {
+        set_error("STG_METHOD_LEARNED: 3D handles only");
+        return fail(STG_E_INVALID);
+    }
     if (dim == 3) {
         if ((rc = dense_init(h->dense, h->lv[0].g))) return fail(rc);
         Level& F = fine(h);
         h->n4 = (long long)F.g.nslot;
         h->setup = update;
         h->resid64 = residual64;
-        h->precond = precond3;
+        h->precond = h->opts.method == STG_METHOD_LEARNED ? precond_learned : precond3;
         h->apply32 = apply3;
         h->finish = finish3;
         h->ncell = (size_t)n * n * n;
@@ -607,6 +636,7 @@ int stg_destroy(stg_t* h) {
     if (h->st) cudaStreamSynchronize(h->st);
     destroy2d(h);
     mma_free(h);
+    net_free(h);
     for (auto& L : h->lv) {
         cudaFree(L.m);
         cudaFree(L.P64);
@@ -634,6 +664,17 @@ int stg_destroy(stg_t* h) {
     for (auto e : h->prof.pool) cudaEventDestroy(e);
     if (h->own_st) cudaStreamDestroy(h->own_st);
     delete h;
+    return STG_OK;
+}
+
+int stg_set_method(stg_t* h, int method) {
+    STG_TRY(check_handle(h));
+    if (method < STG_METHOD_PLAIN || method > STG_METHOD_LEARNED || (method == STG_METHOD_LEARNED && h->dim != 3)) {
+        set_error("stg_set_method: method %d not available for dim %d", method, h->dim);
+        return STG_E_INVALID;
+    }
+    h->opts.method = method;
+    if (h->dim == 3) h->precond = method == STG_METHOD_LEARNED ? precond_learned : precond3;
     return STG_OK;
 }
 
