@@ -246,15 +246,28 @@ int precond3(stg_t* h, const float4* rhs, float4* out) {
     return STG_OK;
 }
 
-// STG_METHOD_LEARNED: out = M(rhs) + NN(rhs - A M(rhs)) while the network is in use.
-// h->w is free here: the Arnoldi step overwrites it with A out next.
+// STG_METHOD_LEARNED: out = S(M(rhs) + NN(rhs - A M(rhs))) while the network is in use,
+// S one post-smoothing pass of the finest level on A out = rhs (it removes the rough part
+// of the network's error, which A would amplify in the residual). h->w is free here: the
+// Arnoldi step overwrites it with A out next.
 int precond_learned(stg_t* h, const float4* rhs, float4* out) {
     STG_TRY(precond3(h, rhs, out));
     if (!h->net_on) return STG_OK;
     Level& F = fine(h);
     PROF(h, 4, 49.0 * F.g.box(), resid32(h->st, F.g, (float)F.vol, rhs, out, F.m, F.P32, h->w, fast(h, F)));
     PROF(h, 11, 0.0, net_correct(h, h->w, out));
-    return STG_OK;
+    // smooth in place: the level's ping-pong buffers point at out and h->w; an even
+    // number of sweeps leaves the result in out
+    float4 *ka = F.xa, *kb = F.xb;
+    const int kc = F.cur;
+    F.xa = out;
+    F.xb = h->w;
+    F.cur = 0;
+    const int rc = smooth(h, F, rhs, true, false);
+    F.xa = ka;
+    F.xb = kb;
+    F.cur = kc;
+    return rc;
 }
 
 int apply3(stg_t* h, const float4* x, float4* y) {

@@ -28,6 +28,18 @@ int conv3_forward(cudaStream_t st, const __nv_bfloat16* in, int cin, int ldin, c
 int conv3_backward_weights(cudaStream_t st, const __nv_bfloat16* x, int cin, int ldx, const __nv_bfloat16* dy, int cout, int lddy,
                            float* dw, float* db, int n);
 int conv3_flip_weights(cudaStream_t st, const __nv_bfloat16* w, int cout, int cin, __nv_bfloat16* wf);
+int conv3_tc_status(cudaStream_t st, int* timed_out);
+
+// error when a tensor-core convolution gave up waiting for its MMAs (bounded waits)
+int tc_check(cudaStream_t st) {
+    int t = 0;
+    STG_TRY(conv3_tc_status(st, &t));
+    if (t) {
+        set_error("tensor-core convolution: MMA completion wait timed out");
+        return STG_E_CUDA;
+    }
+    return STG_OK;
+}
 
 namespace {
 
@@ -69,16 +81,53 @@ __global__ void k_pack_input(Geom g, int n, const double* __restrict__ rho, cons
     d[1] = *reinterpret_cast<const uint4*>(o + 8);
 }
 
-// training target of cell v: (e - z) at slot (i,j,k) divided by sc[1]
+// per-block partials of the sum of (e - z).p over the free cells and of their count
+__global__ void k_pmean(Geom g, int n, const float4* __restrict__ e, const float4* __restrict__ z, const uint8_t* __restrict__ m,
+                        double* __restrict__ part) {
+    __shared__ double sh[2][TPB / 32];
+    double s = 0, c = 0;
+    const long long V = (long long)n * n * n;
+    for (long long v = (long long)blockIdx.x * TPB + threadIdx.x; v < V; v += (long long)gridDim.x * TPB) {
+        const int k = (int)(v % n), j = (int)((v / n) % n), i = (int)(v / ((long long)n * n));
+        const int q = g.slot(i, j, k);
+        if (!(m[q] & MP)) {
+            s += (double)(e[q].x - z[q].x);
+            c += 1.0;
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        s += __shfl_xor_sync(0xffffffffu, s, o);
+        c += __shfl_xor_sync(0xffffffffu, c, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        sh[0][threadIdx.x >> 5] = s;
+        sh[1][threadIdx.x >> 5] = c;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = 0, b = 0;
+        for (int w = 0; w < TPB / 32; w++) {
+            a += sh[0][w];
+            b += sh[1][w];
+        }
+        part[blockIdx.x] = a;
+        part[gridDim.x + blockIdx.x] = b;
+    }
+}
+
+// training target of cell v: (e - z) at slot (i,j,k) divided by sc[1], with the mean
+// pressure pm[0] / pm[1] over the free cells removed when pm != nullptr (closed domains:
+// the constant pressure is the null space of A, so no residual can predict it)
 __global__ void k_pack_target(Geom g, int n, const float4* __restrict__ e, const float4* __restrict__ z, const float* __restrict__ sc,
-                              float* __restrict__ tgt) {
+                              const double* __restrict__ pm, const uint8_t* __restrict__ m, float* __restrict__ tgt) {
     const long long v = (long long)blockIdx.x * TPB + threadIdx.x;
     if (v >= (long long)n * n * n) return;
     const int k = (int)(v % n), j = (int)((v / n) % n), i = (int)(v / ((long long)n * n));
     const int s = g.slot(i, j, k);
     const float4 a = e[s], b = z[s];
     const float w = sc[1] > 0.f ? 1.f / sc[1] : 0.f;
-    *reinterpret_cast<float4*>(tgt + v * 4) = make_float4((a.x - b.x) * w, (a.y - b.y) * w, (a.z - b.z) * w, (a.w - b.w) * w);
+    const float p0 = (pm && pm[1] > 0 && !(m[s] & MP)) ? (float)(pm[0] / pm[1]) : 0.f;
+    *reinterpret_cast<float4*>(tgt + v * 4) = make_float4((a.x - b.x - p0) * w, (a.y - b.y) * w, (a.z - b.z) * w, (a.w - b.w) * w);
 }
 
 // z[slot] += out[v] * sc[1] on the free unknowns of the cells (i,j,k) < n
@@ -229,14 +278,14 @@ __global__ void k_head(const bf16* __restrict__ x, int C, const float* __restric
     *reinterpret_cast<float4*>(out + v * 4) = make_float4(o[0], o[1], o[2], o[3]);
 }
 
-// loss partials and dout = 2 (out - tgt) / count
+// partials of the loss mean (out - tgt)^2 and dout = 2 (out - tgt) / count
 __global__ void k_mse(const float* __restrict__ out, const float* __restrict__ tgt, long long count, float* __restrict__ dout,
                       double* __restrict__ part) {
     __shared__ double sh[TPB / 32];
     double s = 0;
     for (long long e = (long long)blockIdx.x * TPB + threadIdx.x; e < count; e += (long long)gridDim.x * TPB) {
         const float d = out[e] - tgt[e];
-        s += (double)d * d;
+        s += (double)d * d / (double)count;
         dout[e] = 2.f * d / (float)count;
     }
     for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
@@ -407,7 +456,7 @@ int net_alloc_params(NetState& N) {
     STG_TRY(B.get(&N.m2, N.nparam));
     STG_TRY(B.get(&N.p16, N.nparam));
     STG_TRY(B.get(&N.wf, N.nparam));
-    STG_TRY(B.get(&N.part, NPART));
+    STG_TRY(B.get(&N.part, 2 * NPART));
     STG_TRY(B.get(&N.dsum, 2));
     STG_TRY(B.get(&N.dloss, 1));
     STG_TRY(B.get(&N.sc, 2));
@@ -670,7 +719,15 @@ int net_pair(stg_t* h, NetState& N, uint64_t seed) {
     STG_TRY(precond3(h, N.s_r, N.s_z));
     STG_TRY(resid32(h->st, g, (float)F.vol, N.s_r, N.s_z, F.m, F.P32, N.s_r1, fast(h, F)));
     STG_TRY(net_pack(h, N, N.s_r1));
-    k_pack_target<<<nb(vox3(h->n)), TPB, 0, h->st>>>(g, h->n, N.s_e, N.s_z, N.sc, N.tgt);
+    const double* pm = nullptr;
+    if (h->closed) {
+        k_pmean<<<NPART, TPB, 0, h->st>>>(g, h->n, N.s_e, N.s_z, F.m, N.part);
+        STG_LAUNCH_CK();
+        STG_TRY(reduce_parts(h->st, N.part, NPART, N.dsum));
+        STG_TRY(reduce_parts(h->st, N.part + NPART, NPART, N.dsum + 1));
+        pm = N.dsum;
+    }
+    k_pack_target<<<nb(vox3(h->n)), TPB, 0, h->st>>>(g, h->n, N.s_e, N.s_z, N.sc, pm, F.m, N.tgt);
     STG_LAUNCH_CK();
     return STG_OK;
 }
@@ -750,7 +807,7 @@ int stg_net_forward_backward(stg_t* h, int n, const float* in, const float* targ
     }
     if (out) STG_CK(cudaMemcpyAsync(out, N.out, sizeof(float) * V * stg::OUT_CH, cudaMemcpyDeviceToHost, h->st));
     STG_CK(cudaStreamSynchronize(h->st));
-    return STG_OK;
+    return stg::tc_check(h->st);
 }
 
 int stg_net_adam_step(stg_t* h, double lr) {
@@ -806,6 +863,7 @@ int stg_net_train(stg_t* h, int steps, double lr, uint64_t seed, float* losses) 
             for (int s = 0; s < steps; s++) losses[s] = (float)dl[s];
     }
     cudaFree(d_losses);
+    if (rc == STG_OK) rc = stg::tc_check(h->st);
     return rc;
 }
 

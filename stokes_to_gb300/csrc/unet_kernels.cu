@@ -15,6 +15,9 @@
 
 namespace stg {
 
+extern bool g_conv_tc;
+extern int* g_tc_err;
+
 namespace {
 
 constexpr int WPB = 4;  // warps per block
@@ -184,6 +187,243 @@ __global__ void k_flip_weights(const __nv_bfloat16* __restrict__ w, int cout, in
     wf[((size_t)(26 - t) * cin + ci) * cout + co] = w[e];
 }
 
+// ---------------------------------------------------------------- tcgen05 forward
+// The same convolution on the 5th-generation tensor cores. A CTA owns J consecutive
+// j-lines of one i-plane (all k). It stages the halo box (3 planes x (J+2) lines x (n+2)
+// cells) of one 16-channel slice of the input in shared memory as K-major core matrices
+// without swizzle: row r = jj (n+2) + kk of plane p holds the 16 bytes of channels
+// [8g, 8g+8) at ((g 3 + p) R + r) 16, R = (J+2)(n+2). In this layout a tap (di,dj,dk) is a
+// uniform row shift, so one shared-memory descriptor per tap and M-tile addresses the
+// implicit-GEMM A operand (128 consecutive rows; rows that fall on halo columns are
+// computed and discarded). The weights of the slice sit beside it as [g][tap][C_out]
+// rows. One thread issues tcgen05.mma (M 128, N C_out, K 16, BF16 in, FP32 accumulators
+// in tensor memory) for every tap and M-tile, commits to an mbarrier, and the four warps
+// read the accumulators back with tcgen05.ld for the bias / ReLU / store epilogue.
+namespace tc {
+
+__device__ __forceinline__ uint32_t saddr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// shared-memory matrix descriptor: K-major, no swizzle; lbo = byte stride between core
+// matrices along K, sbo = byte stride between 8-row core matrices along M/N
+__device__ __forceinline__ uint64_t sdesc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+// instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both K-major
+__host__ __device__ constexpr uint32_t idesc_bf16(int m, int nn) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(nn >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+
+__device__ __forceinline__ void cp16(uint32_t dst, const void* src, int bytes) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(dst), "l"(src), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void mma(uint32_t d, uint64_t a, uint64_t b, uint32_t id, uint32_t acc) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d),
+        "l"(a), "l"(b), "r"(id), "r"(acc)
+        : "memory");
+}
+
+// waits for the mbarrier phase of the given parity; false after about a second
+__device__ __forceinline__ bool wait_parity(uint32_t bar, uint32_t parity) {
+    uint64_t t0;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+    while (true) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}\n"
+            : "=r"(done)
+            : "r"(bar), "r"(parity)
+            : "memory");
+        if (done) return true;
+        uint64_t t1;
+        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t1));
+        if (t1 - t0 > 1000000000ull) return false;
+    }
+}
+
+__device__ __forceinline__ void ld16(uint32_t taddr, uint32_t (&v)[16]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]), "=r"(v[8]),
+          "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+}
+
+}  // namespace tc
+
+// Tile plan of the tcgen05 kernel for an n^3 grid: J lines per CTA, T M-tiles.
+struct TcPlan {
+    int J = 0, T = 0, ncols = 0;
+    size_t smem = 0;
+};
+
+template <int COUT, bool F32>
+__global__ void __launch_bounds__(128) k_conv3_tc(const __nv_bfloat16* __restrict__ in, int cin, int ldin,
+                                                  const __nv_bfloat16* __restrict__ w, int wtap, const float* __restrict__ bias,
+                                                  void* __restrict__ outp, int ldout, int n, int relu, int J, int T, int ncols,
+                                                  int* __restrict__ err) {
+    extern __shared__ __align__(128) uint8_t smem[];
+    const int Hk = n + 2, R = (J + 2) * Hk;
+    uint8_t* sA = smem;
+    uint8_t* sB = smem + (size_t)96 * R;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(sB + 864 * COUT);
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + 1);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int i = blockIdx.x, j0 = blockIdx.y * J;
+    const uint32_t bar_a = tc::saddr(bar);
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(tc::saddr(tslot)), "r"(ncols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    }
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar_a) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const uint32_t tbase = *tslot;
+    const uint32_t a0 = tc::saddr(sA), b0 = tc::saddr(sB);
+    const uint32_t lbo_a = 48u * (uint32_t)R, lbo_b = 432u * COUT;
+    constexpr uint32_t ID = tc::idesc_bf16(128, COUT);
+    const int rlast = (J + 1) * Hk - 2 - 127;
+    uint32_t phase = 0;
+    int bad = 0;
+    const int nchunk = cin / 16;
+    for (int ch = 0; ch < nchunk && !bad; ch++) {
+        const int c0 = ch * 16;
+        if (ch > 0) {
+            // the previous slice's MMAs read sA / sB: wait for them before overwriting
+            bad = __syncthreads_or(!tc::wait_parity(bar_a, phase));
+            phase ^= 1;
+            if (bad) break;
+        }
+        for (int e = tid; e < 6 * R; e += 128) {
+            const int g = e / (3 * R), rem = e - g * 3 * R, p = rem / R, r = rem - p * R;
+            const int jj = r / Hk, kk = r - jj * Hk;
+            const int gi = i - 1 + p, gj = j0 - 1 + jj, gk = kk - 1;
+            const bool inside = gi >= 0 && gi < n && gj >= 0 && gj < n && gk >= 0 && gk < n;
+            const __nv_bfloat16* src = inside ? in + (size_t)((gi * n + gj) * n + gk) * ldin + c0 + 8 * g : in;
+            tc::cp16(a0 + 16u * e, src, inside ? 16 : 0);
+        }
+        for (int e = tid; e < 54 * COUT; e += 128) {
+            const int g = e / (27 * COUT), rem = e - g * 27 * COUT, t = rem / COUT, co = rem - t * COUT;
+            tc::cp16(b0 + 16u * e, w + (size_t)t * wtap + (size_t)co * cin + c0 + 8 * g, 16);
+        }
+        asm volatile("cp.async.wait_all;\n" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        __syncthreads();
+        if (tid == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            for (int t = 0; t < 27; t++) {
+                const int di = t / 9 - 1, dj = (t / 3) % 3 - 1, dk = t % 3 - 1;
+                const uint64_t bd = tc::sdesc(b0 + 16u * (uint32_t)(t * COUT), lbo_b, 128);
+                for (int q = 0; q < T; q++) {
+                    const int r0 = q < T - 1 ? Hk + 1 + 128 * q : rlast;
+                    const uint32_t row = (uint32_t)((1 + di) * R + r0 + dj * Hk + dk);
+                    tc::mma(tbase + (uint32_t)(q * COUT), tc::sdesc(a0 + 16u * row, lbo_a, 128), bd, ID, (ch > 0 || t > 0) ? 1u : 0u);
+                }
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(bar_a) : "memory");
+        }
+    }
+    if (!bad) bad = __syncthreads_or(!tc::wait_parity(bar_a, phase));
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    if (!bad) {
+        for (int q = 0; q < T; q++) {
+            const int r = (q < T - 1 ? Hk + 1 + 128 * q : rlast) + warp * 32 + lane;
+            const int jj = r / Hk, kk = r - jj * Hk;
+            const int gj = j0 - 1 + jj;
+            const bool valid = jj >= 1 && jj <= J && kk >= 1 && kk <= n && gj < n;
+            const size_t v = (size_t)(i * n + gj) * n + (kk - 1);
+#pragma unroll
+            for (int cb = 0; cb < COUT; cb += 16) {
+                uint32_t x[16];
+                tc::ld16(tbase + ((uint32_t)(warp * 32) << 16) + (uint32_t)(q * COUT + cb), x);
+                if (valid) {
+                    float y[16];
+#pragma unroll
+                    for (int u = 0; u < 16; u++) {
+                        y[u] = __uint_as_float(x[u]) + (bias ? bias[cb + u] : 0.f);
+                        if (relu) y[u] = fmaxf(y[u], 0.f);
+                    }
+                    if (F32) {
+                        float4* o = reinterpret_cast<float4*>(static_cast<float*>(outp) + v * ldout + cb);
+#pragma unroll
+                        for (int u = 0; u < 4; u++) o[u] = make_float4(y[4 * u], y[4 * u + 1], y[4 * u + 2], y[4 * u + 3]);
+                    } else {
+                        __align__(16) __nv_bfloat162 h[8];
+#pragma unroll
+                        for (int u = 0; u < 8; u++) h[u] = __floats2bfloat162_rn(y[2 * u], y[2 * u + 1]);
+                        uint4* o = reinterpret_cast<uint4*>(static_cast<__nv_bfloat16*>(outp) + v * ldout + cb);
+                        o[0] = reinterpret_cast<const uint4*>(h)[0];
+                        o[1] = reinterpret_cast<const uint4*>(h)[1];
+                    }
+                }
+            }
+        }
+    } else if (tid == 0) {
+        atomicExch(err, 1);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tbase), "r"(ncols) : "memory");
+}
+
+constexpr size_t TC_SMEM_MAX = 200 * 1024;
+
+// J (lines per CTA) with the most useful rows per M-tile row, within the shared memory
+// and tensor-memory budgets (two CTAs per SM, else one); J = 0 when no plan fits (small
+// grids use the mma.sync kernel)
+TcPlan tc_plan(int n, int cout) {
+    TcPlan best;
+    for (int tier = 0; tier < 2 && !best.J; tier++) {
+        const size_t budget = tier == 0 ? 110 * 1024 : TC_SMEM_MAX;
+        const int max_cols = tier == 0 ? 256 : 512;
+        double best_eff = 0;
+        for (int J = 1; J <= n; J++) {
+            const int Hk = n + 2, rows = J * Hk - 2;
+            if (rows < 128) continue;
+            const int T = (rows + 127) / 128;
+            const size_t smem = (size_t)96 * (J + 2) * Hk + 864 * (size_t)cout + 16;
+            if (smem > budget || T * cout > max_cols) break;
+            const double eff = (double)J * n / (128.0 * T);
+            if (eff > best_eff + 1e-9) {
+                best_eff = eff;
+                best.J = J;
+                best.T = T;
+                best.smem = smem;
+            }
+        }
+    }
+    if (best.J) {
+        int c = 32;
+        while (c < best.T * cout) c <<= 1;
+        best.ncols = c;
+    }
+    return best;
+}
+
+template <int C, bool F32>
+int launch_tc(const TcPlan& P, cudaStream_t st, const __nv_bfloat16* in, int cin, int ldin, const __nv_bfloat16* w, int wtap,
+              const float* bias, void* out, int ldout, int n, int relu, int* err) {
+    static bool attr = false;
+    if (!attr) {
+        STG_CK(cudaFuncSetAttribute(k_conv3_tc<C, F32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM_MAX));
+        attr = true;
+    }
+    dim3 grid(n, (n + P.J - 1) / P.J);
+    k_conv3_tc<C, F32><<<grid, 128, P.smem, st>>>(in, cin, ldin, w, wtap, bias, out, ldout, n, relu, P.J, P.T, P.ncols, err);
+    return STG_OK;
+}
+
 template <int C>
 void launch_fwd(int nblk, cudaStream_t st, const __nv_bfloat16* in, int cin, int ldin, const __nv_bfloat16* w, const float* bias,
                 void* out, int ldout, int n, int relu, bool f32, int wtap) {
@@ -200,6 +440,19 @@ void launch_dw(dim3 grid, cudaStream_t st, const __nv_bfloat16* x, int ldx, cons
 
 }  // namespace
 
+// tensor-core convolutions on (default) or the mma.sync kernel for every shape; the
+// error flag of the tcgen05 kernel's bounded waits (device, 0 = no timeout)
+bool g_conv_tc = true;
+int* g_tc_err = nullptr;
+
+int conv3_tc_status(cudaStream_t st, int* timed_out) {
+    *timed_out = 0;
+    if (!g_tc_err) return STG_OK;
+    STG_CK(cudaMemcpyAsync(timed_out, g_tc_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    STG_CK(cudaStreamSynchronize(st));
+    return STG_OK;
+}
+
 int conv3_forward(cudaStream_t st, const __nv_bfloat16* in, int cin, int ldin, const __nv_bfloat16* w, const float* bias,
                   void* out, int cout, int ldout, int n, int relu, bool f32_out, int wtap) {
     // wtap: elements between taps of w (0: cout * cin, the dense layout; larger when w is a
@@ -211,7 +464,29 @@ int conv3_forward(cudaStream_t st, const __nv_bfloat16* in, int cin, int ldin, c
         return STG_E_INVALID;
     }
     const long long V = (long long)n * n * n;
-    const int nblk = (int)((V / 16 + WPB - 1) / WPB);
+    // tensor-core path: C_out a multiple of 16, 16-byte aligned rows and weight slices
+    if (g_conv_tc && cout % 16 == 0 && ldin % 8 == 0 && wtap % 8 == 0 && ((uintptr_t)in & 15) == 0 && ((uintptr_t)w & 15) == 0 &&
+        ((uintptr_t)out & 15) == 0 && ldout % 8 == 0) {
+        const TcPlan P = tc_plan(n, cout);
+        if (P.J) {
+            if (!g_tc_err) STG_CK(cudaMalloc((void**)&g_tc_err, sizeof(int)));
+            int rc = STG_OK;
+            switch (cout) {
+                case 16: rc = f32_out ? launch_tc<16, true>(P, st, in, cin, ldin, w, wtap, bias, out, ldout, n, relu, g_tc_err)
+                                      : launch_tc<16, false>(P, st, in, cin, ldin, w, wtap, bias, out, ldout, n, relu, g_tc_err); break;
+                case 32: rc = f32_out ? launch_tc<32, true>(P, st, in, cin, ldin, w, wtap, bias, out, ldout, n, relu, g_tc_err)
+                                      : launch_tc<32, false>(P, st, in, cin, ldin, w, wtap, bias, out, ldout, n, relu, g_tc_err); break;
+                case 48: rc = f32_out ? launch_tc<48, true>(P, st, in, cin, ldin, w, wtap, bias, out, ldout, n, relu, g_tc_err)
+                                      : launch_tc<48, false>(P, st, in, cin, ldin, w, wtap, bias, out, ldout, n, relu, g_tc_err); break;
+                default: rc = f32_out ? launch_tc<64, true>(P, st, in, cin, ldin, w, wtap, bias, out, ldout, n, relu, g_tc_err)
+                                      : launch_tc<64, false>(P, st, in, cin, ldin, w, wtap, bias, out, ldout, n, relu, g_tc_err); break;
+            }
+            STG_TRY(rc);
+            STG_LAUNCH_CK();
+            return STG_OK;
+        }
+    }
+    const int nblk = (int)(((V + 15) / 16 + WPB - 1) / WPB);
     switch (cout) {
         case 8: launch_fwd<8>(nblk, st, in, cin, ldin, w, bias, out, ldout, n, relu, f32_out, wtap); break;
         case 16: launch_fwd<16>(nblk, st, in, cin, ldin, w, bias, out, ldout, n, relu, f32_out, wtap); break;
