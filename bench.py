@@ -5,8 +5,13 @@ FGMRES inside FP64 refinement) of the 256^3 parabolic-inlet problem with a seede
 Gaussian-smoothed density (sigma 4 cells), density filter r = 1.5 and the
 Borrvall-Petersson alpha law (amax 1e4). Working set is ~25 GB, far above the 129 MB L2.
 
-  value  device-resident inputs, CUDA events on the solve stream      (method: mixed)
+  value  device-resident inputs, CUDA events on the solve stream (method: plain, the
+         library default: FP32 V-cycle with one smoother sweep per colour, FGMRES in FP64
+         refinement)
   e2e    host buffers through the C ABI: set_penalty + set_rhs + solve + read back
+  methods  the same solve with the reference's two sweeps per colour, the mixed form (BF16
+         coarse corrections) and the learned form (U-Net trained on the GPU at 64^3 on the
+         same problem family, applied at 256^3); training time reported, not in the timed region
   --impl reference: the CPU reference restatement (oracle) on the host cores.
 
 N>1 (torchrun): independent replicas, one per GPU, barrier + max over ranks.
@@ -28,7 +33,10 @@ sys.path.insert(0, ROOT)
 N_DEFAULT = 256
 TOL = 1e-8
 FALLBACK_HBM_GBS = 6800.0
-METRIC = "s per 256^3 Stokes solve to FP64 resid 1e-8 (mixed precision)"
+METRIC = "s per 256^3 Stokes solve to FP64 resid 1e-8"
+NET_TRAIN_N = 64
+NET_TRAIN_STEPS = 3000
+NET_LR = 3e-4
 
 
 PROFILED_SOLVES = 2
@@ -42,7 +50,7 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=N_DEFAULT)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-methods", action="store_true", help="skip the reference-smoother, mixed and learned legs")
     return ap.parse_args()
 
 
@@ -269,14 +277,15 @@ def run_ours(args):
 
     stream = torch.cuda.current_stream()
 
-    def make_solver(method):
-        s = capi.Solver(n, method=method, tol=TOL)
+    def make_solver(method, nn=n, **kw):
+        bc = parabolic_bc(nn) if nn != n else (cell_vol, cell_fixed, cell_b, face_vol, face_fixed, face_b)
+        s = capi.Solver(nn, method=method, tol=TOL, **kw)
         s.set_stream(stream.cuda_stream)
-        s.set_boundary(cell_vol, cell_fixed, face_vol, face_fixed, True)
+        s.set_boundary(bc[0], bc[1], bc[3], bc[4], True)
         s.density_noise(1 + rank, 4.0, want=False)
         s.filter(1.5, None, want=False)
         s.set_density(None, capi.alpha_bp(1e4))
-        s.set_rhs(cell_b, face_b)
+        s.set_rhs(bc[2], bc[5])
         return s
 
     def timed_device(s, steps, warmup, profile=False):
@@ -301,8 +310,8 @@ def run_ours(args):
         prof = s.profile_read() if profile else None
         return ms, stats, launches, clk.summary(), prof
 
-    # ---- headline: mixed method, inputs resident (no per-kernel events in this region)
-    s = make_solver(capi.STG_METHOD_MIXED)
+    # ---- headline: plain method, inputs resident (no per-kernel events in this region)
+    s = make_solver(capi.STG_METHOD_PLAIN)
     ms, stats, launches, clocks, _ = timed_device(s, args.steps, args.warmup, profile=False)
     t_max = max_over_ranks(ms / 1e3)
     value = t_max / (args.steps * world)
@@ -346,14 +355,43 @@ def run_ours(args):
     h2d = sum(f.nbytes for f in fpen_p) + cb_p.nbytes + sum(f.nbytes for f in fb_p)
     d2h = p_out.nbytes + sum(v.nbytes for v in v_out)
 
-    # ---- plain FP32/FP64 method for context
-    plain = None
-    if not args.no_plain:
-        sp = make_solver(capi.STG_METHOD_PLAIN)
-        pms, pstats, _, _, _ = timed_device(sp, max(2, args.steps // 2), 1)
-        plain = max_over_ranks(pms / 1e3) / (max(2, args.steps // 2) * world)
-        plain_vc = statistics.mean(st["inner_iters"] for st in pstats)
-        sp.close()
+    # ---- the other methods on the same problem, for the comparison the metric names
+    methods = {"plain": {"s_per_solve": value, "v_cycles": statistics.mean(st["inner_iters"] for st in stats)}}
+    if not args.no_methods:
+        k = max(2, args.steps // 2)
+
+        def leg(sv):
+            ms_, st_, _, _, _ = timed_device(sv, k, 1)
+            return {"s_per_solve": max_over_ranks(ms_ / 1e3) / (k * world),
+                    "v_cycles": statistics.mean(x["inner_iters"] for x in st_),
+                    "max_rel_residual": max(x["rel_residual"] for x in st_)}
+
+        sv = make_solver(capi.STG_METHOD_PLAIN, smooth_sweeps=2)
+        methods["plain_reference_smoother"] = leg(sv)
+        sv.close()
+        sv = make_solver(capi.STG_METHOD_MIXED)
+        methods["mixed"] = leg(sv)
+        sv.close()
+        # learned: train at NET_TRAIN_N^3 on the same problem family, apply at n^3
+        tr = make_solver(capi.STG_METHOD_PLAIN, nn=NET_TRAIN_N)
+        tr.net_init(7)
+        barrier()
+        t0 = time.perf_counter()
+        losses = tr.net_train(NET_TRAIN_STEPS, lr=NET_LR, seed=3)
+        barrier()
+        train_s = time.perf_counter() - t0
+        params = tr.net_params()
+        tr.close()
+        sv = make_solver(capi.STG_METHOD_LEARNED)
+        sv.net_init(7)
+        sv.net_set_params(params)
+        r = leg(sv)
+        _, _, st1 = sv.solve(want=False)
+        r.update({"learned_iters": st1["learned_iters"], "fallbacks": st1["fallbacks"], "train_s": round(train_s, 2),
+                  "train": f"{NET_TRAIN_STEPS} Adam steps (lr {NET_LR:g}) at {NET_TRAIN_N}^3, one fresh pair per step",
+                  "final_loss": round(float(np.mean(losses[-100:])), 4)})
+        methods["learned"] = r
+        sv.close()
 
     # ---- roofline of the dominant kernel class, measured over the timed region
     peak, peak_kind = measured_peak()
@@ -378,9 +416,10 @@ def run_ours(args):
         line = {
             "metric": METRIC, "value": value, "unit": "s/solve", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": value * 1e3 * world, "higher_is_better": False, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32 V-cycle / bf16 coarse corrections / f64 refinement", "data": "synthetic",
-            "config": {"workload": f"3D {n}^3 Brinkman-Stokes solve to FP64 rel. residual {TOL:g}, mixed precision",
-                       "n": n, "method": "mixed", "tol": TOL, "bc": "parabolic inlet N/4 patch, mirrored outlet",
+            "vs_baseline": None, "dtype": "f32 V-cycle and Krylov / f64 refinement", "data": "synthetic",
+            "config": {"workload": f"3D {n}^3 Brinkman-Stokes solve to FP64 rel. residual {TOL:g}",
+                       "n": n, "method": "plain (FP32 V-cycle, 1 smoother sweep per colour, FGMRES in FP64 refinement)",
+                       "tol": TOL, "bc": "parabolic inlet N/4 patch, mirrored outlet",
                        "density": "seeded U[0,1], Gaussian sigma 4, filter r 1.5, BP alpha amax 1e4",
                        "l2": "inputs larger than L2 (~25 GB working set)", "parallelism": f"replicas x{world}"},
             "e2e": {"value": e2e_value, "unit": "s/solve", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
@@ -391,8 +430,8 @@ def run_ours(args):
             "cpu_baseline": cpu,
             "clocks": clocks,
             "solver": {"v_cycles_per_solve": vc, "outer_per_solve": statistics.mean(st["outer_iters"] for st in stats),
-                       "final_rel_residual_max": max(st["rel_residual"] for st in stats),
-                       "plain_s_per_solve": plain, "plain_v_cycles": plain_vc if plain else None},
+                       "final_rel_residual_max": max(st["rel_residual"] for st in stats)},
+            "methods": methods,
             "kernels": kernel_table,
         }
         print(json.dumps(line), flush=True)

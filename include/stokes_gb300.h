@@ -43,7 +43,8 @@ typedef struct stg_ctx stg_t;
 #define STG_METHOD_MIXED 1 /* as PLAIN with BF16-stored coarse-level corrections */
 #define STG_METHOD_LEARNED 2 /* as PLAIN with the learned correction of stg_net_* added to every
                                 V-cycle; falls back to PLAIN for the rest of a solve when a
-                                Krylov step reduces the residual estimate by less than 20% */
+                                Krylov step other than the first of a refinement step reduces
+                                the residual estimate by less than 20% */
 
 typedef struct stg_opts {
     int method;          /* STG_METHOD_* */
@@ -291,8 +292,8 @@ int stg_net_set_params(stg_t* h, const float* in, int64_t count);
 /* One forward pass on host data of an n^3 grid (n >= 8, n % 4 == 0), independent of the
  * handle's grid: in [n^3][8] channels (density, p, u, v, w, three penalty shares), cell
  * v = (i n + j) n + k. out [n^3][4] (may be NULL). With target [n^3][4] non-NULL, also the
- * mean-squared-error loss and its gradient with respect to every parameter (grad may be
- * NULL), kept for stg_net_adam_step. */
+ * loss sum (out - target)^2 / sum target^2 and its gradient with respect to every
+ * parameter (grad may be NULL), kept for stg_net_adam_step. */
 int stg_net_forward_backward(stg_t* h, int n, const float* in, const float* target, float* out, float* grad, double* loss);
 /* One Adam step (beta 0.9 / 0.999, eps 1e-8) with the last computed gradient. */
 int stg_net_adam_step(stg_t* h, double lr);

@@ -121,7 +121,8 @@ def up_bwd(g):
 def forward_backward(params, inp, target=None, bf=True, c=16):
     """inp [n^3][8] (float), target [n^3][4] or None.
 
-    Returns dict(out [n^3][4], loss, grad [nparam]) (loss / grad only with a target)."""
+    Returns dict(out [n^3][4], loss, grad [nparam]) (loss / grad only with a target). The
+    loss is the relative squared error sum (out - target)^2 / sum target^2."""
     L = layout(c)
     p = np.asarray(params, dtype=np.float64)
     W, b, hw, hb = unpack(p, L)
@@ -154,9 +155,9 @@ def forward_backward(params, inp, target=None, bf=True, c=16):
     if target is None:
         return res
     t = np.asarray(target, dtype=np.float64).reshape(n, n, n, OUT_CH)
-    cnt = V * OUT_CH
-    res["loss"] = float(np.sum((out - t) ** 2) / cnt)
-    dout = 2.0 * (out - t) / cnt
+    t2 = float(np.sum(t ** 2))
+    res["loss"] = float(np.sum((out - t) ** 2) / t2)
+    dout = 2.0 * (out - t) / t2
     g = np.zeros(L["nparam"])
 
     def put(l, dW, db):

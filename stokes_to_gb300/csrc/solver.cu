@@ -404,8 +404,11 @@ int solve_core(stg_t* h, const d4* b, d4* x, stg_stats* stats) {
             double est = std::fabs(g[j + 1]);
             if (h->opts.verbose > 1) fprintf(stderr, "[stg]   inner %d  est %.3e\n", j, est);
             // a learned step that cut the estimate by less than 20% ends the network's use in
-            // this solve (FGMRES is flexible, so the basis built so far stays valid)
-            if (h->net_on && est > 0.8 * prev_est) {
+            // this solve (FGMRES is flexible, so the basis built so far stays valid). The
+            // first step of a refinement step is not judged: its reduction depends on how
+            // the right-hand side lies (a boundary-driven b gives about 2% with plain
+            // multigrid too).
+            if (h->net_on && j > 0 && est > 0.8 * prev_est) {
                 h->net_on = false;
                 S.fallbacks++;
             }

@@ -1,9 +1,10 @@
 // Learned preconditioner: a 3-level 3D U-Net over the finest-level cells (new; no
 // counterpart in the reference).
 //
-// Input per cell (i,j,k) of the n^3 grid: the physical density and the four unknowns of
-// slot (i,j,k) of a residual vector (p and the three low faces), scaled by the residual's
-// RMS. Output: a correction for the same four unknowns, scaled back. Architecture (c base
+// Input per cell (i,j,k) of the n^3 grid: the physical density, the four unknowns of slot
+// (i,j,k) of a residual vector (p and the three low faces) scaled by the residual's RMS,
+// and the three face penalties as shares P / (P + 6 vol) of the diagonal of A. Output: a
+// correction for the same four unknowns, scaled back. Architecture (c base
 // channels; every convolution 3x3x3 + ReLU, BF16 weights and activations, FP32
 // accumulation on the tensor cores, unet_kernels.cu):
 //   level 0 (n^3):   in(16) -> c -> c = s0
@@ -12,8 +13,8 @@
 //   level 1:         [up(level 2), s1] (6c) -> 2c -> 2c
 //   level 0:         [up(level 1), s0] (3c) -> c -> c -> 1x1 head -> 4 (FP32)
 // Skip connections are channel slices of the concatenation buffers (the encoder writes its
-// output straight into them). Training: mean-squared error against the exact correction,
-// Adam on FP32 master weights, BF16 working copies refreshed after every step.
+// output straight into them). Training: relative squared error against the exact
+// correction, Adam on FP32 master weights, BF16 working copies refreshed after every step.
 #include <cuda_bf16.h>
 
 #include <cmath>
@@ -194,74 +195,116 @@ __global__ void k_noise_slots(Geom g, const uint8_t* __restrict__ m, uint64_t se
     x[s] = make_float4(mm & MP ? 0.f : r[0], mm & MU ? 0.f : r[1], mm & MV ? 0.f : r[2], mm & MW ? 0.f : r[3]);
 }
 
-// 2x2x2 average pooling of channels [0, C) of a (ld_in) into b (ld_out), coarse grid nc
-__global__ void k_pool(const bf16* __restrict__ a, int ld_in, int C, bf16* __restrict__ b, int ld_out, int nc) {
-    const long long e = (long long)blockIdx.x * TPB + threadIdx.x;
-    const long long Vc = (long long)nc * nc * nc;
-    if (e >= Vc * C) return;
-    const int c = (int)(e % C);
-    const long long v = e / C;
-    const int k = (int)(v % nc), j = (int)((v / nc) % nc), i = (int)(v / ((long long)nc * nc));
-    const int nf = 2 * nc;
-    float s = 0.f;
-    for (int q = 0; q < 8; q++) {
-        const long long fv = ((long long)(2 * i + (q >> 2)) * nf + 2 * j + ((q >> 1) & 1)) * nf + 2 * k + (q & 1);
-        s += bf(a[fv * ld_in + c]);
-    }
-    b[v * ld_out + c] = __float2bfloat16(0.125f * s);
+// The resampling kernels below take one thread per (voxel, 8 BF16 or 4 FP32 channels):
+// every channel count and row stride is a multiple of 8 and every row starts on 16 bytes.
+__device__ __forceinline__ void vox_of(long long v, int nn, int& i, int& j, int& k) {
+    const long long q = v / nn;
+    k = (int)(v - q * nn);
+    i = (int)(q / nn);
+    j = (int)(q - (long long)i * nn);
 }
 
-// g_fine[child][c] += g_coarse[parent][c] / 8 (pooling backward; FP32)
-__global__ void k_pool_bwd(const float* __restrict__ gc, int ldc, int C, float* __restrict__ gf, int ldf, int nc) {
+// 2x2x2 average pooling of channels [0, C) of a (ld_in) into b (ld_out), coarse grid nc
+__global__ void k_pool(const bf16* __restrict__ a, int ld_in, int C, bf16* __restrict__ b, int ld_out, int nc) {
+    const int G = C / 8;
     const long long e = (long long)blockIdx.x * TPB + threadIdx.x;
+    if (e >= (long long)nc * nc * nc * G) return;
+    const int q = (int)(e % G);
+    const long long v = e / G;
+    int i, j, k;
+    vox_of(v, nc, i, j, k);
     const int nf = 2 * nc;
-    const long long Vf = (long long)nf * nf * nf;
-    if (e >= Vf * C) return;
-    const int c = (int)(e % C);
-    const long long v = e / C;
-    const int k = (int)(v % nf), j = (int)((v / nf) % nf), i = (int)(v / ((long long)nf * nf));
+    float s[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+#pragma unroll
+    for (int c = 0; c < 8; c++) {
+        const long long fv = ((long long)(2 * i + (c >> 2)) * nf + 2 * j + ((c >> 1) & 1)) * nf + 2 * k + (c & 1);
+        const uint4 x = *reinterpret_cast<const uint4*>(a + fv * ld_in + 8 * q);
+        const bf16* h = reinterpret_cast<const bf16*>(&x);
+#pragma unroll
+        for (int u = 0; u < 8; u++) s[u] += bf(h[u]);
+    }
+    __align__(16) bf16 o[8];
+#pragma unroll
+    for (int u = 0; u < 8; u++) o[u] = __float2bfloat16(0.125f * s[u]);
+    *reinterpret_cast<uint4*>(b + v * ld_out + 8 * q) = *reinterpret_cast<const uint4*>(o);
+}
+
+// g_fine[child][c] += g_coarse[parent][c] / 8 (pooling backward; FP32, 4 channels a thread)
+__global__ void k_pool_bwd(const float* __restrict__ gc, int ldc, int C, float* __restrict__ gf, int ldf, int nc) {
+    const int G = C / 4;
+    const int nf = 2 * nc;
+    const long long e = (long long)blockIdx.x * TPB + threadIdx.x;
+    if (e >= (long long)nf * nf * nf * G) return;
+    const int q = (int)(e % G);
+    const long long v = e / G;
+    int i, j, k;
+    vox_of(v, nf, i, j, k);
     const long long pv = ((long long)(i >> 1) * nc + (j >> 1)) * nc + (k >> 1);
-    gf[v * ldf + c] += 0.125f * gc[pv * ldc + c];
+    const float4 g = *reinterpret_cast<const float4*>(gc + pv * ldc + 4 * q);
+    float4* d = reinterpret_cast<float4*>(gf + v * ldf + 4 * q);
+    float4 x = *d;
+    x.x += 0.125f * g.x;
+    x.y += 0.125f * g.y;
+    x.z += 0.125f * g.z;
+    x.w += 0.125f * g.w;
+    *d = x;
 }
 
 // nearest up-sampling of channels [0, C) of the coarse a into b (fine grid 2 nc)
 __global__ void k_up(const bf16* __restrict__ a, int ld_in, int C, bf16* __restrict__ b, int ld_out, int nc) {
-    const long long e = (long long)blockIdx.x * TPB + threadIdx.x;
+    const int G = C / 8;
     const int nf = 2 * nc;
-    const long long Vf = (long long)nf * nf * nf;
-    if (e >= Vf * C) return;
-    const int c = (int)(e % C);
-    const long long v = e / C;
-    const int k = (int)(v % nf), j = (int)((v / nf) % nf), i = (int)(v / ((long long)nf * nf));
+    const long long e = (long long)blockIdx.x * TPB + threadIdx.x;
+    if (e >= (long long)nf * nf * nf * G) return;
+    const int q = (int)(e % G);
+    const long long v = e / G;
+    int i, j, k;
+    vox_of(v, nf, i, j, k);
     const long long pv = ((long long)(i >> 1) * nc + (j >> 1)) * nc + (k >> 1);
-    b[v * ld_out + c] = a[pv * ld_in + c];
+    *reinterpret_cast<uint4*>(b + v * ld_out + 8 * q) = *reinterpret_cast<const uint4*>(a + pv * ld_in + 8 * q);
 }
 
-// g_coarse[parent][c] = sum of the 8 children's g_fine (up-sampling backward)
+// g_coarse[parent][c] = sum of the 8 children's g_fine (up-sampling backward, 4 channels a thread)
 __global__ void k_up_bwd(const float* __restrict__ gf, int ldf, int C, float* __restrict__ gc, int ldc, int nc) {
+    const int G = C / 4;
     const long long e = (long long)blockIdx.x * TPB + threadIdx.x;
-    const long long Vc = (long long)nc * nc * nc;
-    if (e >= Vc * C) return;
-    const int c = (int)(e % C);
-    const long long v = e / C;
-    const int k = (int)(v % nc), j = (int)((v / nc) % nc), i = (int)(v / ((long long)nc * nc));
+    if (e >= (long long)nc * nc * nc * G) return;
+    const int q = (int)(e % G);
+    const long long v = e / G;
+    int i, j, k;
+    vox_of(v, nc, i, j, k);
     const int nf = 2 * nc;
-    float s = 0.f;
-    for (int q = 0; q < 8; q++) {
-        const long long fv = ((long long)(2 * i + (q >> 2)) * nf + 2 * j + ((q >> 1) & 1)) * nf + 2 * k + (q & 1);
-        s += gf[fv * ldf + c];
+    float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+    for (int c = 0; c < 8; c++) {
+        const long long fv = ((long long)(2 * i + (c >> 2)) * nf + 2 * j + ((c >> 1) & 1)) * nf + 2 * k + (c & 1);
+        const float4 g = *reinterpret_cast<const float4*>(gf + fv * ldf + 4 * q);
+        s.x += g.x;
+        s.y += g.y;
+        s.z += g.z;
+        s.w += g.w;
     }
-    gc[v * ldc + c] = s;
+    *reinterpret_cast<float4*>(gc + v * ldc + 4 * q) = s;
 }
 
-// out = (y > 0) ? g : 0 as BF16 (ReLU backward, the conv input of the next backward pass)
+// out = (y > 0) ? g : 0 as BF16 (ReLU backward, the conv input of the next backward pass),
+// 8 channels a thread
 __global__ void k_relu_grad(const float* __restrict__ g, int ldg, const bf16* __restrict__ y, int ldy, int C, long long V,
                             bf16* __restrict__ out) {
+    const int G = C / 8;
     const long long e = (long long)blockIdx.x * TPB + threadIdx.x;
-    if (e >= V * C) return;
-    const int c = (int)(e % C);
-    const long long v = e / C;
-    out[v * C + c] = __float2bfloat16(bf(y[v * ldy + c]) > 0.f ? g[v * ldg + c] : 0.f);
+    if (e >= V * G) return;
+    const int q = (int)(e % G);
+    const long long v = e / G;
+    const float4 g0 = *reinterpret_cast<const float4*>(g + v * ldg + 8 * q);
+    const float4 g1 = *reinterpret_cast<const float4*>(g + v * ldg + 8 * q + 4);
+    const uint4 yy = *reinterpret_cast<const uint4*>(y + v * ldy + 8 * q);
+    const bf16* h = reinterpret_cast<const bf16*>(&yy);
+    const float gg[8] = {g0.x, g0.y, g0.z, g0.w, g1.x, g1.y, g1.z, g1.w};
+    __align__(16) bf16 o[8];
+#pragma unroll
+    for (int u = 0; u < 8; u++) o[u] = __float2bfloat16(bf(h[u]) > 0.f ? gg[u] : 0.f);
+    *reinterpret_cast<uint4*>(out + v * C + 8 * q) = *reinterpret_cast<const uint4*>(o);
 }
 
 // 1x1 head: out[v][o] = b[o] + sum_c W[o][c] x[v][c]  (4 outputs, FP32)
@@ -278,15 +321,17 @@ __global__ void k_head(const bf16* __restrict__ x, int C, const float* __restric
     *reinterpret_cast<float4*>(out + v * 4) = make_float4(o[0], o[1], o[2], o[3]);
 }
 
-// partials of the loss mean (out - tgt)^2 and dout = 2 (out - tgt) / count
-__global__ void k_mse(const float* __restrict__ out, const float* __restrict__ tgt, long long count, float* __restrict__ dout,
-                      double* __restrict__ part) {
+// partials of the relative squared error sum (out - tgt)^2 / *t2 (t2 = sum tgt^2, so the
+// zero output scores 1 on every sample) and dout = 2 (out - tgt) / *t2
+__global__ void k_mse(const float* __restrict__ out, const float* __restrict__ tgt, long long count, const double* __restrict__ t2,
+                      float* __restrict__ dout, double* __restrict__ part) {
     __shared__ double sh[TPB / 32];
     double s = 0;
+    const double inv = *t2 > 0 ? 1.0 / *t2 : 0.0;
     for (long long e = (long long)blockIdx.x * TPB + threadIdx.x; e < count; e += (long long)gridDim.x * TPB) {
         const float d = out[e] - tgt[e];
-        s += (double)d * d / (double)count;
-        dout[e] = 2.f * d / (float)count;
+        s += (double)d * d * inv;
+        dout[e] = (float)(2.0 * d * inv);
     }
     for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
     if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
@@ -392,7 +437,7 @@ struct NetState {
     __nv_bfloat16 *p16 = nullptr, *wf = nullptr;
     int adam_t = 0;
     float kappa = 0.f;  // host copy of p[kappa_off]
-    double *part = nullptr, *dsum = nullptr, *dloss = nullptr;
+    double *part = nullptr, *dsum = nullptr, *dloss = nullptr, *dt2 = nullptr;
     float* sc = nullptr;
     stg::Buf pbuf;
     // activations for grid n (train: also the gradient buffers)
@@ -459,6 +504,7 @@ int net_alloc_params(NetState& N) {
     STG_TRY(B.get(&N.part, 2 * NPART));
     STG_TRY(B.get(&N.dsum, 2));
     STG_TRY(B.get(&N.dloss, 1));
+    STG_TRY(B.get(&N.dt2, 1));
     STG_TRY(B.get(&N.sc, 2));
     return STG_OK;
 }
@@ -533,13 +579,13 @@ int conv_f(NetState& N, cudaStream_t st, int l, const bf16* in, int ldin, bf16* 
 }
 
 int pool(cudaStream_t st, const bf16* a, int ld_in, int C, bf16* b, int ld_out, int nc) {
-    k_pool<<<nb(vox3(nc) * C), TPB, 0, st>>>(a, ld_in, C, b, ld_out, nc);
+    k_pool<<<nb(vox3(nc) * C / 8), TPB, 0, st>>>(a, ld_in, C, b, ld_out, nc);
     STG_LAUNCH_CK();
     return STG_OK;
 }
 
 int up(cudaStream_t st, const bf16* a, int ld_in, int C, bf16* b, int ld_out, int nc) {
-    k_up<<<nb(vox3(2 * nc) * C), TPB, 0, st>>>(a, ld_in, C, b, ld_out, nc);
+    k_up<<<nb(vox3(2 * nc) * C / 8), TPB, 0, st>>>(a, ld_in, C, b, ld_out, nc);
     STG_LAUNCH_CK();
     return STG_OK;
 }
@@ -568,7 +614,7 @@ int net_forward(NetState& N, cudaStream_t st, int n) {
 
 // dy = relu'(y) * g as BF16 (ld C)
 int relu_grad(NetState& N, cudaStream_t st, const float* g, int ldg, const bf16* y, int ldy, int C, int n) {
-    k_relu_grad<<<nb(vox3(n) * C), TPB, 0, st>>>(g, ldg, y, ldy, C, vox3(n), N.dy);
+    k_relu_grad<<<nb(vox3(n) * C / 8), TPB, 0, st>>>(g, ldg, y, ldy, C, vox3(n), N.dy);
     STG_LAUNCH_CK();
     return STG_OK;
 }
@@ -602,7 +648,7 @@ int net_backward(NetState& N, cudaStream_t st, int n) {
     STG_TRY(relu_grad(N, st, N.G0b, c, N.a0d, c, c, n));
     STG_TRY(conv_dw(N, st, 8, N.cat0, 3 * c, n));
     STG_TRY(conv_dx(N, st, 8, N.G0cat, 3 * c, n));
-    k_up_bwd<<<nb(V1 * 2 * c), TPB, 0, st>>>(N.G0cat, 3 * c, 2 * c, N.G1a, 2 * c, n1);
+    k_up_bwd<<<nb(V1 * 2 * c / 4), TPB, 0, st>>>(N.G0cat, 3 * c, 2 * c, N.G1a, 2 * c, n1);
     STG_LAUNCH_CK();
     // level 1 decoder
     STG_TRY(relu_grad(N, st, N.G1a, 2 * c, N.b1d, 2 * c, 2 * c, n1));
@@ -611,7 +657,7 @@ int net_backward(NetState& N, cudaStream_t st, int n) {
     STG_TRY(relu_grad(N, st, N.G1b, 2 * c, N.a1d, 2 * c, 2 * c, n1));
     STG_TRY(conv_dw(N, st, 6, N.cat1, 6 * c, n1));
     STG_TRY(conv_dx(N, st, 6, N.G1cat, 6 * c, n1));
-    k_up_bwd<<<nb(V2 * 4 * c), TPB, 0, st>>>(N.G1cat, 6 * c, 4 * c, N.G2a, 4 * c, n2);
+    k_up_bwd<<<nb(V2 * 4 * c / 4), TPB, 0, st>>>(N.G1cat, 6 * c, 4 * c, N.G2a, 4 * c, n2);
     STG_LAUNCH_CK();
     // level 2
     STG_TRY(relu_grad(N, st, N.G2a, 4 * c, N.b2, 4 * c, 4 * c, n2));
@@ -620,7 +666,7 @@ int net_backward(NetState& N, cudaStream_t st, int n) {
     STG_TRY(relu_grad(N, st, N.G2b, 4 * c, N.a2, 4 * c, 4 * c, n2));
     STG_TRY(conv_dw(N, st, 4, N.p1, 2 * c, n2));
     STG_TRY(conv_dx(N, st, 4, N.G2a, 2 * c, n2));
-    k_pool_bwd<<<nb(V1 * 2 * c), TPB, 0, st>>>(N.G2a, 2 * c, 2 * c, N.G1cat + 4 * c, 6 * c, n2);
+    k_pool_bwd<<<nb(V1 * 2 * c / 4), TPB, 0, st>>>(N.G2a, 2 * c, 2 * c, N.G1cat + 4 * c, 6 * c, n2);
     STG_LAUNCH_CK();
     // level 1 encoder
     STG_TRY(relu_grad(N, st, N.G1cat + 4 * c, 6 * c, N.cat1 + 4 * c, 6 * c, 2 * c, n1));
@@ -629,7 +675,7 @@ int net_backward(NetState& N, cudaStream_t st, int n) {
     STG_TRY(relu_grad(N, st, N.G1a, 2 * c, N.a1, 2 * c, 2 * c, n1));
     STG_TRY(conv_dw(N, st, 2, N.p0, c, n1));
     STG_TRY(conv_dx(N, st, 2, N.G1b, c, n1));
-    k_pool_bwd<<<nb(V0 * c), TPB, 0, st>>>(N.G1b, c, c, N.G0cat + 2 * c, 3 * c, n1);
+    k_pool_bwd<<<nb(V0 * c / 4), TPB, 0, st>>>(N.G1b, c, c, N.G0cat + 2 * c, 3 * c, n1);
     STG_LAUNCH_CK();
     // level 0 encoder
     STG_TRY(relu_grad(N, st, N.G0cat + 2 * c, 3 * c, N.cat0 + 2 * c, 3 * c, c, n));
@@ -643,8 +689,11 @@ int net_backward(NetState& N, cudaStream_t st, int n) {
 // loss = mean (out - tgt)^2 into N.dloss (device) and dout
 int net_loss(NetState& N, cudaStream_t st, int n) {
     const long long cnt = vox3(n) * OUT_CH;
+    k_sumsq<<<NPART, TPB, 0, st>>>(vox3(n), reinterpret_cast<const float4*>(N.tgt), N.part);
+    STG_LAUNCH_CK();
+    STG_TRY(reduce_parts(st, N.part, NPART, N.dt2));
     const int blocks = (int)std::min<long long>(NPART, (cnt + TPB - 1) / TPB);
-    k_mse<<<blocks, TPB, 0, st>>>(N.out, N.tgt, cnt, N.dout, N.part);
+    k_mse<<<blocks, TPB, 0, st>>>(N.out, N.tgt, cnt, N.dt2, N.dout, N.part);
     STG_LAUNCH_CK();
     return reduce_parts(st, N.part, blocks, N.dloss);
 }

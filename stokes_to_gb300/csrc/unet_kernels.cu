@@ -11,6 +11,8 @@
 // A warp owns 16 voxels (the M side) and all output channels (N = C_out <= 64).
 #include <cuda_bf16.h>
 
+#include <algorithm>
+
 #include "internal.cuh"
 
 namespace stg {
@@ -188,17 +190,20 @@ __global__ void k_flip_weights(const __nv_bfloat16* __restrict__ w, int cout, in
 }
 
 // ---------------------------------------------------------------- tcgen05 forward
-// The same convolution on the 5th-generation tensor cores. A CTA owns J consecutive
-// j-lines of one i-plane (all k). It stages the halo box (3 planes x (J+2) lines x (n+2)
-// cells) of one 16-channel slice of the input in shared memory as K-major core matrices
-// without swizzle: row r = jj (n+2) + kk of plane p holds the 16 bytes of channels
-// [8g, 8g+8) at ((g 3 + p) R + r) 16, R = (J+2)(n+2). In this layout a tap (di,dj,dk) is a
-// uniform row shift, so one shared-memory descriptor per tap and M-tile addresses the
-// implicit-GEMM A operand (128 consecutive rows; rows that fall on halo columns are
-// computed and discarded). The weights of the slice sit beside it as [g][tap][C_out]
-// rows. One thread issues tcgen05.mma (M 128, N C_out, K 16, BF16 in, FP32 accumulators
-// in tensor memory) for every tap and M-tile, commits to an mbarrier, and the four warps
-// read the accumulators back with tcgen05.ld for the bias / ReLU / store epilogue.
+// The same convolution on the 5th-generation tensor cores, as an implicit GEMM (M voxels,
+// N = C_out, K = 27 taps x C_in). A CTA owns J consecutive j-lines (all k) of P
+// consecutive i-planes and marches along i. For each 16-channel slice of the input it
+// streams the P + 2 halo planes ((J+2) lines x (n+2) cells each) through a ring of four
+// shared-memory slots, as K-major core matrices without swizzle: in a slot, row
+// r = jj (n+2) + kk holds the 16 bytes of channels [8g, 8g+8) at (g R + r) 16,
+// R = (J+2)(n+2). In this layout a tap (di,dj,dk) is a uniform row shift within the slot
+// of plane i + di, so one shared-memory descriptor per tap and M-tile addresses the A
+// operand (128 consecutive rows; rows on halo columns are computed and discarded). The
+// slice's weights sit beside the ring as [g][tap][C_out] rows. One thread issues
+// tcgen05.mma (M 128, N C_out, K 16, BF16 in, FP32 accumulators in tensor memory, one
+// accumulator block per plane and M-tile) for plane i while the copies of plane i + 3 are
+// in flight, and commits to an mbarrier; at the end the four warps read the accumulators
+// with tcgen05.ld for the bias / ReLU / store epilogue.
 namespace tc {
 
 __device__ __forceinline__ uint32_t saddr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -257,25 +262,29 @@ __device__ __forceinline__ void ld16(uint32_t taddr, uint32_t (&v)[16]) {
 
 }  // namespace tc
 
-// Tile plan of the tcgen05 kernel for an n^3 grid: J lines per CTA, T M-tiles.
+// Tile plan of the tcgen05 kernel for an n^3 grid: J lines and P planes per CTA, T
+// M-tiles per plane, tensor-memory columns and dynamic shared memory.
 struct TcPlan {
-    int J = 0, T = 0, ncols = 0;
+    int J = 0, T = 0, P = 0, ncols = 0;
     size_t smem = 0;
 };
+
+constexpr int TC_RING = 4;
 
 template <int COUT, bool F32>
 __global__ void __launch_bounds__(128) k_conv3_tc(const __nv_bfloat16* __restrict__ in, int cin, int ldin,
                                                   const __nv_bfloat16* __restrict__ w, int wtap, const float* __restrict__ bias,
-                                                  void* __restrict__ outp, int ldout, int n, int relu, int J, int T, int ncols,
-                                                  int* __restrict__ err) {
+                                                  void* __restrict__ outp, int ldout, int n, int relu, int J, int T, int P,
+                                                  int ncols, int* __restrict__ err) {
     extern __shared__ __align__(128) uint8_t smem[];
     const int Hk = n + 2, R = (J + 2) * Hk;
-    uint8_t* sA = smem;
-    uint8_t* sB = smem + (size_t)96 * R;
+    const uint32_t slot_bytes = 32u * (uint32_t)R;
+    uint8_t* sB = smem + (size_t)TC_RING * slot_bytes;
     uint64_t* bar = reinterpret_cast<uint64_t*>(sB + 864 * COUT);
     uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + 1);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int i = blockIdx.x, j0 = blockIdx.y * J;
+    const int i0 = blockIdx.x * P, j0 = blockIdx.y * J;
+    const int np = min(P, n - i0);
     const uint32_t bar_a = tc::saddr(bar);
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(tc::saddr(tslot)), "r"(ncols)
@@ -290,81 +299,111 @@ __global__ void __launch_bounds__(128) k_conv3_tc(const __nv_bfloat16* __restric
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
     const uint32_t tbase = *tslot;
-    const uint32_t a0 = tc::saddr(sA), b0 = tc::saddr(sB);
-    const uint32_t lbo_a = 48u * (uint32_t)R, lbo_b = 432u * COUT;
+    const uint32_t a0 = tc::saddr(smem), b0 = tc::saddr(sB);
+    const uint32_t lbo_a = 16u * (uint32_t)R, lbo_b = 432u * COUT;
     constexpr uint32_t ID = tc::idesc_bf16(128, COUT);
     const int rlast = (J + 1) * Hk - 2 - 127;
-    uint32_t phase = 0;
+    uint32_t ncommit = 0;  // commits issued; each completes one mbarrier phase
     int bad = 0;
+
+    // halo plane hp (i = i0 - 1 + hp) of channel slice c0 into ring slot hp % 4: line by
+    // line, consecutive threads on consecutive 16-byte pieces
+    auto load_plane = [&](int hp, int c0) {
+        const int gi = i0 - 1 + hp;
+        const uint32_t sbase = a0 + (uint32_t)(hp % TC_RING) * slot_bytes;
+        for (int jj = 0; jj < J + 2; jj++) {
+            const int gj = j0 - 1 + jj;
+            const bool line_ok = gi >= 0 && gi < n && gj >= 0 && gj < n;
+            const __nv_bfloat16* lsrc = line_ok ? in + (size_t)(gi * n + gj) * n * ldin + c0 : in;
+            const uint32_t dst = sbase + 16u * (uint32_t)(jj * Hk);
+            for (int x = tid; x < 2 * Hk; x += 128) {
+                const int kk = x >> 1, g = x & 1;
+                const bool ok = line_ok && kk >= 1 && kk <= n;
+                tc::cp16(dst + 16u * (uint32_t)(g * R + kk), ok ? lsrc + (size_t)(kk - 1) * ldin + 8 * g : in, ok ? 16 : 0);
+            }
+        }
+    };
     const int nchunk = cin / 16;
     for (int ch = 0; ch < nchunk && !bad; ch++) {
         const int c0 = ch * 16;
-        if (ch > 0) {
-            // the previous slice's MMAs read sA / sB: wait for them before overwriting
-            bad = __syncthreads_or(!tc::wait_parity(bar_a, phase));
-            phase ^= 1;
+        // every MMA issued so far reads the ring or the weights: wait before refilling them
+        if (ncommit) {
+            bad = __syncthreads_or(!tc::wait_parity(bar_a, (ncommit - 1) & 1));
             if (bad) break;
-        }
-        for (int e = tid; e < 6 * R; e += 128) {
-            const int g = e / (3 * R), rem = e - g * 3 * R, p = rem / R, r = rem - p * R;
-            const int jj = r / Hk, kk = r - jj * Hk;
-            const int gi = i - 1 + p, gj = j0 - 1 + jj, gk = kk - 1;
-            const bool inside = gi >= 0 && gi < n && gj >= 0 && gj < n && gk >= 0 && gk < n;
-            const __nv_bfloat16* src = inside ? in + (size_t)((gi * n + gj) * n + gk) * ldin + c0 + 8 * g : in;
-            tc::cp16(a0 + 16u * e, src, inside ? 16 : 0);
         }
         for (int e = tid; e < 54 * COUT; e += 128) {
             const int g = e / (27 * COUT), rem = e - g * 27 * COUT, t = rem / COUT, co = rem - t * COUT;
             tc::cp16(b0 + 16u * e, w + (size_t)t * wtap + (size_t)co * cin + c0 + 8 * g, 16);
         }
-        asm volatile("cp.async.wait_all;\n" ::: "memory");
-        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-        __syncthreads();
-        if (tid == 0) {
-            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-            for (int t = 0; t < 27; t++) {
-                const int di = t / 9 - 1, dj = (t / 3) % 3 - 1, dk = t % 3 - 1;
-                const uint64_t bd = tc::sdesc(b0 + 16u * (uint32_t)(t * COUT), lbo_b, 128);
-                for (int q = 0; q < T; q++) {
-                    const int r0 = q < T - 1 ? Hk + 1 + 128 * q : rlast;
-                    const uint32_t row = (uint32_t)((1 + di) * R + r0 + dj * Hk + dk);
-                    tc::mma(tbase + (uint32_t)(q * COUT), tc::sdesc(a0 + 16u * row, lbo_a, 128), bd, ID, (ch > 0 || t > 0) ? 1u : 0u);
-                }
+        for (int hp = 0; hp < 3; hp++) {
+            load_plane(hp, c0);
+            asm volatile("cp.async.commit_group;\n" ::: "memory");
+        }
+        for (int ip = 0; ip < np; ip++) {
+            // halo plane ip + 3 takes the slot of plane ip - 1, which the MMAs of output
+            // plane ip - 1 (the last commit) read
+            if (ip > 0) {
+                bad = __syncthreads_or(!tc::wait_parity(bar_a, (ncommit - 1) & 1));
+                if (bad) break;
             }
-            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(bar_a) : "memory");
+            if (ip + 3 <= np + 1) load_plane(ip + 3, c0);
+            asm volatile("cp.async.commit_group;\n" ::: "memory");
+            asm volatile("cp.async.wait_group 1;\n" ::: "memory");  // halo planes <= ip + 2 have landed
+            asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+            __syncthreads();
+            if (tid == 0) {
+                asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+                for (int t = 0; t < 27; t++) {
+                    const int di = t / 9 - 1, dj = (t / 3) % 3 - 1, dk = t % 3 - 1;
+                    const uint64_t bd = tc::sdesc(b0 + 16u * (uint32_t)(t * COUT), lbo_b, 128);
+                    const uint32_t sb = a0 + (uint32_t)((ip + 1 + di) % TC_RING) * slot_bytes;
+                    for (int q = 0; q < T; q++) {
+                        const int r0 = q < T - 1 ? Hk + 1 + 128 * q : rlast;
+                        const uint32_t row = (uint32_t)(r0 + dj * Hk + dk);
+                        tc::mma(tbase + (uint32_t)((ip * T + q) * COUT), tc::sdesc(sb + 16u * row, lbo_a, 128), bd, ID,
+                                (ch > 0 || t > 0) ? 1u : 0u);
+                    }
+                }
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(bar_a)
+                             : "memory");
+            }
+            ncommit++;
         }
     }
-    if (!bad) bad = __syncthreads_or(!tc::wait_parity(bar_a, phase));
+    asm volatile("cp.async.wait_all;\n" ::: "memory");
+    if (!bad && ncommit) bad = __syncthreads_or(!tc::wait_parity(bar_a, (ncommit - 1) & 1));
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
     if (!bad) {
-        for (int q = 0; q < T; q++) {
-            const int r = (q < T - 1 ? Hk + 1 + 128 * q : rlast) + warp * 32 + lane;
-            const int jj = r / Hk, kk = r - jj * Hk;
-            const int gj = j0 - 1 + jj;
-            const bool valid = jj >= 1 && jj <= J && kk >= 1 && kk <= n && gj < n;
-            const size_t v = (size_t)(i * n + gj) * n + (kk - 1);
+        for (int ip = 0; ip < np; ip++) {
+            for (int q = 0; q < T; q++) {
+                const int r = (q < T - 1 ? Hk + 1 + 128 * q : rlast) + warp * 32 + lane;
+                const int jj = r / Hk, kk = r - jj * Hk;
+                const int gj = j0 - 1 + jj;
+                const bool valid = jj >= 1 && jj <= J && kk >= 1 && kk <= n && gj < n;
+                const size_t v = ((size_t)(i0 + ip) * n + gj) * n + (kk - 1);
 #pragma unroll
-            for (int cb = 0; cb < COUT; cb += 16) {
-                uint32_t x[16];
-                tc::ld16(tbase + ((uint32_t)(warp * 32) << 16) + (uint32_t)(q * COUT + cb), x);
-                if (valid) {
-                    float y[16];
+                for (int cb = 0; cb < COUT; cb += 16) {
+                    uint32_t x[16];
+                    tc::ld16(tbase + ((uint32_t)(warp * 32) << 16) + (uint32_t)((ip * T + q) * COUT + cb), x);
+                    if (valid) {
+                        float y[16];
 #pragma unroll
-                    for (int u = 0; u < 16; u++) {
-                        y[u] = __uint_as_float(x[u]) + (bias ? bias[cb + u] : 0.f);
-                        if (relu) y[u] = fmaxf(y[u], 0.f);
-                    }
-                    if (F32) {
-                        float4* o = reinterpret_cast<float4*>(static_cast<float*>(outp) + v * ldout + cb);
+                        for (int u = 0; u < 16; u++) {
+                            y[u] = __uint_as_float(x[u]) + (bias ? bias[cb + u] : 0.f);
+                            if (relu) y[u] = fmaxf(y[u], 0.f);
+                        }
+                        if (F32) {
+                            float4* o = reinterpret_cast<float4*>(static_cast<float*>(outp) + v * ldout + cb);
 #pragma unroll
-                        for (int u = 0; u < 4; u++) o[u] = make_float4(y[4 * u], y[4 * u + 1], y[4 * u + 2], y[4 * u + 3]);
-                    } else {
-                        __align__(16) __nv_bfloat162 h[8];
+                            for (int u = 0; u < 4; u++) o[u] = make_float4(y[4 * u], y[4 * u + 1], y[4 * u + 2], y[4 * u + 3]);
+                        } else {
+                            __align__(16) __nv_bfloat162 hh[8];
 #pragma unroll
-                        for (int u = 0; u < 8; u++) h[u] = __floats2bfloat162_rn(y[2 * u], y[2 * u + 1]);
-                        uint4* o = reinterpret_cast<uint4*>(static_cast<__nv_bfloat16*>(outp) + v * ldout + cb);
-                        o[0] = reinterpret_cast<const uint4*>(h)[0];
-                        o[1] = reinterpret_cast<const uint4*>(h)[1];
+                            for (int u = 0; u < 8; u++) hh[u] = __floats2bfloat162_rn(y[2 * u], y[2 * u + 1]);
+                            uint4* o = reinterpret_cast<uint4*>(static_cast<__nv_bfloat16*>(outp) + v * ldout + cb);
+                            o[0] = reinterpret_cast<const uint4*>(hh)[0];
+                            o[1] = reinterpret_cast<const uint4*>(hh)[1];
+                        }
                     }
                 }
             }
@@ -377,35 +416,41 @@ __global__ void __launch_bounds__(128) k_conv3_tc(const __nv_bfloat16* __restric
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tbase), "r"(ncols) : "memory");
 }
 
-constexpr size_t TC_SMEM_MAX = 200 * 1024;
+constexpr size_t TC_SMEM_MAX = 227 * 1024;
+constexpr size_t TC_SMEM_TWO = 110 * 1024;  // at most this much: two CTAs per SM
+// requests at least this much so that no more than two (tier 0) or one (tier 1) CTAs share
+// an SM's 512 tensor-memory columns (an SM has 228 KB of shared memory, 1 KB kept per CTA)
+constexpr size_t TC_FLOOR_TWO = 78 * 1024, TC_FLOOR_ONE = 118 * 1024;
 
-// J (lines per CTA) with the most useful rows per M-tile row, within the shared memory
-// and tensor-memory budgets (two CTAs per SM, else one); J = 0 when no plan fits (small
-// grids use the mma.sync kernel)
+// J with the most useful rows per M-tile row, then as many planes per CTA as the tensor
+// memory holds (256 columns with two CTAs per SM, 512 with one); J = 0 when no plan fits
+// (small grids use the mma.sync kernel)
 TcPlan tc_plan(int n, int cout) {
     TcPlan best;
     for (int tier = 0; tier < 2 && !best.J; tier++) {
-        const size_t budget = tier == 0 ? 110 * 1024 : TC_SMEM_MAX;
+        const size_t budget = tier == 0 ? TC_SMEM_TWO : TC_SMEM_MAX;
         const int max_cols = tier == 0 ? 256 : 512;
         double best_eff = 0;
         for (int J = 1; J <= n; J++) {
             const int Hk = n + 2, rows = J * Hk - 2;
             if (rows < 128) continue;
             const int T = (rows + 127) / 128;
-            const size_t smem = (size_t)96 * (J + 2) * Hk + 864 * (size_t)cout + 16;
+            const size_t smem = (size_t)TC_RING * 32 * (J + 2) * Hk + 864 * (size_t)cout + 16;
             if (smem > budget || T * cout > max_cols) break;
             const double eff = (double)J * n / (128.0 * T);
             if (eff > best_eff + 1e-9) {
                 best_eff = eff;
                 best.J = J;
                 best.T = T;
-                best.smem = smem;
+                best.P = std::min(n, max_cols / (T * cout));
+                // one CTA per SM in the second tier: ask for more than half the SM's memory
+                best.smem = std::max(smem, tier == 0 ? TC_FLOOR_TWO : TC_FLOOR_ONE);
             }
         }
     }
     if (best.J) {
         int c = 32;
-        while (c < best.T * cout) c <<= 1;
+        while (c < best.P * best.T * cout) c <<= 1;
         best.ncols = c;
     }
     return best;
@@ -419,8 +464,8 @@ int launch_tc(const TcPlan& P, cudaStream_t st, const __nv_bfloat16* in, int cin
         STG_CK(cudaFuncSetAttribute(k_conv3_tc<C, F32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM_MAX));
         attr = true;
     }
-    dim3 grid(n, (n + P.J - 1) / P.J);
-    k_conv3_tc<C, F32><<<grid, 128, P.smem, st>>>(in, cin, ldin, w, wtap, bias, out, ldout, n, relu, P.J, P.T, P.ncols, err);
+    dim3 grid((n + P.P - 1) / P.P, (n + P.J - 1) / P.J);
+    k_conv3_tc<C, F32><<<grid, 128, P.smem, st>>>(in, cin, ldin, w, wtap, bias, out, ldout, n, relu, P.J, P.T, P.P, P.ncols, err);
     return STG_OK;
 }
 

@@ -39,7 +39,7 @@ def torch_net(p, inp, target, c=16):
     b0d = cv(9, cv(8, torch.cat([up(b1d), s0], 1)))
     out = torch.einsum("bcijk,oc->bijko", b0d, hw) + hb
     t = torch.tensor(target, dtype=torch.float64).reshape(1, n, n, n, 4)
-    loss = ((out - t) ** 2).mean()
+    loss = ((out - t) ** 2).sum() / (t ** 2).sum()
     loss.backward()
     return out.detach().numpy().reshape(-1, 4), float(loss.detach()), P.grad.numpy()
 
