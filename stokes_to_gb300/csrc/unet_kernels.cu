@@ -193,7 +193,7 @@ __global__ void k_flip_weights(const __nv_bfloat16* __restrict__ w, int cout, in
 // The same convolution on the 5th-generation tensor cores, as an implicit GEMM (M voxels,
 // N = C_out, K = 27 taps x C_in). A CTA owns J consecutive j-lines (all k) of P
 // consecutive i-planes and marches along i. For each 16-channel slice of the input it
-// streams the P + 2 halo planes ((J+2) lines x (n+2) cells each) through a ring of four
+// streams the P + 2 halo planes ((J+2) lines x (n+2) cells each) through a ring of five
 // shared-memory slots, as K-major core matrices without swizzle: in a slot, row
 // r = jj (n+2) + kk holds the 16 bytes of channels [8g, 8g+8) at (g R + r) 16,
 // R = (J+2)(n+2). In this layout a tap (di,dj,dk) is a uniform row shift within the slot
@@ -201,9 +201,10 @@ __global__ void k_flip_weights(const __nv_bfloat16* __restrict__ w, int cout, in
 // operand (128 consecutive rows; rows on halo columns are computed and discarded). The
 // slice's weights sit beside the ring as [g][tap][C_out] rows. One thread issues
 // tcgen05.mma (M 128, N C_out, K 16, BF16 in, FP32 accumulators in tensor memory, one
-// accumulator block per plane and M-tile) for plane i while the copies of plane i + 3 are
-// in flight, and commits to an mbarrier; at the end the four warps read the accumulators
-// with tcgen05.ld for the bias / ReLU / store epilogue.
+// accumulator block per plane and M-tile) for plane i while the copies of plane i + 3 and
+// the MMAs of plane i - 1 are in flight, and commits to one of two mbarriers; at the end
+// the four warps read the accumulators with tcgen05.ld for the bias / ReLU / store
+// epilogue.
 namespace tc {
 
 __device__ __forceinline__ uint32_t saddr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -269,7 +270,7 @@ struct TcPlan {
     size_t smem = 0;
 };
 
-constexpr int TC_RING = 4;
+constexpr int TC_RING = 5;
 
 template <int COUT, bool F32>
 __global__ void __launch_bounds__(128) k_conv3_tc(const __nv_bfloat16* __restrict__ in, int cin, int ldin,
@@ -280,8 +281,8 @@ __global__ void __launch_bounds__(128) k_conv3_tc(const __nv_bfloat16* __restric
     const int Hk = n + 2, R = (J + 2) * Hk;
     const uint32_t slot_bytes = 32u * (uint32_t)R;
     uint8_t* sB = smem + (size_t)TC_RING * slot_bytes;
-    uint64_t* bar = reinterpret_cast<uint64_t*>(sB + 864 * COUT);
-    uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + 1);
+    uint64_t* bar = reinterpret_cast<uint64_t*>(sB + 864 * COUT);  // two mbarriers: commits alternate
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + 2);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int i0 = blockIdx.x * P, j0 = blockIdx.y * J;
     const int np = min(P, n - i0);
@@ -293,6 +294,7 @@ __global__ void __launch_bounds__(128) k_conv3_tc(const __nv_bfloat16* __restric
     }
     if (tid == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar_a) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar_a + 8u) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     }
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
@@ -303,7 +305,10 @@ __global__ void __launch_bounds__(128) k_conv3_tc(const __nv_bfloat16* __restric
     const uint32_t lbo_a = 16u * (uint32_t)R, lbo_b = 432u * COUT;
     constexpr uint32_t ID = tc::idesc_bf16(128, COUT);
     const int rlast = (J + 1) * Hk - 2 - 127;
-    uint32_t ncommit = 0;  // commits issued; each completes one mbarrier phase
+    // commit c goes to mbarrier c & 1 and completes its phase (c >> 1) & 1; a wait is only
+    // ever made for the latest commit of its barrier, so the parity is unambiguous
+    uint32_t ncommit = 0;
+    auto commit_done = [&](uint32_t c) { return tc::wait_parity(bar_a + 8u * (c & 1u), (c >> 1) & 1u); };
     int bad = 0;
 
     // halo plane hp (i = i0 - 1 + hp) of channel slice c0 into ring slot hp % 4: line by
@@ -328,7 +333,7 @@ __global__ void __launch_bounds__(128) k_conv3_tc(const __nv_bfloat16* __restric
         const int c0 = ch * 16;
         // every MMA issued so far reads the ring or the weights: wait before refilling them
         if (ncommit) {
-            bad = __syncthreads_or(!tc::wait_parity(bar_a, (ncommit - 1) & 1));
+            bad = __syncthreads_or(!(commit_done(ncommit - 1) && (ncommit < 2 || commit_done(ncommit - 2))));
             if (bad) break;
         }
         for (int e = tid; e < 54 * COUT; e += 128) {
@@ -340,10 +345,10 @@ __global__ void __launch_bounds__(128) k_conv3_tc(const __nv_bfloat16* __restric
             asm volatile("cp.async.commit_group;\n" ::: "memory");
         }
         for (int ip = 0; ip < np; ip++) {
-            // halo plane ip + 3 takes the slot of plane ip - 1, which the MMAs of output
-            // plane ip - 1 (the last commit) read
-            if (ip > 0) {
-                bad = __syncthreads_or(!tc::wait_parity(bar_a, (ncommit - 1) & 1));
+            // halo plane ip + 3 takes the slot of plane ip - 2, which output planes ip - 3
+            // and ip - 2 read: wait for the commit of ip - 2 (output ip - 1 may still run)
+            if (ip >= 2) {
+                bad = __syncthreads_or(!commit_done(ncommit - 2));
                 if (bad) break;
             }
             if (ip + 3 <= np + 1) load_plane(ip + 3, c0);
@@ -364,14 +369,15 @@ __global__ void __launch_bounds__(128) k_conv3_tc(const __nv_bfloat16* __restric
                                 (ch > 0 || t > 0) ? 1u : 0u);
                     }
                 }
-                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(bar_a)
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                                 bar_a + 8u * (ncommit & 1u))
                              : "memory");
             }
             ncommit++;
         }
     }
     asm volatile("cp.async.wait_all;\n" ::: "memory");
-    if (!bad && ncommit) bad = __syncthreads_or(!tc::wait_parity(bar_a, (ncommit - 1) & 1));
+    if (!bad && ncommit) bad = __syncthreads_or(!(commit_done(ncommit - 1) && (ncommit < 2 || commit_done(ncommit - 2))));
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
     if (!bad) {
         for (int ip = 0; ip < np; ip++) {
@@ -435,7 +441,7 @@ TcPlan tc_plan(int n, int cout) {
             const int Hk = n + 2, rows = J * Hk - 2;
             if (rows < 128) continue;
             const int T = (rows + 127) / 128;
-            const size_t smem = (size_t)TC_RING * 32 * (J + 2) * Hk + 864 * (size_t)cout + 16;
+            const size_t smem = (size_t)TC_RING * 32 * (J + 2) * Hk + 864 * (size_t)cout + 32;
             if (smem > budget || T * cout > max_cols) break;
             const double eff = (double)J * n / (128.0 * T);
             if (eff > best_eff + 1e-9) {
