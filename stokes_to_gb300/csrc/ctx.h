@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_bf16.h>
 
+#include <functional>
 #include <vector>
 
 #include "kernels.h"
@@ -28,6 +29,20 @@ struct Level {
 
 using stg::DenseCoarse;
 using stg::Level;
+
+// A captured launch sequence (CUDA graph) and the configuration it was captured for.
+struct GraphCache {
+    bool enabled = true;
+    cudaGraphExec_t exec = nullptr;
+    long long key = -1, seen = -1, kernels = 0;
+    std::vector<int> cur;  // ping-pong state of each level after the sequence
+    void release() {
+        if (exec) cudaGraphExecDestroy(exec);
+        exec = nullptr;
+        key = -1;
+    }
+    ~GraphCache() { release(); }
+};
 
 // Per-kernel-class CUDA-event timing on the handle's stream.
 struct Prof {
@@ -86,6 +101,7 @@ struct stg_ctx {
     int (*finish)(stg_t*, const stg::d4* b, stg::d4* x) = nullptr;  // optional, after the refinement loop
     struct Ctx2* c2 = nullptr;        // 2D state (dim == 2)
     struct MmaState* mma = nullptr;   // MMA optimizer state (mma.cu), created on first use
+    GraphCache vgraph;                // the V-cycle below the finest level (3D) or all of it (2D)
     struct NetState* net = nullptr;   // learned preconditioner (unet.cu), stg_net_init
     bool net_on = false;              // LEARNED: the network is in use in the current refinement step
 };
@@ -118,6 +134,8 @@ int apply_op2d(stg_t* h, int op, int level, double* out, const double* in);
 int level_descr2d(stg_t* h, int level, double* vol, double* pen, uint8_t* fixed);
 
 Level& fine(stg_t* h);
+// runs body() through a CUDA-graph cache (solver.cu)
+int graphed(stg_t* h, GraphCache& G, long long key, const std::function<int()>& body, const std::function<void(bool)>& state);
 bool fast(const stg_t* h, const Level& L);
 // one V-cycle out = M(rhs) and y = A x on the finest level (FP32, solver.cu)
 int precond3(stg_t* h, const float4* rhs, float4* out);

@@ -110,6 +110,7 @@ int cuda_fail(cudaError_t e, const char* what, const char* file, int line);
     } while (0)
 // every kernel launch site checks the launch and counts it
 void count_launch();
+void add_launches(long long k);
 #define STG_LAUNCH_CK()            \
     do {                           \
         ::stg::count_launch();     \

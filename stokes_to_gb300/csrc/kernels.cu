@@ -41,14 +41,16 @@ __global__ void __launch_bounds__(TPB) k_op64(Geom g, double vol, const d4* __re
         int i, j, k;
         g.box_ijk(t, i, j, k);
         int s = g.slot(i, j, k);
-        double o[4];
-        if (LAP)
+        double o[4] = {0.0, 0.0, 0.0, 0.0};
+        if (MODE == 3)
+            ;  // x = 0
+        else if (LAP)
             lap_rows<double>(x, P, s, g.di(), g.dj(), vol, o);
         else if (MODE == 2)
             apply_rows<double, true>(x, m, P, s, g.di(), g.dj(), vol, o);
         else
             apply_rows<double, false>(x, m, P, s, g.di(), g.dj(), vol, o);
-        if (MODE == 1) {
+        if (MODE == 1 || MODE == 3) {
             double bp, bu, bv, bw;
             load4(b, s, bp, bu, bv, bw);
             o[0] = bp - o[0];
@@ -57,7 +59,7 @@ __global__ void __launch_bounds__(TPB) k_op64(Geom g, double vol, const d4* __re
             o[3] = bw - o[3];
         }
         if (LAP) mask4<double>(__ldg(m + s), o);
-        if (MODE == 1) {
+        if (MODE == 1 || MODE == 3) {
             acc = o[0] * o[0] + o[1] * o[1] + o[2] * o[2] + o[3] * o[3];
         } else if (MODE == 2) {
             double xp, xu, xv, xw;
@@ -470,6 +472,10 @@ int op64(cudaStream_t st, const Geom& g, double vol, const d4* x, const uint8_t*
         k_op64<0, true><<<nb, TPB, 0, st>>>(g, vol, x, m, P, b, out, part);
     else if (mode == 0)
         k_op64<0, false><<<nb, TPB, 0, st>>>(g, vol, x, m, P, b, out, part);
+    else if (mode == 1 && !x && lap)  // r = b with x = 0: no operator pass
+        k_op64<3, true><<<nb, TPB, 0, st>>>(g, vol, x, m, P, b, out, part);
+    else if (mode == 1 && !x)
+        k_op64<3, false><<<nb, TPB, 0, st>>>(g, vol, x, m, P, b, out, part);
     else if (mode == 1 && lap)
         k_op64<1, true><<<nb, TPB, 0, st>>>(g, vol, x, m, P, b, out, part);
     else if (mode == 1)

@@ -8,7 +8,7 @@
 namespace stg {
 
 // ---------------------------------------------------------------- operators (kernels.cu)
-// mode: 0 out = A x, 1 out = b - A x, 2 out = E x. If part != nullptr, each block writes
+// mode: 0 out = A x, 1 out = b - A x (x == nullptr: x = 0), 2 out = E x. If part != nullptr, each block writes
 // its partial sum of out.out (mode 1) or x.out (mode 2) to part[blockIdx.x] (FP64).
 // lap (modes 0 and 1): Laplacian form of A (stencil.cuh) for x zero on fixed unknowns,
 // rows of fixed unknowns 0. Every operator below takes the same switch; the solver sets

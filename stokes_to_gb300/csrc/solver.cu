@@ -17,6 +17,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <functional>
 #include <vector>
 
 #include "ctx.h"
@@ -27,6 +28,7 @@ static thread_local char g_err[512] = "";
 static std::atomic<long long> g_launches{0};
 
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+void add_launches(long long k) { g_launches.fetch_add(k, std::memory_order_relaxed); }
 
 void set_error(const char* fmt, ...) {
     va_list ap;
@@ -190,12 +192,13 @@ int smooth(stg_t* h, Level& L, const float4* r, bool post, bool x_is_zero) {
     return STG_OK;
 }
 
-// MultigridSolve::Vcycle (common_cpx/MultigridSolve.cpp:73-106) from a zero guess; the
-// finest right-hand side is `rhs`, the result is left in fine(h).x().
-int vcycle(stg_t* h, const float4* rhs) {
+// MultigridSolve::Vcycle (common_cpx/MultigridSolve.cpp:73-106) from a zero guess on levels
+// top .. 0: level i < L - 1 takes its right-hand side from its own r; the finest level's is
+// `rhs`. The result is left in lv[top].x().
+int vcycle_levels(stg_t* h, int top, const float4* rhs) {
     const bool mixed = h->opts.method == STG_METHOD_MIXED;
     const int L = h->L;
-    for (int i = L - 1; i >= 1; i--) {
+    for (int i = top; i >= 1; i--) {
         Level& F = h->lv[i];
         const float4* r = (i == L - 1) ? rhs : F.r;
         F.cur = 0;
@@ -206,7 +209,7 @@ int vcycle(stg_t* h, const float4* rhs) {
     Level& C0 = h->lv[0];
     C0.cur = 0;
     PROF(h, 7, 0.0, dense_apply32(h->st, h->dense, C0.g, L == 1 ? rhs : C0.r, C0.x()));
-    for (int i = 1; i < L; i++) {
+    for (int i = 1; i <= top; i++) {
         Level& F = h->lv[i];
         Level& C = h->lv[i - 1];
         const float4* r = (i == L - 1) ? rhs : F.r;
@@ -221,11 +224,95 @@ int vcycle(stg_t* h, const float4* rhs) {
     return STG_OK;
 }
 
+// Runs body() through the graph cache G: a launch sequence that touches only fixed
+// buffers is captured into a CUDA graph on its second call with the same configuration
+// `key` (the first runs normally, so one-time set-up such as kernel attributes happens
+// outside the capture) and replayed on later calls. state(true) records the host-side state
+// the sequence leaves, state(false) restores it after a replay. Off while the per-kernel
+// profiler is on.
+int graphed(stg_t* h, GraphCache& G, long long key, const std::function<int()>& body, const std::function<void(bool)>& state) {
+    if (h->prof.on || !G.enabled) return body();
+    if (G.exec && G.key == key) {
+        STG_CK(cudaGraphLaunch(G.exec, h->st));
+        add_launches(G.kernels);
+        state(false);
+        return STG_OK;
+    }
+    if (G.seen != key) {
+        G.seen = key;
+        return body();
+    }
+    G.release();
+    cudaGraph_t graph = nullptr;
+    STG_CK(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
+    const long long l0 = stg_kernel_launches();
+    const int rc = body();
+    const cudaError_t e = cudaStreamEndCapture(h->st, &graph);
+    if (rc != STG_OK) {
+        if (graph) cudaGraphDestroy(graph);
+        return rc;
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture", __FILE__, __LINE__);
+    G.kernels = stg_kernel_launches() - l0;  // counted during the capture: they stand for the first replay
+    const cudaError_t e2 = cudaGraphInstantiate(&G.exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e2 != cudaSuccess) {
+        G.exec = nullptr;
+        return cuda_fail(e2, "cudaGraphInstantiate", __FILE__, __LINE__);
+    }
+    G.key = key;
+    state(true);
+    STG_CK(cudaGraphLaunch(G.exec, h->st));
+    return STG_OK;
+}
+
+// The levels below the finest touch only their own buffers, so their part of the V-cycle is
+// the same launch sequence on every call and runs as a replayed CUDA graph.
+int coarse_cycle(stg_t* h) {
+    const int top = h->L - 2;
+    const int per = h->reference_cycle ? 2 : std::max(1, std::min(4, h->opts.smooth_sweeps));
+    // the coarsest inverse lives in one of two buffers (fixed per handle): part of the key
+    const long long key = (long long)per | ((long long)(h->opts.method == STG_METHOD_MIXED) << 3) |
+                          ((long long)fast(h, h->lv[top]) << 4) | ((long long)(h->dense.inv == h->dense.Ainv) << 5) |
+                          ((long long)h->L << 6);
+    GraphCache& G = h->vgraph;
+    return graphed(h, G, key, [&] { return vcycle_levels(h, top, nullptr); },
+                   [&](bool save) {
+                       if (save) {
+                           G.cur.assign(top + 1, 0);
+                           for (int i = 0; i <= top; i++) G.cur[i] = h->lv[i].cur;
+                       } else {
+                           for (int i = 0; i <= top; i++) h->lv[i].cur = G.cur[i];
+                       }
+                   });
+}
+
+// MultigridSolve::Vcycle (common_cpx/MultigridSolve.cpp:73-106) from a zero guess; the
+// finest right-hand side is `rhs`, the result is left in fine(h).x().
+int vcycle(stg_t* h, const float4* rhs) {
+    const int L = h->L;
+    if (L == 1) return vcycle_levels(h, 0, rhs);
+    const bool mixed = h->opts.method == STG_METHOD_MIXED;
+    Level& F = h->lv[L - 1];
+    Level& C = h->lv[L - 2];
+    F.cur = 0;
+    STG_TRY(smooth(h, F, rhs, false, true));
+    PROF(h, 2, 49.0 * F.g.box() + 17.0 * C.g.box(), restrict_resid32(h->st, C.g, F.g, (float)F.vol, rhs, F.x(), F.m, F.P32, C.m, C.r, fast(h, F)));
+    STG_TRY(coarse_cycle(h));
+    if (mixed) {
+        PROF(h, 3, 24.0 * C.g.box(), to_bf16(h->st, C.g, C.x(), C.xbf));
+        PROF(h, 3, 8.0 * C.g.box() + 33.0 * F.g.box(), prolong_add_bf16(h->st, F.g, C.g, C.xbf, F.m, F.x()));
+    } else {
+        PROF(h, 3, 16.0 * C.g.box() + 33.0 * F.g.box(), prolong_add32(h->st, F.g, C.g, C.x(), F.m, F.x()));
+    }
+    return smooth(h, F, rhs, true, false);
+}
+
 // ---------------------------------------------------------------- FP64 refinement + FGMRES
 int residual64(stg_t* h, const d4* b, const d4* x, d4* r, double* nrm2_host) {
     Level& F = fine(h);
     int nb = 0;
-    PROF(h, 5, 129.0 * F.g.box(), op64(h->st, F.g, F.vol, x, F.m, F.P64, b, r, 1, h->d_parts, &nb, fast(h, F)));
+    PROF(h, 5, (x ? 129.0 : 65.0) * F.g.box(), op64(h->st, F.g, F.vol, x, F.m, F.P64, b, r, 1, h->d_parts, &nb, fast(h, F)));
     STG_TRY(reduce_parts(h->st, h->d_parts, nb, h->dnrm));
     STG_CK(cudaMemcpyAsync(nrm2_host, h->dnrm, sizeof(double), cudaMemcpyDeviceToHost, h->st));
     STG_CK(cudaStreamSynchronize(h->st));
@@ -314,9 +401,11 @@ int solve_core(stg_t* h, const d4* b, d4* x, stg_stats* stats) {
     std::vector<double> H((size_t)(m + 1) * m), cs(m), sn(m), g(m + 1), y(m), hcol(m + 2), sig(m + 1);
     double rel = 0, rn = 0;
     int status = STG_E_NOT_CONVERGED;
+    // a zero start makes the first residual b itself (fixed rows cleared in the Laplacian form)
+    const bool x_zero = !(h->opts.warm_start && h->has_x0(x));
     for (int outer = 0; outer <= h->opts.max_outer; outer++) {
         double rn2 = 0;
-        STG_TRY(h->resid64(h, b, x, h->r64, &rn2));
+        STG_TRY(h->resid64(h, b, (outer == 0 && x_zero && h->dim == 3) ? nullptr : x, h->r64, &rn2));
         rn = std::sqrt(rn2);
         rel = bn > 0 ? rn / bn : 0.0;
         if (!std::isfinite(rn)) {

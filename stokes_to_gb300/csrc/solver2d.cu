@@ -613,7 +613,8 @@ int precond2(stg_t* h, const float4* rhs, float4* out) {
     const int n = F.g.size();
     STG_CK(cudaMemcpyAsync(F.r, rhs, sizeof(float) * n, cudaMemcpyDeviceToDevice, h->st));
     STG_CK(cudaMemsetAsync(F.x, 0, sizeof(float) * n, h->st));
-    STG_TRY(vcycle2(h));
+    // the V-cycle works on the level buffers only: replayed as a CUDA graph
+    STG_TRY(graphed(h, h->vgraph, 1, [&] { return vcycle2(h); }, [](bool) {}));
     STG_CK(cudaMemcpyAsync(out, F.x, sizeof(float) * n, cudaMemcpyDeviceToDevice, h->st));
     return STG_OK;
 }
