@@ -190,6 +190,28 @@ def ncu_traffic():
     return out
 
 
+def design_loop_2d(driver, iters=20):
+    """Runs the fluid_topo driver on the 2D 64^2 problem (no frames written) and returns
+    the median time per design iteration (two solves, sensitivity, filter, OC update) over
+    iterations 1..iters-1, from the driver's own log."""
+    import tempfile
+
+    with tempfile.TemporaryDirectory() as d:
+        cmd = [driver, "-driver", "0", "-test", "1", "-s", "64", "-frac", "0.3", "-lf", str(iters), "-frames", "0",
+               "-o", d]
+        r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True)
+        if r.returncode != 0:
+            return {"error": r.stderr.strip()[-300:]}
+        log = np.genfromtxt(os.path.join(d, "log.csv"), delimiter=",", names=True)
+    it_ms = np.atleast_1d(log["iteration_ms"])
+    vc = np.atleast_1d(log["v_cycles_forward"]) + np.atleast_1d(log["v_cycles_adjoint"])
+    return {"workload": "2D 64^2 design loop (fluid_topo -driver 0 -test 1 -s 64 -frac 0.3), OC, filter 1.5, solves to 1e-10",
+            "iterations": int(iters), "total_s": round(float(np.sum(it_ms)) / 1e3, 3),
+            "ms_per_iteration_median": round(float(np.median(it_ms[1:])), 3),
+            "v_cycles_per_iteration_median": float(np.median(vc[1:])),
+            "final_objective": float(np.atleast_1d(log["objective"])[-1])}
+
+
 # ------------------------------------------------------------------ reference (CPU) arm
 def cpu_reference_sample(sample_n=64):
     """The reference algorithm restated on the CPU (GMRES with the reference V-cycle: Vanka
@@ -393,6 +415,12 @@ def run_ours(args):
         methods["learned"] = r
         sv.close()
 
+    # ---- the 2D 64^2 design loop (fluid_topo -driver 0 -test 1: parabolic inlet, uniform 0.3
+    # start, filter 1.5, OC, solves to 1e-10), the latency-bound configuration
+    loop2d = None
+    if rank == 0 and world == 1 and not args.no_methods:
+        loop2d = design_loop_2d(build.DRIVER)
+
     # ---- roofline of the dominant kernel class, measured over the timed region
     peak, peak_kind = measured_peak()
     dom = max((k for k in prof if prof[k]["launches"]), key=lambda k: prof[k]["ms"])
@@ -432,6 +460,7 @@ def run_ours(args):
             "solver": {"v_cycles_per_solve": vc, "outer_per_solve": statistics.mean(st["outer_iters"] for st in stats),
                        "final_rel_residual_max": max(st["rel_residual"] for st in stats)},
             "methods": methods,
+            "design_loop_2d": loop2d,
             "kernels": kernel_table,
         }
         print(json.dumps(line), flush=True)

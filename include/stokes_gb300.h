@@ -50,7 +50,7 @@ typedef struct stg_opts {
     int method;          /* STG_METHOD_* */
     double tol;          /* FP64 true relative residual ||b-Ax||/||b|| to reach */
     int max_outer;       /* FP64 refinement steps */
-    int inner_max;       /* FGMRES basis size of one refinement step */
+    int inner_max;       /* FGMRES basis size of one refinement step (2D: at least 60) */
     double inner_tol;    /* relative reduction asked of one refinement step */
     int verbose;         /* print per-iteration residuals to stderr */
     int smooth_sweeps;   /* sweeps per colour in the solver's smoother: 1 (default; 0 means

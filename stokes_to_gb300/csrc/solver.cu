@@ -469,7 +469,15 @@ int solve_core(stg_t* h, const d4* b, d4* x, stg_stats* stats) {
                 set_error("non-finite Arnoldi norm");
                 break;
             }
-            if (nw2 > 0) {
+            if (nw2 > 1e8 || (nw2 > 0 && nw2 < 1e-8)) {
+                // the unnormalised basis drifts in scale by the gain of A M each step (large
+                // for a weak preconditioner on high-contrast designs): renormalise before FP32
+                // over- or underflows
+                PROF(h, 6, 32.0 * n4, scale32(h->st, n4, h->V[j + 1], h->dnrm, h->V[j + 1]));
+                sig[j + 1] = 1.0;
+                const double one1 = 1.0;
+                STG_CK(cudaMemcpyAsync(h->dsig2 + j + 1, &one1, sizeof(double), cudaMemcpyHostToDevice, h->st));
+            } else if (nw2 > 0) {
                 sig[j + 1] = 1.0 / std::sqrt(nw2);
                 const double s2 = 1.0 / nw2;
                 STG_CK(cudaMemcpyAsync(h->dsig2 + j + 1, &s2, sizeof(double), cudaMemcpyHostToDevice, h->st));
@@ -663,7 +671,9 @@ int stg_create(int dim, int n, const stg_opts* opts, stg_t** out) {
         stg_default_opts(&h->opts);
     if (h->opts.inner_max < 1) h->opts.inner_max = 1;
     if (h->opts.smooth_sweeps < 1) h->opts.smooth_sweeps = 1;  // unset: the default
-    h->m = h->opts.inner_max;
+    // 2D vectors are small: keep at least the reference GMRES's 60-vector basis there (high-
+    // contrast 2D designs need long Krylov runs per refinement step)
+    h->m = dim == 2 ? std::max(h->opts.inner_max, 60) : h->opts.inner_max;
     h->L = dim == 3 ? level_count(n) : 0;
     int rc = STG_OK;
     auto fail = [&](int r) {

@@ -10,12 +10,17 @@ ref_grid2d_index.npz   the 2D blocked-layout tables produced by the reference's 
                        host code (oracle/_ref/libref_grid2d.so).
 oracle2d_n16.npz       2D oracle outputs on a seeded 16^2 problem (same contents as the
                        3D fixture).
+oracle_loop2d_n64.npz  the oracle's 20-iteration design loop of the 2D 64^2 benchmark case
+                       (parabolic inlet on a centred 16-cell segment, uniform 0.3 start,
+                       volume fraction 0.3, BP law, filter radius 1.5, OC with move limit 0.2,
+                       every solve to FP64 relative residual 1e-11): objective per iteration
+                       and the design of the last iteration (before its update).
 ref_mma.npz            six updates of the reference's own MMA solver (oracle/_ref/libref_mma.so,
                        built from simplex/ext/mma by oracle/ref_build.sh) on a seeded problem
                        with the reference optimizer's settings (one volume constraint with
                        coefficient 1e4, move limit 0.2, bounds [0.01, 1]).
 
-usage: python tests/golden/make_golden.py [3d] [2d] [mma]
+usage: python tests/golden/make_golden.py [3d] [2d] [mma] [loop2d]
 """
 import ctypes
 import os
@@ -147,8 +152,37 @@ def ref_mma():
     np.savez_compressed(os.path.join(HERE, "ref_mma.npz"), dfdx=np.array(dfs), x=xs)
 
 
+def oracle_loop2d(n=64, iters=20, frac=0.3, rmin=1.5):
+    from oracle import pyoracle as po
+
+    po.build()
+    b = po.bc_parabolic(n, 2, width=n // 4)
+    vw = po.filt(np.ones((n, n)), rmin, transpose=True)
+    x = np.full((n, n), frac)
+    Js = []
+    for it in range(iters):
+        x_last = x.copy()
+        phys = po.filt(x, rmin)
+        fp = po.face_penalty(phys, 1, [1e4], dim=2)
+        o = po.Steady2D(n)
+        o.init_boundary(b)
+        o.update_penalty(np.zeros((n, n)), fp)
+        o.update_b(b.cell_b, b.face_b)
+        u, _ = o.solve(max_iter=60, abs_thr=0.0, rel_thr=1e-13, norm_thr=0.0, restarts=8, true_tol=1e-11)
+        Js.append(o.energy(u))
+        o.set_b_blocked(o.apply_E(u))
+        lam, _ = o.solve(max_iter=60, abs_thr=0.0, rel_thr=1e-13, norm_thr=0.0, restarts=8, true_tol=1e-11)
+        _, uf = po.blocked_to_field2(n, u)
+        _, lf = po.blocked_to_field2(n, lam)
+        sens = po.sensitivity(phys, 1, [1e4], uf, lf, dim=2)
+        dc = po.filt(sens, rmin, transpose=True)
+        x = po.oc_update(x, dc, vw / n ** 2, vw, frac)[0].reshape(n, n)
+        print("loop2d", it, Js[-1], flush=True)
+    np.savez_compressed(os.path.join(HERE, "oracle_loop2d_n64.npz"), objective=np.array(Js), x_last=x_last)
+
+
 if __name__ == "__main__":
-    what = sys.argv[1:] or ["3d", "2d", "mma"]
+    what = sys.argv[1:] or ["3d", "2d", "mma", "loop2d"]
     if "3d" in what:
         ref_index_tables()
         oracle_regression()
@@ -157,4 +191,6 @@ if __name__ == "__main__":
         oracle_regression_2d()
     if "mma" in what:
         ref_mma()
+    if "loop2d" in what:
+        oracle_loop2d()
     print("wrote", os.listdir(HERE))

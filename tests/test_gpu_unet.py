@@ -10,7 +10,8 @@
 * one Adam step against the oracle's restatement with the GPU's own gradient (1e-6);
 * training on the solver's own operator lowers the loss below the loss of the zero
   correction, i.e. the trained network removes part of the error a V-cycle leaves;
-* the LEARNED method reaches the same FP64 tolerance and solution as PLAIN.
+* the LEARNED method reaches the same FP64 tolerance and solution as PLAIN in fewer
+  V-cycles.
 """
 import numpy as np
 import pytest
@@ -119,4 +120,6 @@ def test_learned_solve_matches_plain(oracle, stg):
     assert st0["learned_iters"] == 0
     for a, b in zip(v1, v0):
         assert relerr(a, b) < 1e-6
-    print("learned", st1, "plain", st0)
+    # what the trained network gains: fewer V-cycles to the same tolerance (10-11 against
+    # 16 on this problem)
+    assert st1["inner_iters"] < st0["inner_iters"], (st1, st0)

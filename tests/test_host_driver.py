@@ -152,3 +152,21 @@ def test_driver_2d_reference_test0_mma_matches_oracle(oracle, driver, tmp_path):
     assert np.allclose(log["objective"], J, rtol=1e-6, atol=0)
     for k in range(iters):
         assert relerr(read_field(out / str(k) / "x", n, 2), xs[k]) < 1e-6, k
+
+
+@pytest.mark.gpu
+def test_driver_2d_benchmark_loop_matches_oracle_fixture(driver, tmp_path):
+    """The 2D 64^2 benchmark case end to end: fluid_topo -driver 0 -test 1 -s 64 -frac 0.3
+    -lf 20 (parabolic inlet, OC, filter 1.5, every solve to 1e-10) against the oracle's
+    20-iteration loop (tests/golden/oracle_loop2d_n64.npz): objective at every iteration
+    within 1e-6, the last iteration's design within 1e-4. From iteration 4 on the designs
+    are high-contrast (density down to 1e-8): the V-cycle is a weak preconditioner there
+    and solves take hundreds of V-cycles over several refinement steps."""
+    n, iters = 64, 20
+    g = np.load(os.path.join(ROOT, "tests", "golden", "oracle_loop2d_n64.npz"))
+    out = tmp_path / "run"
+    subprocess.run([driver, "-driver", "0", "-test", "1", "-s", str(n), "-frac", "0.3", "-lf", str(iters), "-frames",
+                    str(iters - 1), "-o", str(out)], check=True)
+    log = np.genfromtxt(out / "log.csv", delimiter=",", names=True)
+    assert np.allclose(log["objective"], g["objective"], rtol=1e-6, atol=0)
+    assert relerr(read_field(out / str(iters - 1) / "x", n, 2), g["x_last"]) < 1e-4
