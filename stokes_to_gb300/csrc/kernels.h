@@ -26,6 +26,8 @@ int apply32(cudaStream_t st, const Geom& g, float vol, const float4* x, const ui
 // residual: xout = xin + SHATTER(B^-1 GATHER(r - A xin)) (sweep.cu). xin == nullptr: xin = 0.
 int sweep32(cudaStream_t st, const Geom& g, float vol, const float4* r, const float4* xin, float4* xout, const uint8_t* m,
             const float4* P, int flag, bool lap = false);
+// 1 in *timed_out when a sweep with TMA staging gave up waiting for its loads (sticky)
+int sweep_status(cudaStream_t st, int* timed_out);
 // rc = R (rf - A xf) with R the 8-child sum masked by the coarse mask (xf == nullptr: rc = R rf).
 int restrict_resid32(cudaStream_t st, const Geom& gc, const Geom& gf, float volf, const float4* rf, const float4* xf,
                      const uint8_t* mf, const float4* Pf, const uint8_t* mc, float4* rc, bool lap = false);

@@ -524,6 +524,12 @@ int solve_core(stg_t* h, const d4* b, d4* x, stg_stats* stats) {
         PROF(h, 6, (16.0 * k + 64.0) * n4, axpy_multi_32to64(h->st, n4, h->Z.data(), h->dy, k, rn, x));
     }
     if (h->finish) STG_TRY(h->finish(h, b, x));
+    int sweep_timeout = 0;
+    STG_TRY(sweep_status(h->st, &sweep_timeout));
+    if (sweep_timeout) {
+        set_error("smoother sweep: a staging wait timed out");
+        return STG_E_CUDA;
+    }
     STG_CK(cudaEventRecord(h->e1, h->st));
     STG_CK(cudaEventSynchronize(h->e1));
     float ms = 0;

@@ -23,6 +23,8 @@
 // side, whichever has the colour); faces with neither are left unchanged, as SHATTER
 // leaves them. If the Schur complement is 0 (the reference's LU meets a zero pivot) the
 // pressure is left unchanged.
+#include <cuda.h>
+
 #include "kernels.h"
 #include "stencil.cuh"
 
@@ -638,7 +640,375 @@ __global__ void __launch_bounds__(NT, 3) k_sweep_lap(Geom g, float vol, const fl
     }
 }
 
+// ---------------------------------------------------------------- Laplacian-form sweep, TMA staging
+// The Laplacian-form sweep with the planes of x, r and P staged by the tensor-memory
+// accelerator: one thread issues one cp.async.bulk.tensor box load per plane and array
+// (x: 36 x 12 slots, r and P: 34 x 10 slots, 16 bytes each) into the ring slot, with an
+// mbarrier counting the bytes, instead of every thread issuing 16-byte copies. The boxes
+// read zero outside the allocation, as the copies did. Everything else is k_sweep_lap.
+constexpr int RNP = 344;  // r / P ring slot in float4s: RN padded to 128 bytes (TMA destinations)
+constexpr unsigned XBYTES = XN * 16, RBYTES = RN * 16;
+static_assert(RNP >= RN && (RNP * 16) % 128 == 0 && (XN * 16) % 128 == 0, "TMA ring slots must be 128-byte aligned");
+
+struct SmemT {
+    float4 x[4 * XN];
+    float4 P[3 * RNP];
+    float4 r[2 * RNP];
+    float4 rr[2 * RN];
+    float dp[DJ * DK];
+    float dpp[SJ * SK];
+    uint8_t m[4 * XN];
+    unsigned long long bar;
+};
+
+// 3D box load of the tensor map at coordinates (c0, c1, c2) into shared memory, counted on bar
+__device__ __forceinline__ void tma3(unsigned dst, const CUtensorMap* map, int c0, int c1, int c2, unsigned bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];\n" ::"r"(dst),
+        "l"(reinterpret_cast<unsigned long long>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(bar)
+        : "memory");
+}
+
+// arrive on bar expecting `bytes` of transfers in the current phase
+__device__ __forceinline__ void arm_tx(unsigned bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+// waits for the phase of the given parity to complete; false after about a second
+__device__ __forceinline__ bool wait_phase(unsigned bar, unsigned parity) {
+    unsigned long long t0;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+    while (true) {
+        unsigned done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
+            : "=r"(done)
+            : "r"(bar), "r"(parity)
+            : "memory");
+        if (done) return true;
+        unsigned long long t1;
+        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t1));
+        if (t1 - t0 > 1000000000ull) return false;
+    }
+}
+
+__device__ __forceinline__ void fail(int* err) {
+    if (threadIdx.x == 0 && threadIdx.y == 0) atomicExch(err, 1);
+}
+
+template <bool HAS_X>
+__global__ void __launch_bounds__(NT, 3) k_sweep_tma(const __grid_constant__ CUtensorMap tmx, const __grid_constant__ CUtensorMap tmr,
+                                                    const __grid_constant__ CUtensorMap tmp, Geom g, float vol,
+                                                    float4* __restrict__ xout, const uint8_t* __restrict__ m, int flag, int chunk,
+                                                    int* __restrict__ err) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    SmemT& S = *reinterpret_cast<SmemT*>(smem_raw);
+    const int n = g.n;
+    const int tk = threadIdx.x, tj = threadIdx.y, tid = tj * SK + tk;
+    const int k0 = blockIdx.x * SK, j0 = blockIdx.y * SJ, i0 = blockIdx.z * chunk;
+    const int i1 = min(i0 + chunk, n + 1);
+    const int j = j0 + tj, k = k0 + tk;
+    const float v6 = 6.f * vol;
+
+    // staging elements: x / mask region (X) and P / r region (R), two per thread
+    const Stage X0 = make_stage(g, tid, XN, XK, j0 - 2, k0 - 2), X1 = make_stage(g, tid + NT, XN, XK, j0 - 2, k0 - 2);
+    const unsigned sx = (unsigned)__cvta_generic_to_shared(S.x), sP = (unsigned)__cvta_generic_to_shared(S.P),
+                   sr = (unsigned)__cvta_generic_to_shared(S.r);
+
+    // residual elements: rr/P index e and x/mask index xi, and whether (j,k) lies in [0,n]^2
+    const int re0 = tid, re1 = tid + NT;
+    const int rx0 = re0 + (re0 / RK) * (XK - RK) + XK + 1, rx1 = re1 + (re1 / RK) * (XK - RK) + XK + 1;
+    auto in_box = [&](int e) {
+        int jj = j0 - 1 + e / RK, kk = k0 - 1 + e % RK;
+        return e < RN && jj >= 0 && jj <= n && kk >= 0 && kk <= n;
+    };
+    const bool rb0 = in_box(re0), rb1 = in_box(re1);
+
+    // pressure-phase cell of this thread for the two plane parities
+    const int pdj = tid / DRED, pq = tid % DRED, pj = j0 - 1 + pdj;
+    const bool p_thread = tid < DJ * DRED;
+    const int ppar0 = (pj + flag - (k0 - 1)) & 1;  // dk = ((p & 1) ^ ppar0) + 2 pq
+    // (the two parities as scalars: a runtime-indexed array would live in local memory)
+    const int pdk0 = 2 * pq, pdk1 = 2 * pq + 1;
+    const bool pok0 = p_thread && pdk0 < DK && pj >= 0 && k0 - 1 + pdk0 >= 0 && pj < n && k0 - 1 + pdk0 < n;
+    const bool pok1 = p_thread && pdk1 < DK && pj >= 0 && k0 - 1 + pdk1 >= 0 && pj < n && k0 - 1 + pdk1 < n;
+
+    // update-phase slot
+    const bool out_ok = j <= n && k <= n;
+    const long long out_jk = (long long)(j + 1) * g.sz + (k + 1);
+    const int oxi = (tj + 2) * XK + (tk + 2), ori = (tj + 1) * RK + (tk + 1), odi = (tj + 1) * DK + (tk + 1);
+    const bool jk_cell = j < n && k < n;
+    const int opar = (j + k + flag) & 1;  // own colour is red when ((i & 1) ^ opar) == 0
+    const bool lo_j_ok = j >= 1 && k < n, lo_k_ok = k >= 1 && j < n;
+
+    // plane p of x (region origin j0-2, k0-2) or of r / P (origin j0-1, k0-1) into a ring
+    // slot by one TMA box load each; out-of-allocation parts of a box read as zero
+    const uint32_t bar = (uint32_t)__cvta_generic_to_shared(&S.bar);
+    auto tma_x = [&](int slot, int p) { tma3(sx + 16u * slot, &tmx, 4 * (k0 - 1), j0 - 1, p + 1, bar); };
+    auto tma_r = [&](unsigned base, int slot, int p, const CUtensorMap* tm) { tma3(base + 16u * slot, tm, 4 * k0, j0, p + 1, bar); };
+    uint32_t phase = 0;
+    // every thread waits for the current phase; a wait that gives up (about a second) makes
+    // the whole block record the error and leave at the next barrier
+    auto wait_loads = [&]() {
+        const bool ok = wait_phase(bar, phase);
+        phase ^= 1u;
+        return ok;
+    };
+    uint8_t mr0 = MALL, mr1 = MALL;
+    auto fetch_m = [&](int p, const uint8_t* src) {
+        const bool pok = p >= -1 && p <= n + 1;
+        mr0 = (pok && X0.jk >= 0) ? __ldg(src + X0.jk) : (uint8_t)MALL;
+        mr1 = (pok && X1.jk >= 0) ? __ldg(src + X1.jk) : (uint8_t)MALL;
+    };
+    auto store_m = [&](int slot) {
+        if (X0.s >= 0) S.m[slot + X0.s] = mr0;
+        if (X1.s >= 0) S.m[slot + X1.s] = mr1;
+    };
+
+    // residual of plane p: x slots (p-1, p, p+1), r / P / mask slots of p, into rr slot
+    auto residual = [&](int p, int xa, int xb, int xc, int rs, int ps, int ms, int rrs) {
+        const bool pin = p >= 0 && p <= n;
+        auto one = [&](int e, int xi, bool box) {
+            float4 out = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (pin && box) {
+                const float4 rv = S.r[rs + e];
+                if (HAS_X) {
+                    auto q = [&](int idx) {
+                        const float4 v = S.x[idx];
+                        return Q4<float>{v.x, v.y, v.z, v.w};
+                    };
+                    const float4 pv = S.P[ps + e];
+                    float o[4];
+                    lap_core<float>(q(xb + xi), q(xa + xi), q(xc + xi), q(xb + xi - XK), q(xb + xi + XK), q(xb + xi - 1),
+                                    q(xb + xi + 1), Q4<float>{pv.x, pv.y, pv.z, pv.w}, vol, o);
+                    o[0] = rv.x - o[0];
+                    o[1] = rv.y - o[1];
+                    o[2] = rv.z - o[2];
+                    o[3] = rv.w - o[3];
+                    mask4<float>(S.m[ms + xi], o);
+                    out = make_float4(o[0], o[1], o[2], o[3]);
+                } else {
+                    out = rv;  // r is zero on fixed unknowns
+                }
+            }
+            S.rr[rrs + e] = out;
+        };
+        one(re0, rx0, rb0);
+        if (re1 < RN) one(re1, rx1, rb1);
+    };
+
+    // pressure update of the red cells of plane p (rr slots p, p+1; P slots p, p+1; mask slots p, p+1)
+    auto pressure = [&](int p, int rr0, int rr1, int p0, int p1, int m0s, int m1s) {
+        const int b = (p & 1) ^ ppar0;
+        if (!(b ? pok1 : pok0) || p < 0 || p >= n) return;
+        const int dk = b ? pdk1 : pdk0;
+        const int ri = pdj * RK + dk, xi = (pdj + 1) * XK + (dk + 1);
+        const float4 rc = S.rr[rr0 + ri], pc = S.P[p0 + ri];
+        const uint8_t mo = S.m[m0s + xi];
+        const float rL[3] = {rc.y, rc.z, rc.w}, pL[3] = {pc.y, pc.z, pc.w};
+        const uint8_t mhi[3] = {S.m[m1s + xi], S.m[m0s + xi + XK], S.m[m0s + xi + 1]};
+        const float rh[3] = {S.rr[rr1 + ri].y, S.rr[rr0 + ri + RK].z, S.rr[rr0 + ri + 1].w};
+        const float ph[3] = {S.P[p1 + ri].y, S.P[p0 + ri + RK].z, S.P[p0 + ri + 1].w};
+        const uint8_t bit[3] = {MU, MV, MW};
+        float num = rc.x, den = 2.f * pc.x;
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+            const float vL = (mo & bit[d]) ? 0.f : vol, vR = (mhi[d] & bit[d]) ? 0.f : vol;
+            const float iL = __fdividef(vL, v6 + pL[d]), iR = __fdividef(vR, v6 + ph[d]);
+            num += rL[d] * iL - rh[d] * iR;
+            den -= vL * iL + vR * iR;
+        }
+        S.dp[pdj * DK + dk] = den != 0.f ? __fdividef(num, den) : 0.f;
+    };
+
+    // ring slots as element offsets (rotated each plane)
+    int xm1 = 0 * XN, x0 = 1 * XN, x1 = 2 * XN, x2 = 3 * XN;  // x(i-1), x(i), x(i+1), x(i+2)
+    int pm1 = 0 * RNP, p0 = 1 * RNP, p1 = 2 * RNP;            // P(i-1), P(i), P(i+1)
+    int r0 = 0 * RNP, r1 = 1 * RNP;                           // r(i), r(i+1)
+    int rrm1 = 0 * RN, rr0 = 1 * RN;                          // rr(i-1), rr(i)
+    int mm1 = 0 * XN, m0 = 1 * XN, m1 = 2 * XN, m2 = 3 * XN;  // masks of planes i-1 .. i+2
+
+    // prologue: planes i0-2 .. i0+1 of x, i0-1 .. i0+1 of P, i0-1 and i0 of r, masks i0-1 .. i0+2
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    __syncthreads();
+    if (tid == 0) {
+        arm_tx(bar, (HAS_X ? 4 * XBYTES : 0) + 5 * RBYTES);
+        if (HAS_X) {
+            tma_x(xm1, i0 - 2);
+            tma_x(x0, i0 - 1);
+            tma_x(x1, i0);
+            tma_x(x2, i0 + 1);
+        }
+        tma_r(sP, pm1, i0 - 1, &tmp);
+        tma_r(sP, p0, i0, &tmp);
+        tma_r(sP, p1, i0 + 1, &tmp);
+        tma_r(sr, r0, i0 - 1, &tmr);
+        tma_r(sr, r1, i0, &tmr);
+    }
+    const long long plane = (long long)g.sy * g.sz;
+    const uint8_t* gm = m + i0 * plane;  // plane i0-1
+    fetch_m(i0 - 1, gm);
+    store_m(mm1);
+    fetch_m(i0, gm + plane);
+    store_m(m0);
+    fetch_m(i0 + 1, gm + 2 * plane);
+    store_m(m1);
+    fetch_m(i0 + 2, gm + 3 * plane);
+    store_m(m2);
+    if (__syncthreads_or(!wait_loads())) return fail(err);
+    // residual of i0-1: x(i0-2, i0-1, i0) = slots (xm1, x0, x1), r(i0-1) = r0, P(i0-1) = pm1, mask(i0-1) = mm1
+    residual(i0 - 1, xm1, x0, x1, r0, pm1, mm1, rrm1);
+    __syncthreads();
+    if (tid == 0) {
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        arm_tx(bar, (HAS_X ? XBYTES : 0) + RBYTES);
+        if (HAS_X) tma_x(xm1, i0 + 2);  // x(i0+2) replaces x(i0-2)
+        tma_r(sr, r0, i0 + 1, &tmr);    // r(i0+1) replaces r(i0-1)
+    }
+    // residual of i0: x(i0-1, i0, i0+1) = (x0, x1, x2), r(i0) = r1, P(i0) = p0, mask(i0) = m0
+    residual(i0, x0, x1, x2, r1, p0, m0, rr0);
+    __syncthreads();
+    pressure(i0 - 1, rrm1, rr0, pm1, p0, mm1, m0);
+    __syncthreads();
+    S.dpp[tid] = S.dp[odi];
+    if (__syncthreads_or(!wait_loads())) return fail(err);
+    // rotate to the loop's view at i = i0: x(i0-1..i0+2) = (x0, x1, x2, xm1), r(i0) = r1,
+    // r(i0+1) = r0, rr(i0-1) = rrm1, rr(i0) = rr0, P(i0-1) = pm1, masks i0-1 .. i0+2 unchanged
+    {
+        int t = xm1;
+        xm1 = x0;
+        x0 = x1;
+        x1 = x2;
+        x2 = t;
+        t = r0;
+        r0 = r1;
+        r1 = t;
+    }
+    gm += 4 * plane;  // plane i0+3
+    float4* gout = xout + (i0 + 1) * plane + out_jk;
+
+    for (int i = i0; i < i1; i++) {
+        // stream x(i+3) into the slot of x(i-1), P(i+2) into P(i-1), r(i+2) into r(i)
+        if (tid == 0) {
+            asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+            arm_tx(bar, (HAS_X ? XBYTES : 0) + 2 * RBYTES);
+            if (HAS_X) tma_x(xm1, i + 3);
+            tma_r(sP, pm1, i + 2, &tmp);
+            tma_r(sr, r0, i + 2, &tmr);
+        }
+        fetch_m(i + 3, gm);
+        residual(i + 1, x0, x1, x2, r1, p1, m1, rrm1);
+        __syncthreads();
+        pressure(i, rr0, rrm1, p0, p1, m0, m1);
+        __syncthreads();
+        if (out_ok) {
+            float4 xo = HAS_X ? S.x[x0 + oxi] : make_float4(0.f, 0.f, 0.f, 0.f);
+            const float4 rv = S.rr[rr0 + ori], pv = S.P[p0 + ori];
+            const uint8_t mo = S.m[m0 + oxi];
+            const bool cell = jk_cell && i < n;
+            const bool own_col = ((i & 1) ^ opar) == 0;  // (i + j + k + flag) even
+            const bool own_red = cell && own_col;
+            const float dpown = S.dp[odi];
+            if (own_red) xo.x += dpown;
+            // the lower cells have the other colour: red exactly when the own colour is black
+            const bool lo_ok[3] = {!own_col && i >= 1 && jk_cell, !own_col && lo_j_ok && i < n, !own_col && lo_k_ok && i < n};
+            const float dplo[3] = {S.dpp[tid], S.dp[odi - DK], S.dp[odi - 1]};
+            const float rf[3] = {rv.y, rv.z, rv.w}, pf[3] = {pv.y, pv.z, pv.w};
+            const uint8_t bit[3] = {MU, MV, MW};
+            float upd[3];
+#pragma unroll
+            for (int d = 0; d < 3; d++) {
+                upd[d] = 0.f;
+                if (!own_red && !lo_ok[d]) continue;
+                const bool fix = mo & bit[d];
+                const float v = fix ? 0.f : vol;
+                const float D = fix ? 1.f : v6 + pf[d];
+                upd[d] = __fdividef(rf[d] - (own_red ? -v : v) * (own_red ? dpown : dplo[d]), D);
+            }
+            xo.y += upd[0];
+            xo.z += upd[1];
+            xo.w += upd[2];
+            *gout = xo;
+        }
+        store_m(mm1);  // mask (i+3) into the slot of mask (i-1)
+        if (__syncthreads_or(!wait_loads())) return fail(err);
+        S.dpp[tid] = S.dp[odi];
+        // rotate the rings and advance the plane pointers
+        {
+            int t = xm1;
+            xm1 = x0;
+            x0 = x1;
+            x1 = x2;
+            x2 = t;
+            t = pm1;
+            pm1 = p0;
+            p0 = p1;
+            p1 = t;
+            t = r0;
+            r0 = r1;
+            r1 = t;
+            t = rrm1;
+            rrm1 = rr0;
+            rr0 = t;
+            t = mm1;
+            mm1 = m0;
+            m0 = m1;
+            m1 = m2;
+            m2 = t;
+        }
+        gm += plane;
+        gout += plane;
+    }
+}
+
 }  // namespace
+
+namespace {
+
+using EncodeTiled = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*, const cuuint64_t*,
+                                 const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                 CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+// the driver's tensor-map encoder, fetched through the runtime (no link against the driver
+// library); null when unavailable, in which case the sweep stages with cp.async
+EncodeTiled encoder() {
+    static EncodeTiled fn = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiled>(p);
+        cudaGetLastError();
+    }
+    return fn;
+}
+
+// tensor map of a slot array of g as FP32 [planes][rows][4 (n+4)], box (4 bk) x bj x 1
+bool slot_map(EncodeTiled enc, CUtensorMap* map, const void* base, const Geom& g, int bk, int bj) {
+    const cuuint64_t dims[3] = {(cuuint64_t)g.sz * 4, (cuuint64_t)g.sy, (cuuint64_t)g.sx};
+    const cuuint64_t strides[2] = {(cuuint64_t)g.sz * 16, (cuuint64_t)g.sy * g.sz * 16};
+    const cuuint32_t box[3] = {(cuuint32_t)(4 * bk), (cuuint32_t)bj, 1}, es[3] = {1, 1, 1};
+    return enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<void*>(base), dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+               CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+int* g_sweep_err = nullptr;  // set by a TMA sweep whose wait gave up (device)
+
+}  // namespace
+
+int sweep_status(cudaStream_t st, int* timed_out) {
+    *timed_out = 0;
+    if (!g_sweep_err) return STG_OK;
+    STG_CK(cudaMemcpyAsync(timed_out, g_sweep_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    STG_CK(cudaStreamSynchronize(st));
+    return STG_OK;
+}
 
 int sweep32(cudaStream_t st, const Geom& g, float vol, const float4* r, const float4* xin, float4* xout, const uint8_t* m,
             const float4* P, int flag, bool lap) {
@@ -655,6 +1025,28 @@ int sweep32(cudaStream_t st, const Geom& g, float vol, const float4* r, const fl
     // coarse levels, where the sequential march, not bandwidth, sets the time
     const int chunk = g.n >= 192 ? 32 : g.n >= 96 ? 16 : g.n >= 48 ? 8 : g.n >= 24 ? 4 : 2;
     dim3 grid((g.n + SK) / SK, (g.n + SJ) / SJ, (g.n + chunk) / chunk), block(SK, SJ);
+    if (lap && encoder()) {
+        static bool tattr = false;
+        const int smem_t = (int)sizeof(SmemT);
+        if (!tattr) {
+            STG_CK(cudaFuncSetAttribute(k_sweep_tma<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_t));
+            STG_CK(cudaFuncSetAttribute(k_sweep_tma<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_t));
+            STG_CK(cudaMalloc((void**)&g_sweep_err, sizeof(int)));
+            STG_CK(cudaMemset(g_sweep_err, 0, sizeof(int)));
+            tattr = true;
+        }
+        CUtensorMap mx{}, mr{}, mp{};
+        const EncodeTiled enc = encoder();
+        const bool ok = (!xin || slot_map(enc, &mx, xin, g, XK, XJ)) && slot_map(enc, &mr, r, g, RK, RJ) && slot_map(enc, &mp, P, g, RK, RJ);
+        if (ok) {
+            if (xin)
+                k_sweep_tma<true><<<grid, block, smem_t, st>>>(mx, mr, mp, g, vol, xout, m, flag, chunk, g_sweep_err);
+            else
+                k_sweep_tma<false><<<grid, block, smem_t, st>>>(mr, mr, mp, g, vol, xout, m, flag, chunk, g_sweep_err);
+            STG_LAUNCH_CK();
+            return STG_OK;
+        }
+    }
     if (xin && lap)
         k_sweep_lap<true><<<grid, block, smem_l, st>>>(g, vol, r, xin, xout, m, P, flag, chunk);
     else if (xin)
