@@ -98,6 +98,7 @@ struct stg_ctx {
     int (*resid64)(stg_t*, const stg::d4* b, const stg::d4* x, stg::d4* r, double* nrm2_host) = nullptr;
     int (*precond)(stg_t*, const float4* rhs, float4* out) = nullptr;
     int (*apply32)(stg_t*, const float4* x, float4* y) = nullptr;
+    int (*shift32)(stg_t*, const float4* v, const float4* z, float4* out) = nullptr;  // out = v - A z
     int (*finish)(stg_t*, const stg::d4* b, stg::d4* x) = nullptr;  // optional, after the refinement loop
     struct Ctx2* c2 = nullptr;        // 2D state (dim == 2)
     struct MmaState* mma = nullptr;   // MMA optimizer state (mma.cu), created on first use

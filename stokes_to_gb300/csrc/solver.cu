@@ -357,6 +357,12 @@ int precond_learned(stg_t* h, const float4* rhs, float4* out) {
     return rc;
 }
 
+int shift3(stg_t* h, const float4* v, const float4* z, float4* out) {
+    Level& F = fine(h);
+    PROF(h, 4, 65.0 * F.g.box(), resid32(h->st, F.g, (float)F.vol, v, z, F.m, F.P32, out, fast(h, F)));
+    return STG_OK;
+}
+
 int apply3(stg_t* h, const float4* x, float4* y) {
     Level& F = fine(h);
     PROF(h, 4, 49.0 * F.g.box(), apply32(h->st, F.g, (float)F.vol, x, F.m, F.P32, y, fast(h, F)));
@@ -440,7 +446,10 @@ int solve_core(stg_t* h, const d4* b, d4* x, stg_stats* stats) {
         for (int j = 0; j < m; j++) {
             if (h->net_on) S.learned_iters++;
             STG_TRY(h->precond(h, h->V[j], h->Z[j]));
-            STG_TRY(h->apply32(h, h->Z[j], h->w));
+            // Arnoldi on the shifted operator A M - I, written as w = V_j - A Z_j: same Krylov
+            // space, and a good preconditioner (A M near I) no longer leaves w dominated by
+            // V_j, whose removal cancelled most of w and forced the second projection pass
+            STG_TRY(h->shift32(h, h->V[j], h->Z[j], h->w));
             PROF(h, 6, 16.0 * (j + 2) * n4, multidot32(h->st, n4, h->V.data(), j + 1, h->w, h->dh, h->dscr, h->dnrm + 1));
             PROF(h, 6, 16.0 * (j + 3) * n4,
                  project32(h->st, n4, h->V.data(), j + 1, h->dh, h->dsig2, h->w, h->V[j + 1], h->dh + m + 2, h->dnrm, h->dscr));
@@ -461,9 +470,10 @@ int solve_core(stg_t* h, const d4* b, d4* x, stg_stats* stats) {
                 std::fill(h2.begin(), h2.end(), 0.0);
             }
             S.inner_iters++;
+            // A z_j = v_j - sum_q sig_q sig_j d_q v_q - (sig_j / sig_{j+1}) v_{j+1}
             const double hn = sig[j] * std::sqrt(nw2);
-            for (int q = 0; q <= j; q++) hcol[q] = sig[q] * sig[j] * (h1[q] + h2[q]);
-            hcol[j + 1] = hn;
+            for (int q = 0; q <= j; q++) hcol[q] = (q == j ? 1.0 : 0.0) - sig[q] * sig[j] * (h1[q] + h2[q]);
+            hcol[j + 1] = -hn;
             if (!std::isfinite(hn)) {
                 status = STG_E_NONFINITE;
                 set_error("non-finite Arnoldi norm");
@@ -720,6 +730,7 @@ int stg_create(int dim, int n, const stg_opts* opts, stg_t** out) {
         h->resid64 = residual64;
         h->precond = h->opts.method == STG_METHOD_LEARNED ? precond_learned : precond3;
         h->apply32 = apply3;
+        h->shift32 = shift3;
         h->finish = finish3;
         h->ncell = (size_t)n * n * n;
         h->nface = (size_t)n * n * (n + 1);

@@ -619,6 +619,14 @@ int precond2(stg_t* h, const float4* rhs, float4* out) {
     return STG_OK;
 }
 
+int shift2(stg_t* h, const float4* v, const float4* z, float4* out) {
+    Level2& L = fine2(h);
+    k2_apply<float, 1><<<g1(L.g.size()), TPB, 0, h->st>>>(L.g, coef32(L), (float)L.lap, reinterpret_cast<const float*>(z),
+                                                           reinterpret_cast<const float*>(v), reinterpret_cast<float*>(out), nullptr);
+    STG_LAUNCH_CK();
+    return STG_OK;
+}
+
 int apply2(stg_t* h, const float4* x, float4* y) {
     return apply2_32(h, fine2(h), reinterpret_cast<const float*>(x), reinterpret_cast<float*>(y));
 }
@@ -664,6 +672,7 @@ int create2d(stg_t* h) {
     h->resid64 = resid2;
     h->precond = precond2;
     h->apply32 = apply2;
+    h->shift32 = shift2;
     return STG_OK;
 }
 
