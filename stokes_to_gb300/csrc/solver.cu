@@ -438,7 +438,9 @@ int solve_core(stg_t* h, const d4* b, d4* x, stg_stats* stats) {
         // host (and sig_q^2 on the device), z_q = sig_q Z_q with Z_q = M V_q. Arnoldi step:
         // pass 1 d1 = V^T w; pass 2 V_{j+1} = w - sum sig^2 d1 V together with
         // d2 = V^T V_{j+1}; pass 3 (classical Gram-Schmidt's second sweep, only when the
-        // first cancelled most of w: ||V_{j+1}|| < 0.7 ||w||) V_{j+1} -= sum sig^2 d2 V.
+        // first cancelled nearly all of w: ||V_{j+1}|| < 0.1 ||w||) V_{j+1} -= sum sig^2 d2 V.
+        // The looser trigger than the usual 0.7 costs orthogonality of order 1e-6 in FP32,
+        // far below the 1e-4 an inner solve is asked for; the FP64 refinement is the judge.
         sig[0] = 1.0;
         const double one = 1.0;
         STG_CK(cudaMemcpyAsync(h->dsig2, &one, sizeof(double), cudaMemcpyHostToDevice, h->st));
@@ -460,7 +462,7 @@ int solve_core(stg_t* h, const d4* b, d4* x, stg_stats* stats) {
             STG_CK(cudaMemcpyAsync(nrm, h->dnrm, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->st));
             STG_CK(cudaStreamSynchronize(h->st));
             double nw2 = nrm[0];
-            if (nrm[0] < 0.49 * nrm[1]) {
+            if (nrm[0] < 0.01 * nrm[1]) {
                 PROF(h, 6, 16.0 * (j + 3) * n4,
                      project32(h->st, n4, h->V.data(), j + 1, h->dh + m + 2, h->dsig2, h->V[j + 1], h->V[j + 1], nullptr, h->dnrm,
                                h->dscr));
