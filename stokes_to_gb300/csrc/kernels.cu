@@ -106,49 +106,63 @@ __global__ void __launch_bounds__(TPB) k_op32(Geom g, float vol, const float4* _
 // the coarse unknown of every kind at slot (I,J,K) sums the eight fine unknowns of the same
 // kind at slots (2I+a, 2J+b, 2K+c), then fixed coarse unknowns are zeroed. Fused with the
 // fine residual r - A x.
+// One thread per fine slot: a 32 (k) x 8 (j) block covers the 16 x 4 coarse cells of one
+// coarse plane I, each thread adds the residuals of its fine
+// slot on planes 2I and 2I+1 (coalesced loads, neighbours through L1), and the 2 x 2 (j, k)
+// children sums go through shared memory to the 64 writing threads.
 template <bool HAS_X, bool LAP>
-__global__ void __launch_bounds__(TPB) k_restrict_res32(Geom gc, Geom gf, float volf, const float4* __restrict__ rf,
-                                                        const float4* __restrict__ xf, const uint8_t* __restrict__ mf,
-                                                        const float4* __restrict__ Pf, const uint8_t* __restrict__ mc,
-                                                        float4* __restrict__ rc) {
-    long long t = (long long)blockIdx.x * TPB + threadIdx.x;
-    if (t >= gc.box()) return;
-    int I, J, K;
-    gc.box_ijk(t, I, J, K);
+__global__ void __launch_bounds__(256) k_restrict_fine32(Geom gc, Geom gf, float volf, const float4* __restrict__ rf,
+                                                         const float4* __restrict__ xf, const uint8_t* __restrict__ mf,
+                                                         const float4* __restrict__ Pf, const uint8_t* __restrict__ mc,
+                                                         float4* __restrict__ rc) {
+    __shared__ float4 sv[8][32];
+    const int tk = threadIdx.x, tj = threadIdx.y;
+    const int k = blockIdx.x * 32 + tk, j = blockIdx.y * 8 + tj, I = blockIdx.z;
     const int nf = gf.n;
-    float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
+    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (j <= nf && k <= nf) {
 #pragma unroll
-    for (int c = 0; c < 8; c++) {
-        int i = 2 * I + (c & 1), j = 2 * J + ((c >> 1) & 1), k = 2 * K + ((c >> 2) & 1);
-        if (i > nf || j > nf || k > nf) continue;
-        int s = gf.slot(i, j, k);
-        float4 r = __ldg(rf + s);
-        if (HAS_X) {
-            float o[4];
-            if (LAP) {
-                lap_rows<float>(xf, Pf, s, gf.di(), gf.dj(), volf, o);
-                o[0] = r.x - o[0];
-                o[1] = r.y - o[1];
-                o[2] = r.z - o[2];
-                o[3] = r.w - o[3];
-                mask4<float>(__ldg(mf + s), o);
-                r = make_float4(o[0], o[1], o[2], o[3]);
-            } else {
-                apply_rows<float, false>(xf, mf, Pf, s, gf.di(), gf.dj(), volf, o);
-                r.x -= o[0];
-                r.y -= o[1];
-                r.z -= o[2];
-                r.w -= o[3];
+        for (int q = 0; q < 2; q++) {
+            const int i = 2 * I + q;
+            if (i > nf) continue;
+            const int s = gf.slot(i, j, k);
+            float4 r = __ldg(rf + s);
+            if (HAS_X) {
+                float o[4];
+                if (LAP) {
+                    lap_rows<float>(xf, Pf, s, gf.di(), gf.dj(), volf, o);
+                    o[0] = r.x - o[0];
+                    o[1] = r.y - o[1];
+                    o[2] = r.z - o[2];
+                    o[3] = r.w - o[3];
+                    mask4<float>(__ldg(mf + s), o);
+                    r = make_float4(o[0], o[1], o[2], o[3]);
+                } else {
+                    apply_rows<float, false>(xf, mf, Pf, s, gf.di(), gf.dj(), volf, o);
+                    r.x -= o[0];
+                    r.y -= o[1];
+                    r.z -= o[2];
+                    r.w -= o[3];
+                }
             }
+            v.x += r.x;
+            v.y += r.y;
+            v.z += r.z;
+            v.w += r.w;
         }
-        a0 += r.x;
-        a1 += r.y;
-        a2 += r.z;
-        a3 += r.w;
     }
-    int sc = gc.slot(I, J, K);
-    uint8_t mm = __ldg(mc + sc);
-    rc[sc] = make_float4((mm & MP) ? 0.f : a0, (mm & MU) ? 0.f : a1, (mm & MV) ? 0.f : a2, (mm & MW) ? 0.f : a3);
+    sv[tj][tk] = v;
+    __syncthreads();
+    const int t = tj * 32 + tk;
+    if (t >= 64) return;
+    const int cj = t >> 4, ck = t & 15;
+    const int J = blockIdx.y * 4 + cj, K = blockIdx.x * 16 + ck;
+    if (J > gc.n || K > gc.n) return;
+    const float4 a = sv[2 * cj][2 * ck], b = sv[2 * cj][2 * ck + 1], c = sv[2 * cj + 1][2 * ck], d = sv[2 * cj + 1][2 * ck + 1];
+    const int sc = gc.slot(I, J, K);
+    const uint8_t mm = __ldg(mc + sc);
+    rc[sc] = make_float4((mm & MP) ? 0.f : (a.x + b.x) + (c.x + d.x), (mm & MU) ? 0.f : (a.y + b.y) + (c.y + d.y),
+                         (mm & MV) ? 0.f : (a.z + b.z) + (c.z + d.z), (mm & MW) ? 0.f : (a.w + b.w) + (c.w + d.w));
 }
 
 // Prolongation (stoke/StokeFlowSubSystem3D.cu:81-101 with SubsystemUtils3D.cuh:370-495):
@@ -510,13 +524,14 @@ int apply32(cudaStream_t st, const Geom& g, float vol, const float4* x, const ui
 
 int restrict_resid32(cudaStream_t st, const Geom& gc, const Geom& gf, float volf, const float4* rf, const float4* xf,
                      const uint8_t* mf, const float4* Pf, const uint8_t* mc, float4* rc, bool lap) {
-    unsigned nb = grid_for(gc.box(), TPB);
+    // fine box [0, nf]^3 in 32 x 8 (k, j) tiles, one coarse plane per z block
+    const dim3 grid((gf.n + 1 + 31) / 32, (gf.n + 1 + 7) / 8, gc.n + 1), block(32, 8);
     if (xf && lap)
-        k_restrict_res32<true, true><<<nb, TPB, 0, st>>>(gc, gf, volf, rf, xf, mf, Pf, mc, rc);
+        k_restrict_fine32<true, true><<<grid, block, 0, st>>>(gc, gf, volf, rf, xf, mf, Pf, mc, rc);
     else if (xf)
-        k_restrict_res32<true, false><<<nb, TPB, 0, st>>>(gc, gf, volf, rf, xf, mf, Pf, mc, rc);
+        k_restrict_fine32<true, false><<<grid, block, 0, st>>>(gc, gf, volf, rf, xf, mf, Pf, mc, rc);
     else
-        k_restrict_res32<false, false><<<nb, TPB, 0, st>>>(gc, gf, volf, rf, xf, mf, Pf, mc, rc);
+        k_restrict_fine32<false, false><<<grid, block, 0, st>>>(gc, gf, volf, rf, xf, mf, Pf, mc, rc);
     STG_LAUNCH_CK();
     return STG_OK;
 }
