@@ -46,25 +46,53 @@ struct Tab {
     const float4* p[MAXV];
 };
 
-// x64 += sum_q (alpha y_q) z_q, accumulated in FP64 (an FP32 sum of the basis loses
-// the outer refinement step's accuracy to cancellation among the terms)
+// Double-float accumulator (hi + lo, two FP32 words, ~46 significant bits): the products
+// c z of an FP64 coefficient split as ch + cl and an FP32 value z are added exactly up to
+// the lo words (ch z by its FMA remainder, cl z rounded in FP32, a term 2^-24 smaller).
+struct DF {
+    float hi = 0.f, lo = 0.f;
+    __device__ __forceinline__ void add_prod(float ch, float cl, float z) {
+        const float p = ch * z;
+        const float pe = fmaf(ch, z, -p) + cl * z;
+        const float t = hi + p;  // two-sum of hi and p
+        const float bb = t - hi;
+        const float e = (hi - (t - bb)) + (p - bb);
+        hi = t;
+        lo += e + pe;
+    }
+    __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+};
+
+// x64 += sum_q (alpha y_q) z_q. The sum runs in double-float arithmetic, not FP64: an FP32
+// sum of the basis loses the outer refinement step's accuracy to cancellation among the
+// terms, and GB300's FP64 pipe is far slower than HBM for this stream; only the final
+// addition to x is FP64.
 template <int NV>
 __global__ void __launch_bounds__(TPB) k_axpy_multi_32to64(long long n4, Tab z, const double* __restrict__ y, double alpha,
                                                            d4* __restrict__ x) {
-    double c[NV];
+    float ch[NV], cl[NV];
 #pragma unroll
-    for (int q = 0; q < NV; q++) c[q] = alpha * y[q];
+    for (int q = 0; q < NV; q++) {
+        const double c = alpha * y[q];
+        ch[q] = (float)c;
+        cl[q] = (float)(c - (double)ch[q]);
+    }
     for (long long t = (long long)blockIdx.x * TPB + threadIdx.x; t < n4; t += (long long)gridDim.x * TPB) {
-        double2* xp = reinterpret_cast<double2*>(x + t);
-        double2 a = xp[0], b = xp[1];
+        DF s0, s1, s2, s3;
 #pragma unroll
         for (int q = 0; q < NV; q++) {
-            float4 v = __ldg(z.p[q] + t);
-            a.x += c[q] * v.x;
-            a.y += c[q] * v.y;
-            b.x += c[q] * v.z;
-            b.y += c[q] * v.w;
+            const float4 v = __ldg(z.p[q] + t);
+            s0.add_prod(ch[q], cl[q], v.x);
+            s1.add_prod(ch[q], cl[q], v.y);
+            s2.add_prod(ch[q], cl[q], v.z);
+            s3.add_prod(ch[q], cl[q], v.w);
         }
+        double2* xp = reinterpret_cast<double2*>(x + t);
+        double2 a = xp[0], b = xp[1];
+        a.x += s0.value();
+        a.y += s1.value();
+        b.x += s2.value();
+        b.y += s3.value();
         xp[0] = a;
         xp[1] = b;
     }

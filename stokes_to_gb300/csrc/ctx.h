@@ -35,7 +35,8 @@ struct GraphCache {
     bool enabled = true;
     cudaGraphExec_t exec = nullptr;
     long long key = -1, seen = -1, kernels = 0;
-    std::vector<int> cur;  // ping-pong state of each level after the sequence
+    std::vector<int> cur;          // ping-pong state of each level after the sequence
+    const void* saved = nullptr;   // a pointer the sequence sets on the host (restored on replay)
     void release() {
         if (exec) cudaGraphExecDestroy(exec);
         exec = nullptr;
@@ -103,6 +104,7 @@ struct stg_ctx {
     struct Ctx2* c2 = nullptr;        // 2D state (dim == 2)
     struct MmaState* mma = nullptr;   // MMA optimizer state (mma.cu), created on first use
     GraphCache vgraph;                // the V-cycle below the finest level (3D) or all of it (2D)
+    GraphCache sgraph;                // the coarsest-level set-up (probes and Gauss-Jordan inverse)
     struct NetState* net = nullptr;   // learned preconditioner (unet.cu), stg_net_init
     bool net_on = false;              // LEARNED: the network is in use in the current refinement step
 };

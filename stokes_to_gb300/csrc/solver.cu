@@ -158,7 +158,18 @@ int update(stg_t* h) {
     }
     // coarse boundary faces have fixed children, so the Laplacian form carries down
     for (auto& L : h->lv) L.lap = h->lap_ok;
-    PROF(h, 8, 0.0, dense_setup(h->st, h->dense, h->lv[0].g, h->lv[0].vol, h->lv[0].m, h->lv[0].P64, h->closed ? 1 : 0));
+    // the coarsest set-up (one launch per Gauss-Jordan pivot) reads and writes fixed buffers:
+    // replayed as a CUDA graph; the inverse's buffer pointer is host state
+    GraphCache& G = h->sgraph;
+    PROF(h, 8, 0.0,
+         graphed(h, G, h->closed ? 2 : 1,
+                 [&] { return dense_setup(h->st, h->dense, h->lv[0].g, h->lv[0].vol, h->lv[0].m, h->lv[0].P64, h->closed ? 1 : 0); },
+                 [&](bool save) {
+                     if (save)
+                         G.saved = h->dense.inv;
+                     else
+                         h->dense.inv = static_cast<const double*>(G.saved);
+                 }));
     h->updated = true;
     return STG_OK;
 }

@@ -582,16 +582,27 @@ int setup2(stg_t* h) {
         return STG_E_INVALID;
     }
     auto& lv = h->c2->lv;
-    for (int i = (int)lv.size() - 2; i >= 0; i--) {
-        Level2 &c = lv[i], &f = lv[i + 1];
-        k2_coarsen<<<g1(c.g.size()), TPB, 0, h->st>>>(c.g, f.g, f.fixed, f.vol, f.pen, c.fixed, c.vol, c.pen, c.vol32, c.pen32);
+    // coarsening, the analytic coarsest matrix and its Gauss-Jordan inverse touch fixed
+    // buffers only: replayed as a CUDA graph; the inverse's buffer pointer is host state
+    auto body = [&]() -> int {
+        for (int i = (int)lv.size() - 2; i >= 0; i--) {
+            Level2 &c = lv[i], &f = lv[i + 1];
+            k2_coarsen<<<g1(c.g.size()), TPB, 0, h->st>>>(c.g, f.g, f.fixed, f.vol, f.pen, c.fixed, c.vol, c.pen, c.vol32, c.pen32);
+            STG_LAUNCH_CK();
+        }
+        Level2& C = lv[0];
+        const int nd = C.g.size();
+        k2_calcA<<<g1((long long)nd * nd), TPB, 0, h->st>>>(C.g, C.vol, C.pen, C.fixed, C.lap, h->closed ? 1 : 0, h->c2->aug0);
         STG_LAUNCH_CK();
-    }
-    Level2& C = lv[0];
-    const int nd = C.g.size();
-    k2_calcA<<<g1((long long)nd * nd), TPB, 0, h->st>>>(C.g, C.vol, C.pen, C.fixed, C.lap, h->closed ? 1 : 0, h->c2->aug0);
-    STG_LAUNCH_CK();
-    STG_TRY(gj_invert(h->st, nd, h->c2->aug0, h->c2->aug1, h->c2->info, &h->c2->inv));
+        return gj_invert(h->st, nd, h->c2->aug0, h->c2->aug1, h->c2->info, &h->c2->inv);
+    };
+    GraphCache& G = h->sgraph;
+    STG_TRY(graphed(h, G, h->closed ? 2 : 1, body, [&](bool save) {
+        if (save)
+            G.saved = h->c2->inv;
+        else
+            h->c2->inv = static_cast<const double*>(G.saved);
+    }));
     h->updated = true;
     return STG_OK;
 }
