@@ -69,7 +69,7 @@ struct DF {
 // addition to x is FP64.
 template <int NV>
 __global__ void __launch_bounds__(TPB) k_axpy_multi_32to64(long long n4, Tab z, const double* __restrict__ y, double alpha,
-                                                           d4* __restrict__ x) {
+                                                           d4* __restrict__ x, float4* __restrict__ xh, float4* __restrict__ xl) {
     float ch[NV], cl[NV];
 #pragma unroll
     for (int q = 0; q < NV; q++) {
@@ -95,6 +95,12 @@ __global__ void __launch_bounds__(TPB) k_axpy_multi_32to64(long long n4, Tab z, 
         b.y += s3.value();
         xp[0] = a;
         xp[1] = b;
+        if (xh) {
+            const float4 hv = make_float4((float)a.x, (float)a.y, (float)b.x, (float)b.y);
+            xh[t] = hv;
+            xl[t] = make_float4((float)(a.x - (double)hv.x), (float)(a.y - (double)hv.y), (float)(b.x - (double)hv.z),
+                                (float)(b.y - (double)hv.w));
+        }
     }
 }
 
@@ -277,8 +283,8 @@ static void dispatch_nv(int nb, A&&... args) {
 
 template <int NV>
 struct AxpyL {
-    static void run(cudaStream_t st, long long n4, const Tab& t, const double* y, double alpha, d4* x) {
-        k_axpy_multi_32to64<NV><<<rgrid(n4), TPB, 0, st>>>(n4, t, y, alpha, x);
+    static void run(cudaStream_t st, long long n4, const Tab& t, const double* y, double alpha, d4* x, float4* xh, float4* xl) {
+        k_axpy_multi_32to64<NV><<<rgrid(n4), TPB, 0, st>>>(n4, t, y, alpha, x, xh, xl);
     }
 };
 template <int NV>
@@ -301,12 +307,14 @@ struct ProjL {
     }
 };
 
-int axpy_multi_32to64(cudaStream_t st, long long n4, const float4* const* z, const double* y, int nz, double alpha, d4* x) {
+int axpy_multi_32to64(cudaStream_t st, long long n4, const float4* const* z, const double* y, int nz, double alpha, d4* x,
+                      float4* xh, float4* xl) {
     for (int j0 = 0; j0 < nz; j0 += MAXV) {
         int nb = nz - j0 < MAXV ? nz - j0 : MAXV;
         Tab t{};
         for (int q = 0; q < nb; q++) t.p[q] = z[j0 + q];
-        dispatch_nv<AxpyL>(nb, st, n4, t, y + j0, alpha, x);
+        const bool last = j0 + MAXV >= nz;  // the copy is written by the last chunk
+        dispatch_nv<AxpyL>(nb, st, n4, t, y + j0, alpha, x, last ? xh : nullptr, last ? xl : nullptr);
         STG_LAUNCH_CK();
     }
     return STG_OK;

@@ -77,6 +77,11 @@ struct stg_ctx {
     bool x0_valid[2] = {false, false};  // x64 / lam64 hold a previous solution (warm start)
     bool has_x0(const stg::d4* x) const { return (x == x64 && x0_valid[0]) || (x == lam64 && x0_valid[1]); }
     int* dflag = nullptr;
+    // 3D double-float copies for the FP64 residual (kernels.cu k_resid_df): x and b of the
+    // solve in progress (valid while df_x / df_b name them), the low words of the finest
+    // penalty (its high words are the level's P32)
+    float4 *xh = nullptr, *xl = nullptr, *bh = nullptr, *bl = nullptr, *Plo = nullptr;
+    const stg::d4 *df_x = nullptr, *df_b = nullptr;
     // fine-level FP64
     stg::d4 *b64 = nullptr, *x64 = nullptr, *r64 = nullptr, *t64 = nullptr, *lam64 = nullptr;
     // Krylov (FP32)

@@ -470,6 +470,125 @@ int patch_fixed(cudaStream_t st, const Geom& g, const d4* b, const uint8_t* m, d
     return STG_OK;
 }
 
+// ------------------------------------------------------------------ double-float residual
+// FP64 values as unevaluated sums hi + lo of two FP32 words (~46 significant bits). GB300
+// executes FP64 arithmetic far slower than FP32, so the FP64 residual of the solver's
+// refinement loop is evaluated in this arithmetic on double-float copies of x, b and the
+// penalty, and only the result is formed in FP64.
+struct F2 {
+    float h, l;
+};
+__device__ __forceinline__ F2 f2(float h, float l) { return F2{h, l}; }
+__device__ __forceinline__ F2 df_add(F2 a, F2 b) {
+    const float s = a.h + b.h, bb = s - a.h;
+    const float e = ((a.h - (s - bb)) + (b.h - bb)) + (a.l + b.l);
+    const float h = s + e;
+    return F2{h, e - (h - s)};
+}
+__device__ __forceinline__ F2 df_sub(F2 a, F2 b) { return df_add(a, F2{-b.h, -b.l}); }
+__device__ __forceinline__ F2 df_mul(F2 a, F2 b) {
+    const float p = a.h * b.h;
+    const float e = fmaf(a.h, b.l, fmaf(a.l, b.h, fmaf(a.h, b.h, -p)));
+    const float h = p + e;
+    return F2{h, e - (h - p)};
+}
+
+// hi = fl32(a), lo = fl32(a - hi) componentwise
+__global__ void __launch_bounds__(TPB) k_split64(long long n4, const d4* __restrict__ a, float4* __restrict__ hi,
+                                                 float4* __restrict__ lo) {
+    for (long long t = (long long)blockIdx.x * TPB + threadIdx.x; t < n4; t += (long long)gridDim.x * TPB) {
+        double v[4];
+        load4(a, (int)t, v[0], v[1], v[2], v[3]);
+        float h[4], l[4];
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+            h[c] = (float)v[c];
+            l[c] = (float)(v[c] - (double)h[c]);
+        }
+        if (hi) hi[t] = make_float4(h[0], h[1], h[2], h[3]);
+        lo[t] = make_float4(l[0], l[1], l[2], l[3]);
+    }
+}
+
+// r = b - A x in the Laplacian form (rows of fixed unknowns 0, x zero on fixed unknowns),
+// double-float arithmetic, r in FP64, per-block partials of |r|^2
+__global__ void __launch_bounds__(TPB) k_resid_df(Geom g, F2 vol, const float4* __restrict__ xh, const float4* __restrict__ xl,
+                                                  const float4* __restrict__ bh, const float4* __restrict__ bl,
+                                                  const float4* __restrict__ Ph, const float4* __restrict__ Pl,
+                                                  const uint8_t* __restrict__ m, d4* __restrict__ r, double* __restrict__ part) {
+    const long long t = (long long)blockIdx.x * TPB + threadIdx.x;
+    float acc = 0.f;
+    if (t < g.box()) {
+        int i, j, k;
+        g.box_ijk(t, i, j, k);
+        const int s = g.slot(i, j, k);
+        auto ld = [&](int q, F2 (&v)[4]) {
+            const float4 a = __ldg(xh + q), b = __ldg(xl + q);
+            v[0] = f2(a.x, b.x);
+            v[1] = f2(a.y, b.y);
+            v[2] = f2(a.z, b.z);
+            v[3] = f2(a.w, b.w);
+        };
+        F2 c[4], xm[4], xp[4], ym[4], yp[4], zm[4], zp[4];
+        ld(s, c);
+        ld(s - g.di(), xm);
+        ld(s + g.di(), xp);
+        ld(s - g.dj(), ym);
+        ld(s + g.dj(), yp);
+        ld(s - 1, zm);
+        ld(s + 1, zp);
+        const float4 ph = __ldg(Ph + s), pl = __ldg(Pl + s), b0 = __ldg(bh + s), b1 = __ldg(bl + s);
+        const F2 pen[4] = {f2(ph.x, pl.x), f2(ph.y, pl.y), f2(ph.z, pl.z), f2(ph.w, pl.w)};
+        const F2 bb[4] = {f2(b0.x, b1.x), f2(b0.y, b1.y), f2(b0.z, b1.z), f2(b0.w, b1.w)};
+        const F2 six = f2(6.f, 0.f);
+        // the rows of stencil.cuh lap_core
+        const F2 div = df_add(df_add(df_sub(xp[1], c[1]), df_sub(yp[2], c[2])), df_sub(zp[3], c[3]));
+        F2 o[4];
+        o[0] = df_add(df_mul(vol, div), df_mul(pen[0], c[0]));
+        const F2* lo_nb[3] = {xm, ym, zm};
+#pragma unroll
+        for (int d = 1; d <= 3; d++) {
+            F2 l = df_mul(six, c[d]);
+            l = df_sub(l, df_add(xm[d], xp[d]));
+            l = df_sub(l, df_add(ym[d], yp[d]));
+            l = df_sub(l, df_add(zm[d], zp[d]));
+            const F2 gp = df_sub(c[0], lo_nb[d - 1][0]);
+            o[d] = df_add(df_mul(vol, df_sub(l, gp)), df_mul(pen[d], c[d]));
+        }
+        const uint8_t ms = __ldg(m + s);
+        const uint8_t bit[4] = {MP, MU, MV, MW};
+        double rv[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const F2 d = df_sub(bb[q], o[q]);
+            rv[q] = (ms & bit[q]) ? 0.0 : (double)d.h + (double)d.l;
+            const float f = (ms & bit[q]) ? 0.f : d.h;
+            acc += f * f;
+        }
+        store4(r, s, rv[0], rv[1], rv[2], rv[3]);
+    }
+    if (part) {
+        const double v = block_sum((double)acc);
+        if (threadIdx.x == 0) part[blockIdx.x] = v;
+    }
+}
+
+int split64(cudaStream_t st, long long n4, const d4* a, float4* hi, float4* lo) {
+    k_split64<<<grid_for(n4, TPB) > 4096 ? 4096 : grid_for(n4, TPB), TPB, 0, st>>>(n4, a, hi, lo);
+    STG_LAUNCH_CK();
+    return STG_OK;
+}
+
+int resid64_df(cudaStream_t st, const Geom& g, double vol, const float4* xh, const float4* xl, const float4* bh, const float4* bl,
+               const float4* Ph, const float4* Pl, const uint8_t* m, d4* r, double* part, int* nblocks_out) {
+    const unsigned nb = grid_for(g.box(), TPB);
+    if (nblocks_out) *nblocks_out = (int)nb;
+    const float vh = (float)vol;
+    k_resid_df<<<nb, TPB, 0, st>>>(g, F2{vh, (float)(vol - (double)vh)}, xh, xl, bh, bl, Ph, Pl, m, r, part);
+    STG_LAUNCH_CK();
+    return STG_OK;
+}
+
 int half_square64(cudaStream_t st, long long n4, const d4* x, d4* out) {
     long long nb = (4 * n4 + TPB - 1) / TPB;
     k_half_square64<<<(unsigned)(nb > 4096 ? 4096 : nb), TPB, 0, st>>>(4 * n4, reinterpret_cast<const double*>(x),

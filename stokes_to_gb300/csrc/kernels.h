@@ -31,6 +31,12 @@ int sweep_status(cudaStream_t st, int* timed_out);
 // rc = R (rf - A xf) with R the 8-child sum masked by the coarse mask (xf == nullptr: rc = R rf).
 int restrict_resid32(cudaStream_t st, const Geom& gc, const Geom& gf, float volf, const float4* rf, const float4* xf,
                      const uint8_t* mf, const float4* Pf, const uint8_t* mc, float4* rc, bool lap = false);
+// Double-float (hi + lo FP32 words) copies of FP64 vectors and the FP64 residual from them:
+// hi = fl32(a), lo = fl32(a - hi) (hi may be null); r = b - A x in the Laplacian form with
+// per-block partials of |r|^2 (FP32 per slot, FP64 block sums)
+int split64(cudaStream_t st, long long n4, const d4* a, float4* hi, float4* lo);
+int resid64_df(cudaStream_t st, const Geom& g, double vol, const float4* xh, const float4* xl, const float4* bh, const float4* bl,
+               const float4* Ph, const float4* Pl, const uint8_t* m, d4* r, double* part, int* nblocks_out);
 // 1 in *flag (device) when x is nonzero on some fixed or absent unknown of the box, else 0
 int fixed_nonzero(cudaStream_t st, const Geom& g, const d4* x, const uint8_t* m, int* flag);
 // x_f = 0 on every fixed or absent unknown of the box
@@ -72,8 +78,10 @@ int half_square64(cudaStream_t st, long long n4, const d4* x, d4* out);
 int fill_bytes(cudaStream_t st, void* p, size_t bytes);
 int f64_to_f32(cudaStream_t st, long long n4, const d4* a, double scale, float4* out);
 int f32_to_f64(cudaStream_t st, long long n4, const float4* a, d4* out);
-// x64 += alpha * sum_j y[j] z[j]  (z FP32 vectors), y on device (nz entries)
-int axpy_multi_32to64(cudaStream_t st, long long n4, const float4* const* z, const double* y, int nz, double alpha, d4* x);
+// x64 += alpha * sum_j y[j] z[j]  (z FP32 vectors), y on device (nz entries); with xh / xl
+// non-null also writes the double-float copy of the new x there
+int axpy_multi_32to64(cudaStream_t st, long long n4, const float4* const* z, const double* y, int nz, double alpha, d4* x,
+                      float4* xh = nullptr, float4* xl = nullptr);
 // h[j] = <v_j, w> for j < nv (FP32 per-thread partials, FP64 block and grid sums),
 // and <w, w> into *ww when ww != nullptr
 

@@ -158,6 +158,8 @@ int update(stg_t* h) {
     }
     // coarse boundary faces have fixed children, so the Laplacian form carries down
     for (auto& L : h->lv) L.lap = h->lap_ok;
+    // low words of the finest penalty for the double-float residual (P32 holds the high)
+    PROF(h, 8, 0.0, split64(h->st, fine(h).g.nslot, fine(h).P64, nullptr, h->Plo));
     // the coarsest set-up (one launch per Gauss-Jordan pivot) reads and writes fixed buffers:
     // replayed as a CUDA graph; the inverse's buffer pointer is host state
     GraphCache& G = h->sgraph;
@@ -323,7 +325,11 @@ int vcycle(stg_t* h, const float4* rhs) {
 int residual64(stg_t* h, const d4* b, const d4* x, d4* r, double* nrm2_host) {
     Level& F = fine(h);
     int nb = 0;
-    PROF(h, 5, (x ? 129.0 : 65.0) * F.g.box(), op64(h->st, F.g, F.vol, x, F.m, F.P64, b, r, 1, h->d_parts, &nb, fast(h, F)));
+    if (x && x == h->df_x && b == h->df_b && fast(h, F))
+        PROF(h, 5, 129.0 * F.g.box(),
+             resid64_df(h->st, F.g, F.vol, h->xh, h->xl, h->bh, h->bl, F.P32, h->Plo, F.m, r, h->d_parts, &nb));
+    else
+        PROF(h, 5, (x ? 129.0 : 65.0) * F.g.box(), op64(h->st, F.g, F.vol, x, F.m, F.P64, b, r, 1, h->d_parts, &nb, fast(h, F)));
     STG_TRY(reduce_parts(h->st, h->d_parts, nb, h->dnrm));
     STG_CK(cudaMemcpyAsync(nrm2_host, h->dnrm, sizeof(double), cudaMemcpyDeviceToHost, h->st));
     STG_CK(cudaStreamSynchronize(h->st));
@@ -420,6 +426,20 @@ int solve_core(stg_t* h, const d4* b, d4* x, stg_stats* stats) {
     int status = STG_E_NOT_CONVERGED;
     // a zero start makes the first residual b itself (fixed rows cleared in the Laplacian form)
     const bool x_zero = !(h->opts.warm_start && h->has_x0(x));
+    // double-float copies of x and b for the FP64 residual (3D Laplacian form)
+    const bool df = h->dim == 3 && fast(h, fine(h));
+    h->df_x = h->df_b = nullptr;
+    if (df) {
+        if (x_zero) {
+            STG_CK(cudaMemsetAsync(h->xh, 0, sizeof(float4) * n4, h->st));
+            STG_CK(cudaMemsetAsync(h->xl, 0, sizeof(float4) * n4, h->st));
+        } else {
+            PROF(h, 6, 64.0 * n4, split64(h->st, n4, x, h->xh, h->xl));
+        }
+        PROF(h, 6, 64.0 * n4, split64(h->st, n4, b, h->bh, h->bl));
+        h->df_x = x;
+        h->df_b = b;
+    }
     for (int outer = 0; outer <= h->opts.max_outer; outer++) {
         double rn2 = 0;
         STG_TRY(h->resid64(h, b, (outer == 0 && x_zero && h->dim == 3) ? nullptr : x, h->r64, &rn2));
@@ -544,8 +564,10 @@ int solve_core(stg_t* h, const d4* b, d4* x, stg_stats* stats) {
         }
         for (int q = 0; q < k; q++) y[q] *= sig[q];  // z_q = sig_q Z_q
         STG_CK(cudaMemcpyAsync(h->dy, y.data(), sizeof(double) * k, cudaMemcpyHostToDevice, h->st));
-        PROF(h, 6, (16.0 * k + 64.0) * n4, axpy_multi_32to64(h->st, n4, h->Z.data(), h->dy, k, rn, x));
+        PROF(h, 6, (16.0 * k + 64.0) * n4,
+             axpy_multi_32to64(h->st, n4, h->Z.data(), h->dy, k, rn, x, df ? h->xh : nullptr, df ? h->xl : nullptr));
     }
+    h->df_x = h->df_b = nullptr;  // finish() changes x; adapters must not see the copies
     if (h->finish) STG_TRY(h->finish(h, b, x));
     int sweep_timeout = 0;
     STG_TRY(sweep_status(h->st, &sweep_timeout));
@@ -753,7 +775,9 @@ int stg_create(int dim, int n, const stg_opts* opts, stg_t** out) {
     }
     const size_t ns = (size_t)h->n4;
     if ((rc = dalloc(&h->b64, ns)) || (rc = dalloc(&h->x64, ns)) || (rc = dalloc(&h->r64, ns)) || (rc = dalloc(&h->t64, ns)) ||
-        (rc = dalloc(&h->lam64, ns)) || (rc = dalloc(&h->w, ns)))
+        (rc = dalloc(&h->lam64, ns)) || (rc = dalloc(&h->w, ns)) ||
+        (dim == 3 && ((rc = dalloc(&h->xh, ns)) || (rc = dalloc(&h->xl, ns)) || (rc = dalloc(&h->bh, ns)) || (rc = dalloc(&h->bl, ns)) ||
+                      (rc = dalloc(&h->Plo, ns)))))
         return fail(rc);
     h->V.assign(h->m + 1, nullptr);
     h->Z.assign(h->m, nullptr);
@@ -797,6 +821,7 @@ int stg_destroy(stg_t* h) {
     dense_free(h->dense);
     for (d4* p : {h->b64, h->x64, h->r64, h->t64, h->lam64}) cudaFree(p);
     cudaFree(h->w);
+    for (float4* p : {h->xh, h->xl, h->bh, h->bl, h->Plo}) cudaFree(p);
     for (auto p : h->V) cudaFree(p);
     for (auto p : h->Z) cudaFree(p);
     for (double* p : {h->dscr, h->dh, h->dnrm, h->dy, h->dsig2, h->stage, h->d_design, h->d_phys, h->d_sens, h->d_sens_design, h->d_vw,

@@ -1023,7 +1023,7 @@ int sweep32(cudaStream_t st, const Geom& g, float vol, const float4* r, const fl
     }
     // planes per block: long marches on big grids (prologue amortised), short ones on the
     // coarse levels, where the sequential march, not bandwidth, sets the time
-    const int chunk = g.n >= 192 ? 32 : g.n >= 96 ? 16 : g.n >= 48 ? 8 : g.n >= 24 ? 4 : 2;
+    const int chunk = g.n >= 192 ? 32 : g.n >= 96 ? 8 : g.n >= 48 ? 4 : g.n >= 24 ? 2 : 1;
     dim3 grid((g.n + SK) / SK, (g.n + SJ) / SJ, (g.n + chunk) / chunk), block(SK, SJ);
     if (lap && encoder()) {
         static bool tattr = false;
