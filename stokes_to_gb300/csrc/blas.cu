@@ -2,6 +2,7 @@
 // dot products and updates for the Arnoldi step, and deterministic reductions (fixed
 // grid, partials summed in a fixed order, so repeated runs are bitwise identical).
 #include "kernels.h"
+#include "stencil.cuh"
 
 namespace stg {
 
@@ -120,6 +121,44 @@ __global__ void __launch_bounds__(TPB) k_multidot32(long long n4, Tab v, const f
             acc[q] += a.x * b.x + a.y * b.y + a.z * b.z + a.w * b.w;
         }
         if (WW) acc[NV] += a.x * a.x + a.y * a.y + a.z * a.z + a.w * a.w;
+    }
+    double d[NV + 1];
+#pragma unroll
+    for (int q = 0; q <= NV; q++) d[q] = acc[q];
+    block_sums<NV + 1>(d, part + (long long)blockIdx.x * (MAXV + 1));
+}
+
+// The FGMRES operator fused with the first multi-dot of the Arnoldi step, in the
+// Laplacian form: w = v - A z over the box slots (rows of fixed unknowns 0), written out,
+// and per-block partials of <V_q, w> and <w, w> (w never re-read from memory for them).
+template <int NV>
+__global__ void __launch_bounds__(TPB) k_shift_dots(Geom g, float vol, const float4* __restrict__ v, const float4* __restrict__ z,
+                                                    const uint8_t* __restrict__ m, const float4* __restrict__ P, Tab V,
+                                                    float4* __restrict__ w, double* __restrict__ part) {
+    float acc[NV + 1];
+#pragma unroll
+    for (int q = 0; q <= NV; q++) acc[q] = 0.f;
+    const long long nb = g.box();
+    for (long long t = (long long)blockIdx.x * TPB + threadIdx.x; t < nb; t += (long long)gridDim.x * TPB) {
+        int i, j, k;
+        g.box_ijk(t, i, j, k);
+        const int s = g.slot(i, j, k);
+        float o[4];
+        lap_rows<float>(z, P, s, g.di(), g.dj(), vol, o);
+        const float4 vv = __ldg(v + s);
+        o[0] = vv.x - o[0];
+        o[1] = vv.y - o[1];
+        o[2] = vv.z - o[2];
+        o[3] = vv.w - o[3];
+        mask4<float>(__ldg(m + s), o);
+        const float4 a = make_float4(o[0], o[1], o[2], o[3]);
+        w[s] = a;
+#pragma unroll
+        for (int q = 0; q < NV; q++) {
+            const float4 b = __ldg(V.p[q] + s);
+            acc[q] += a.x * b.x + a.y * b.y + a.z * b.z + a.w * b.w;
+        }
+        acc[NV] += a.x * a.x + a.y * a.y + a.z * a.z + a.w * a.w;
     }
     double d[NV + 1];
 #pragma unroll
@@ -317,6 +356,30 @@ int axpy_multi_32to64(cudaStream_t st, long long n4, const float4* const* z, con
         dispatch_nv<AxpyL>(nb, st, n4, t, y + j0, alpha, x, last ? xh : nullptr, last ? xl : nullptr);
         STG_LAUNCH_CK();
     }
+    return STG_OK;
+}
+
+template <int NV>
+struct ShiftL {
+    static void run(cudaStream_t st, const Geom& g, float vol, const float4* v, const float4* z, const uint8_t* m, const float4* P,
+                    const Tab& t, float4* w, double* part) {
+        k_shift_dots<NV><<<RGRID, TPB, 0, st>>>(g, vol, v, z, m, P, t, w, part);
+    }
+};
+
+int shift_multidot32(cudaStream_t st, const Geom& g, float vol, const float4* v, const float4* z, const uint8_t* m, const float4* P,
+                     long long n4, const float4* const* V, int nv, float4* w, double* h, double* scratch, double* ww) {
+    const int nb = nv < MAXV ? nv : MAXV;
+    Tab t{};
+    for (int q = 0; q < nb; q++) t.p[q] = V[q];
+    dispatch_nv<ShiftL>(nb, st, g, vol, v, z, m, P, t, w, scratch);
+    STG_LAUNCH_CK();
+    k_reduce_cols<<<1, TPB, 0, st>>>(scratch, RGRID, MAXV + 1, nb, h);
+    STG_LAUNCH_CK();
+    k_reduce_cols<<<1, TPB, 0, st>>>(scratch + nb, RGRID, MAXV + 1, 1, ww);
+    STG_LAUNCH_CK();
+    // basis vectors past the first MAXV: a plain multi-dot pass over the written w
+    if (nv > MAXV) STG_TRY(multidot32(st, n4, V + MAXV, nv - MAXV, w, h + MAXV, scratch, nullptr));
     return STG_OK;
 }
 

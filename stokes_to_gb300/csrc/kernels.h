@@ -87,6 +87,10 @@ int axpy_multi_32to64(cudaStream_t st, long long n4, const float4* const* z, con
 
 int multidot32(cudaStream_t st, long long n4, const float4* const* v, int nv, const float4* w, double* h, double* scratch,
                double* ww);
+// w = v - A z (Laplacian form, slot layout of g) fused with h[q] = <V_q, w> (q < nv) and
+// <w, w> into *ww (device)
+int shift_multidot32(cudaStream_t st, const Geom& g, float vol, const float4* v, const float4* z, const uint8_t* m, const float4* P,
+                     long long n4, const float4* const* V, int nv, float4* w, double* h, double* scratch, double* ww);
 // w -= sum_j h[j] v_j ; then returns ||w||^2 into nrm2 (device)
 int multiaxpy32_norm(cudaStream_t st, long long n4, const float4* const* v, int nv, const double* h, float4* w, double* nrm2,
                      double* scratch);

@@ -482,8 +482,16 @@ int solve_core(stg_t* h, const d4* b, d4* x, stg_stats* stats) {
             // Arnoldi on the shifted operator A M - I, written as w = V_j - A Z_j: same Krylov
             // space, and a good preconditioner (A M near I) no longer leaves w dominated by
             // V_j, whose removal cancelled most of w and forced the second projection pass
-            STG_TRY(h->shift32(h, h->V[j], h->Z[j], h->w));
-            PROF(h, 6, 16.0 * (j + 2) * n4, multidot32(h->st, n4, h->V.data(), j + 1, h->w, h->dh, h->dscr, h->dnrm + 1));
+            if (h->dim == 3 && fast(h, fine(h))) {
+                // one pass: the operator and the first multi-dot (w is not re-read)
+                Level& F = fine(h);
+                PROF(h, 6, (65.0 + 16.0 * (j + 1)) * F.g.box(),
+                     shift_multidot32(h->st, F.g, (float)F.vol, h->V[j], h->Z[j], F.m, F.P32, n4, h->V.data(), j + 1, h->w, h->dh,
+                                      h->dscr, h->dnrm + 1));
+            } else {
+                STG_TRY(h->shift32(h, h->V[j], h->Z[j], h->w));
+                PROF(h, 6, 16.0 * (j + 2) * n4, multidot32(h->st, n4, h->V.data(), j + 1, h->w, h->dh, h->dscr, h->dnrm + 1));
+            }
             PROF(h, 6, 16.0 * (j + 3) * n4,
                  project32(h->st, n4, h->V.data(), j + 1, h->dh, h->dsig2, h->w, h->V[j + 1], h->dh + m + 2, h->dnrm, h->dscr));
             std::vector<double> h1(j + 1), h2(j + 1, 0.0);
