@@ -117,6 +117,18 @@ void add_launches(long long k);
         STG_CK(cudaGetLastError()); \
     } while (0)
 
+// One-time per-device state (kernel attributes, device flags) is kept per device ordinal:
+// these are properties of a device, and a process may drive several.
+constexpr int MAX_DEVICES = 64;
+inline int device_slot() {
+    int d = 0;
+    if (cudaGetDevice(&d) != cudaSuccess || d < 0 || d >= MAX_DEVICES) {
+        cudaGetLastError();
+        return -1;
+    }
+    return d;
+}
+
 inline unsigned grid_for(long long work, int block) {
     long long g = (work + block - 1) / block;
     return (unsigned)(g < 1 ? 1 : g);

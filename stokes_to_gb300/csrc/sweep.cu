@@ -998,51 +998,57 @@ bool slot_map(EncodeTiled enc, CUtensorMap* map, const void* base, const Geom& g
                CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-int* g_sweep_err = nullptr;  // set by a TMA sweep whose wait gave up (device)
+// per device: kernel attributes set, and the flag a TMA sweep sets when its wait gave up
+bool g_attr_set[MAX_DEVICES] = {}, g_tattr_set[MAX_DEVICES] = {};
+int* g_sweep_err[MAX_DEVICES] = {};
 
 }  // namespace
 
 int sweep_status(cudaStream_t st, int* timed_out) {
     *timed_out = 0;
-    if (!g_sweep_err) return STG_OK;
-    STG_CK(cudaMemcpyAsync(timed_out, g_sweep_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    const int dev = device_slot();
+    if (dev < 0 || !g_sweep_err[dev]) return STG_OK;
+    STG_CK(cudaMemcpyAsync(timed_out, g_sweep_err[dev], sizeof(int), cudaMemcpyDeviceToHost, st));
     STG_CK(cudaStreamSynchronize(st));
     return STG_OK;
 }
 
 int sweep32(cudaStream_t st, const Geom& g, float vol, const float4* r, const float4* xin, float4* xout, const uint8_t* m,
             const float4* P, int flag, bool lap) {
-    static bool attr_set = false;
+    const int dev = device_slot();
+    if (dev < 0) {
+        set_error("sweep32: device ordinal beyond %d", MAX_DEVICES - 1);
+        return STG_E_UNSUPPORTED;
+    }
     const int smem = (int)sizeof(Smem), smem_l = (int)sizeof(SmemL);
-    if (!attr_set) {
+    if (!g_attr_set[dev]) {
         STG_CK(cudaFuncSetAttribute(k_sweep<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
         STG_CK(cudaFuncSetAttribute(k_sweep<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
         STG_CK(cudaFuncSetAttribute(k_sweep_lap<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_l));
         STG_CK(cudaFuncSetAttribute(k_sweep_lap<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_l));
-        attr_set = true;
+        g_attr_set[dev] = true;
     }
     // planes per block: long marches on big grids (prologue amortised), short ones on the
     // coarse levels, where the sequential march, not bandwidth, sets the time
     const int chunk = g.n >= 192 ? 32 : g.n >= 96 ? 8 : g.n >= 48 ? 4 : g.n >= 24 ? 2 : 1;
     dim3 grid((g.n + SK) / SK, (g.n + SJ) / SJ, (g.n + chunk) / chunk), block(SK, SJ);
     if (lap && encoder()) {
-        static bool tattr = false;
         const int smem_t = (int)sizeof(SmemT);
-        if (!tattr) {
+        if (!g_tattr_set[dev]) {
             STG_CK(cudaFuncSetAttribute(k_sweep_tma<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_t));
             STG_CK(cudaFuncSetAttribute(k_sweep_tma<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_t));
-            STG_CK(cudaMalloc((void**)&g_sweep_err, sizeof(int)));
-            STG_CK(cudaMemset(g_sweep_err, 0, sizeof(int)));
-            tattr = true;
+            STG_CK(cudaMalloc((void**)&g_sweep_err[dev], sizeof(int)));
+            STG_CK(cudaMemset(g_sweep_err[dev], 0, sizeof(int)));
+            g_tattr_set[dev] = true;
         }
         CUtensorMap mx{}, mr{}, mp{};
         const EncodeTiled enc = encoder();
         const bool ok = (!xin || slot_map(enc, &mx, xin, g, XK, XJ)) && slot_map(enc, &mr, r, g, RK, RJ) && slot_map(enc, &mp, P, g, RK, RJ);
         if (ok) {
             if (xin)
-                k_sweep_tma<true><<<grid, block, smem_t, st>>>(mx, mr, mp, g, vol, xout, m, flag, chunk, g_sweep_err);
+                k_sweep_tma<true><<<grid, block, smem_t, st>>>(mx, mr, mp, g, vol, xout, m, flag, chunk, g_sweep_err[dev]);
             else
-                k_sweep_tma<false><<<grid, block, smem_t, st>>>(mr, mr, mp, g, vol, xout, m, flag, chunk, g_sweep_err);
+                k_sweep_tma<false><<<grid, block, smem_t, st>>>(mr, mr, mp, g, vol, xout, m, flag, chunk, g_sweep_err[dev]);
             STG_LAUNCH_CK();
             return STG_OK;
         }

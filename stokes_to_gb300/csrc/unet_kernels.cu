@@ -18,7 +18,6 @@
 namespace stg {
 
 extern bool g_conv_tc;
-extern int* g_tc_err;
 
 namespace {
 
@@ -465,10 +464,11 @@ TcPlan tc_plan(int n, int cout) {
 template <int C, bool F32>
 int launch_tc(const TcPlan& P, cudaStream_t st, const __nv_bfloat16* in, int cin, int ldin, const __nv_bfloat16* w, int wtap,
               const float* bias, void* out, int ldout, int n, int relu, int* err) {
-    static bool attr = false;
-    if (!attr) {
+    static bool attr[MAX_DEVICES] = {};
+    const int dev = device_slot();
+    if (dev >= 0 && !attr[dev]) {
         STG_CK(cudaFuncSetAttribute(k_conv3_tc<C, F32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM_MAX));
-        attr = true;
+        attr[dev] = true;
     }
     dim3 grid((n + P.P - 1) / P.P, (n + P.J - 1) / P.J);
     k_conv3_tc<C, F32><<<grid, 128, P.smem, st>>>(in, cin, ldin, w, wtap, bias, out, ldout, n, relu, P.J, P.T, P.P, P.ncols, err);
@@ -492,14 +492,15 @@ void launch_dw(dim3 grid, cudaStream_t st, const __nv_bfloat16* x, int ldx, cons
 }  // namespace
 
 // tensor-core convolutions on (default) or the mma.sync kernel for every shape; the
-// error flag of the tcgen05 kernel's bounded waits (device, 0 = no timeout)
+// error flag of the tcgen05 kernel's bounded waits, per device (0 = no timeout)
 bool g_conv_tc = true;
-int* g_tc_err = nullptr;
+static int* g_tc_err[MAX_DEVICES] = {};
 
 int conv3_tc_status(cudaStream_t st, int* timed_out) {
     *timed_out = 0;
-    if (!g_tc_err) return STG_OK;
-    STG_CK(cudaMemcpyAsync(timed_out, g_tc_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    const int dev = device_slot();
+    if (dev < 0 || !g_tc_err[dev]) return STG_OK;
+    STG_CK(cudaMemcpyAsync(timed_out, g_tc_err[dev], sizeof(int), cudaMemcpyDeviceToHost, st));
     STG_CK(cudaStreamSynchronize(st));
     return STG_OK;
 }
@@ -519,18 +520,23 @@ int conv3_forward(cudaStream_t st, const __nv_bfloat16* in, int cin, int ldin, c
     if (g_conv_tc && cout % 16 == 0 && ldin % 8 == 0 && wtap % 8 == 0 && ((uintptr_t)in & 15) == 0 && ((uintptr_t)w & 15) == 0 &&
         ((uintptr_t)out & 15) == 0 && ldout % 8 == 0) {
         const TcPlan P = tc_plan(n, cout);
-        if (P.J) {
-            if (!g_tc_err) STG_CK(cudaMalloc((void**)&g_tc_err, sizeof(int)));
+        const int dev = device_slot();
+        if (P.J && dev >= 0) {
+            if (!g_tc_err[dev]) {
+                STG_CK(cudaMalloc((void**)&g_tc_err[dev], sizeof(int)));
+                STG_CK(cudaMemset(g_tc_err[dev], 0, sizeof(int)));
+            }
+            int* const err = g_tc_err[dev];
             int rc = STG_OK;
             switch (cout) {
-                case 16: rc = f32_out ? launch_tc<16, true>(P, st, in, cin, ldin, w, wtap, bias, out, ldout, n, relu, g_tc_err)
-                                      : launch_tc<16, false>(P, st, in, cin, ldin, w, wtap, bias, out, ldout, n, relu, g_tc_err); break;
-                case 32: rc = f32_out ? launch_tc<32, true>(P, st, in, cin, ldin, w, wtap, bias, out, ldout, n, relu, g_tc_err)
-                                      : launch_tc<32, false>(P, st, in, cin, ldin, w, wtap, bias, out, ldout, n, relu, g_tc_err); break;
-                case 48: rc = f32_out ? launch_tc<48, true>(P, st, in, cin, ldin, w, wtap, bias, out, ldout, n, relu, g_tc_err)
-                                      : launch_tc<48, false>(P, st, in, cin, ldin, w, wtap, bias, out, ldout, n, relu, g_tc_err); break;
-                default: rc = f32_out ? launch_tc<64, true>(P, st, in, cin, ldin, w, wtap, bias, out, ldout, n, relu, g_tc_err)
-                                      : launch_tc<64, false>(P, st, in, cin, ldin, w, wtap, bias, out, ldout, n, relu, g_tc_err); break;
+                case 16: rc = f32_out ? launch_tc<16, true>(P, st, in, cin, ldin, w, wtap, bias, out, ldout, n, relu, err)
+                                      : launch_tc<16, false>(P, st, in, cin, ldin, w, wtap, bias, out, ldout, n, relu, err); break;
+                case 32: rc = f32_out ? launch_tc<32, true>(P, st, in, cin, ldin, w, wtap, bias, out, ldout, n, relu, err)
+                                      : launch_tc<32, false>(P, st, in, cin, ldin, w, wtap, bias, out, ldout, n, relu, err); break;
+                case 48: rc = f32_out ? launch_tc<48, true>(P, st, in, cin, ldin, w, wtap, bias, out, ldout, n, relu, err)
+                                      : launch_tc<48, false>(P, st, in, cin, ldin, w, wtap, bias, out, ldout, n, relu, err); break;
+                default: rc = f32_out ? launch_tc<64, true>(P, st, in, cin, ldin, w, wtap, bias, out, ldout, n, relu, err)
+                                      : launch_tc<64, false>(P, st, in, cin, ldin, w, wtap, bias, out, ldout, n, relu, err); break;
             }
             STG_TRY(rc);
             STG_LAUNCH_CK();
