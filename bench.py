@@ -3,7 +3,7 @@
 One step = one full solve (coarse re-discretisation, coarsest inverse, FP32 V-cycle
 FGMRES inside FP64 refinement) of the 256^3 parabolic-inlet problem with a seeded,
 Gaussian-smoothed density (sigma 4 cells), density filter r = 1.5 and the
-Borrvall-Petersson alpha law (amax 1e4). Working set is ~25 GB, far above the 129 MB L2.
+Borrvall-Petersson alpha law (amax 1e4). Working set is ~27 GB, far above the 129 MB L2.
 
   value  device-resident inputs, CUDA events on the solve stream (method: plain, the
          library default: FP32 V-cycle with one smoother sweep per colour, FGMRES in FP64
@@ -449,7 +449,7 @@ def run_ours(args):
                        "n": n, "method": "plain (FP32 V-cycle, 1 smoother sweep per colour, FGMRES in FP64 refinement)",
                        "tol": TOL, "bc": "parabolic inlet N/4 patch, mirrored outlet",
                        "density": "seeded U[0,1], Gaussian sigma 4, filter r 1.5, BP alpha amax 1e4",
-                       "l2": "inputs larger than L2 (~25 GB working set)", "parallelism": f"replicas x{world}"},
+                       "l2": "inputs larger than L2 (~27 GB working set)", "parallelism": f"replicas x{world}"},
             "e2e": {"value": e2e_value, "unit": "s/solve", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": launches,
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
