@@ -56,7 +56,9 @@ typedef struct stg_opts {
     int smooth_sweeps;   /* sweeps per colour in the solver's smoother: 1 (default; 0 means
                             1) or 2, the reference's DescentSmoother. At 256^3 one sweep per
                             colour reaches the same FP64 tolerance in as many V-cycles at
-                            2/3 of the time. The LinearMapping adapters always run the
+                            2/3 of the time. A refinement step that uses the whole basis
+                            without reaching its target raises it to 2 for the rest of
+                            the solve (3D). The LinearMapping adapters always run the
                             reference smoother. */
     int warm_start;      /* 1: start each solve from the previous solution of the same
                             equation (the forward one for stg_solve, the adjoint one for
@@ -142,7 +144,13 @@ int stg_set_rhs(stg_t* h, const double* cell_b, const double* const* face_b);
 /* FluidSteadyState3D::solve() (:152-170): coarse re-discretisation, smoother and
  * coarsest set-up, then the Krylov solve from a zero initial guess. The results go to
  * p_out (cells) and vel_out[dim] (faces), the public members p and vel of the
- * reference; either may be NULL to keep the solution on the device only. */
+ * reference; either may be NULL to keep the solution on the device only.
+ * The solver's own coarse levels differ from the reference's in one rule: a coarse
+ * velocity unknown carries 2^dim x the smallest penalty of its free children, not their
+ * sum, so that channels narrower than a coarse cell stay open on the coarse levels (with
+ * the sum, solves on optimised high-contrast designs stagnate). The adapters below
+ * (stg_update, stg_vcycle_device, stg_apply_op_device, stg_level_descr_device) keep the
+ * reference's sums; the two set-ups replace each other as the calls alternate. */
 int stg_solve(stg_t* h, double* p_out, double* const* vel_out, stg_stats* stats);
 
 /* Copies the last solution to host Field arrays. */

@@ -74,6 +74,12 @@ struct stg_ctx {
     // lap_ok: the boundary admits the Laplacian form; general: force the masked general
     // stencil (set while an adapter works on a vector that is nonzero on fixed unknowns)
     bool lap_ok = false, general = false, reference_cycle = false;
+    // the coarse levels hold the solver's own penalties (flow rule of kernels.cu k_coarsen)
+    // rather than the reference's sums, which the component adapters reproduce
+    bool hier_flow = false;
+    // a refinement step of the solve in progress ended at the basis limit short of its
+    // target: the rest of the solve smooths with at least two sweeps per colour
+    bool boost = false;
     bool x0_valid[2] = {false, false};  // x64 / lam64 hold a previous solution (warm start)
     bool has_x0(const stg::d4* x) const { return (x == x64 && x0_valid[0]) || (x == lam64 && x0_valid[1]); }
     int* dflag = nullptr;
@@ -109,6 +115,7 @@ struct stg_ctx {
     struct Ctx2* c2 = nullptr;        // 2D state (dim == 2)
     struct MmaState* mma = nullptr;   // MMA optimizer state (mma.cu), created on first use
     GraphCache vgraph;                // the V-cycle below the finest level (3D) or all of it (2D)
+    GraphCache vgraph_boost;          // the 3D one while `boost` raises the sweeps
     GraphCache sgraph;                // the coarsest-level set-up (probes and Gauss-Jordan inverse)
     struct NetState* net = nullptr;   // learned preconditioner (unet.cu), stg_net_init
     bool net_on = false;              // LEARNED: the network is in use in the current refinement step
@@ -142,6 +149,8 @@ int apply_op2d(stg_t* h, int op, int level, double* out, const double* in);
 int level_descr2d(stg_t* h, int level, double* vol, double* pen, uint8_t* fixed);
 
 Level& fine(stg_t* h);
+// builds the hierarchy for the adapters (reference = true) or the solves (solver.cu)
+int ensure_setup(stg_t* h, bool reference);
 // runs body() through a CUDA-graph cache (solver.cu)
 int graphed(stg_t* h, GraphCache& G, long long key, const std::function<int()>& body, const std::function<void(bool)>& state);
 bool fast(const stg_t* h, const Level& L);

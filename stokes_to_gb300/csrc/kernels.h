@@ -48,9 +48,10 @@ int prolong_add32(cudaStream_t st, const Geom& gf, const Geom& gc, const float4*
 // same with BF16-stored coarse correction
 int prolong_add_bf16(cudaStream_t st, const Geom& gf, const Geom& gc, const __nv_bfloat16* xc, const uint8_t* mf, float4* xf);
 int to_bf16(cudaStream_t st, const Geom& g, const float4* x, __nv_bfloat16* y);
-// coarse descriptor from the fine one (updateSubSystem + finish)
+// coarse descriptor from the fine one (updateSubSystem + finish); flow: velocity penalties
+// by 8 x the smallest free child instead of the sum (the solver's own hierarchy)
 int coarsen(cudaStream_t st, const Geom& gc, const Geom& gf, const uint8_t* mf, const d4* Pf, uint8_t* mc, d4* Pc64,
-            float4* Pc32);
+            float4* Pc32, bool flow);
 // FP64 restriction / prolongation (component adapters): rc = fix_c R rf ; xf = fix_f P xc
 int restrict64(cudaStream_t st, const Geom& gc, const Geom& gf, const d4* rf, const uint8_t* mc, d4* rc);
 int prolong64(cudaStream_t st, const Geom& gf, const Geom& gc, const d4* xc, const uint8_t* mf, d4* xf);

@@ -152,7 +152,7 @@ int update(stg_t* h) {
     }
     for (int i = h->L - 2; i >= 0; i--) {
         Level &c = h->lv[i], &f = h->lv[i + 1];
-        PROF(h, 8, 0.0, coarsen(h->st, c.g, f.g, f.m, f.P64, c.m, c.P64, c.P32));
+        PROF(h, 8, 0.0, coarsen(h->st, c.g, f.g, f.m, f.P64, c.m, c.P64, c.P32, h->hier_flow));
         c.vol = 4.0 * f.vol;
         c.cell_vol = 8.0 * f.cell_vol;
     }
@@ -176,6 +176,16 @@ int update(stg_t* h) {
     return STG_OK;
 }
 
+// Builds the hierarchy when it is missing or was built for the other kind of caller: the
+// component adapters (reference = true) reproduce the reference's coarse penalties, the
+// solves use the flow rule.
+int ensure_setup(stg_t* h, bool reference) {
+    const bool flow = !reference;
+    if (h->updated && h->hier_flow == flow) return STG_OK;
+    h->hier_flow = flow;
+    return h->setup(h);
+}
+
 // ---------------------------------------------------------------- V-cycle (FP32)
 // Smoother of StokeLike::GenerateJacobiPreconditioner(grid, A, 2) (stoke/StokeLike.cu:345-372):
 // DescentSmoother({red, black}, {2, 2}) before the coarse correction and {black, red} after
@@ -194,9 +204,16 @@ int sweep(stg_t* h, Level& L, const float4* r, int flag, bool first) {
     return STG_OK;
 }
 
+// Sweeps per colour: the reference's 2 for the adapters, else the solver option, raised to
+// 2 for the rest of a solve whose refinement step stalled.
+int sweeps_per_colour(const stg_t* h) {
+    if (h->reference_cycle) return 2;
+    const int s = std::max(1, std::min(4, h->opts.smooth_sweeps));
+    return h->boost ? std::max(s, 2) : s;
+}
+
 int smooth(stg_t* h, Level& L, const float4* r, bool post, bool x_is_zero) {
-    // sweeps per colour: the reference's 2, or the solver option (adapters keep the reference)
-    const int per = h->reference_cycle ? 2 : std::max(1, std::min(4, h->opts.smooth_sweeps));
+    const int per = sweeps_per_colour(h);
     int s = 0;
     for (int c = 0; c < 2; c++) {
         const int flag = post ? 1 - c : c;
@@ -283,12 +300,12 @@ int graphed(stg_t* h, GraphCache& G, long long key, const std::function<int()>& 
 // the same launch sequence on every call and runs as a replayed CUDA graph.
 int coarse_cycle(stg_t* h) {
     const int top = h->L - 2;
-    const int per = h->reference_cycle ? 2 : std::max(1, std::min(4, h->opts.smooth_sweeps));
+    const int per = sweeps_per_colour(h);
     // the coarsest inverse lives in one of two buffers (fixed per handle): part of the key
     const long long key = (long long)per | ((long long)(h->opts.method == STG_METHOD_MIXED) << 3) |
                           ((long long)fast(h, h->lv[top]) << 4) | ((long long)(h->dense.inv == h->dense.Ainv) << 5) |
                           ((long long)h->L << 6);
-    GraphCache& G = h->vgraph;
+    GraphCache& G = h->boost && !h->reference_cycle ? h->vgraph_boost : h->vgraph;
     return graphed(h, G, key, [&] { return vcycle_levels(h, top, nullptr); },
                    [&](bool save) {
                        if (save) {
@@ -397,9 +414,9 @@ int finish3(stg_t* h, const d4* b, d4* x) {
 int solve_core(stg_t* h, const d4* b, d4* x, stg_stats* stats) {
     const long long n4 = h->n4;
     stg_stats S{};
-    if (!h->updated) {
+    if (!h->updated || !h->hier_flow) {
         auto t0 = std::chrono::steady_clock::now();
-        STG_TRY(h->setup(h));
+        STG_TRY(ensure_setup(h, false));
         STG_CK(cudaStreamSynchronize(h->st));
         S.setup_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     }
@@ -421,6 +438,11 @@ int solve_core(stg_t* h, const d4* b, d4* x, stg_stats* stats) {
     STG_CK(cudaStreamSynchronize(h->st));
     const double bn = std::sqrt(bn2);
     const int m = h->m;
+    struct BoostGuard {
+        stg_t* h;
+        ~BoostGuard() { h->boost = false; }
+    } boost_guard{h};
+    h->boost = false;
     std::vector<double> H((size_t)(m + 1) * m), cs(m), sn(m), g(m + 1), y(m), hcol(m + 2), sig(m + 1);
     double rel = 0, rn = 0;
     int status = STG_E_NOT_CONVERGED;
@@ -574,6 +596,10 @@ int solve_core(stg_t* h, const d4* b, d4* x, stg_stats* stats) {
         STG_CK(cudaMemcpyAsync(h->dy, y.data(), sizeof(double) * k, cudaMemcpyHostToDevice, h->st));
         PROF(h, 6, (16.0 * k + 64.0) * n4,
              axpy_multi_32to64(h->st, n4, h->Z.data(), h->dy, k, rn, x, df ? h->xh : nullptr, df ? h->xl : nullptr));
+        // the step used the whole basis short of its target: the V-cycle is too weak for this
+        // design (high-contrast optimised densities), so the rest of the solve smooths twice
+        // per colour (about 1.5x the V-cycle's cost for 1.5-2x fewer V-cycles there)
+        if (h->dim == 3 && k == m && std::fabs(g[k]) > itol * beta) h->boost = true;
     }
     h->df_x = h->df_b = nullptr;  // finish() changes x; adapters must not see the copies
     if (h->finish) STG_TRY(h->finish(h, b, x));
@@ -1219,7 +1245,7 @@ int stg_apply_A_device(stg_t* h, int level, double* d_Ap, const double* d_p) {
         set_error("bad level or pointer");
         return STG_E_INVALID;
     }
-    if (level < h->L - 1 && !h->updated) STG_TRY(h->setup(h));
+    if (level < h->L - 1) STG_TRY(ensure_setup(h, true));
     if (h->dim == 2) {
         STG_TRY(apply_A2d(h, level, d_Ap, d_p));
         STG_CK(cudaStreamSynchronize(h->st));
@@ -1253,6 +1279,7 @@ int stg_apply_E_device(stg_t* h, double* d_Ap, const double* d_p) {
 
 int stg_update(stg_t* h) {
     STG_TRY(check_handle(h));
+    h->hier_flow = false;  // FluidSteadyState3D::update: the reference's hierarchy
     STG_TRY(h->setup(h));
     STG_CK(cudaStreamSynchronize(h->st));
     return STG_OK;
@@ -1260,7 +1287,7 @@ int stg_update(stg_t* h) {
 
 int stg_vcycle_device(stg_t* h, double* d_out, const double* d_in) {
     STG_TRY(check_handle(h));
-    if (!h->updated) STG_TRY(h->setup(h));
+    STG_TRY(ensure_setup(h, true));
     if (h->dim == 2) {
         STG_TRY(vcycle2d(h, d_out, d_in));
         STG_CK(cudaStreamSynchronize(h->st));
@@ -1285,7 +1312,7 @@ int stg_apply_op_device(stg_t* h, int op, int level, double* d_out, const double
         set_error("bad level or pointer");
         return STG_E_INVALID;
     }
-    if (!h->updated) STG_TRY(h->setup(h));
+    STG_TRY(ensure_setup(h, true));
     if (h->dim == 2) {
         STG_TRY(apply_op2d(h, op, level, d_out, d_in));
         STG_CK(cudaStreamSynchronize(h->st));
@@ -1356,7 +1383,7 @@ int stg_level_descr_device(stg_t* h, int level, double* d_vol, double* d_penalty
         set_error("bad level");
         return STG_E_INVALID;
     }
-    if (!h->updated) STG_TRY(h->setup(h));
+    STG_TRY(ensure_setup(h, true));
     if (h->dim == 2) {
         STG_TRY(level_descr2d(h, level, d_vol, d_penalty, d_fixed));
         STG_CK(cudaStreamSynchronize(h->st));

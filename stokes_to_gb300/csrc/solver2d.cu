@@ -245,6 +245,10 @@ __device__ __forceinline__ bool padded2(const G2d& g, int kind, int x, int y) {
     return kind >= 0 && !g.face_ok(x, y, kind);
 }
 
+// FLOW (the solver's own hierarchy): a coarse face takes 4 x the smallest penalty of its
+// children instead of the sum, so channels narrower than a coarse cell stay open on the
+// coarse levels (the 3D k_coarsen gives the reason).
+template <bool FLOW>
 __global__ void k2_coarsen(G2d gc, G2d gf, const uint8_t* __restrict__ ff, const double* __restrict__ fvol,
                            const double* __restrict__ fpen, uint8_t* __restrict__ cf, double* __restrict__ cvol,
                            double* __restrict__ cpen, float* __restrict__ cvol32, float* __restrict__ cpen32) {
@@ -253,7 +257,7 @@ __global__ void k2_coarsen(G2d gc, G2d gf, const uint8_t* __restrict__ ff, const
     int kind, X, Y;
     gc.decode(t, kind, X, Y);
     uint8_t fx = 0;
-    double v = 0, p = 0;
+    double v = 0, p = 0, lo = INFINITY;
     for (int q = 0; q < 4; q++) {
         int x = 2 * X + (q & 1), y = 2 * Y + (q >> 1);
         int i;
@@ -265,10 +269,12 @@ __global__ void k2_coarsen(G2d gc, G2d gf, const uint8_t* __restrict__ ff, const
             continue;
         fx |= ff[i];
         p += fpen[i];
+        lo = fmin(lo, fpen[i]);
         // cells: sum of 4; faces: the 2 coincident children (zero offset along the normal)
         bool coincident = kind < 0 || (kind == 0 ? (q & 1) == 0 : (q >> 1) == 0);
         if (coincident) v += fvol[i];
     }
+    if (FLOW && kind >= 0 && lo < INFINITY) p = 4.0 * lo;
     if (padded2(gc, kind, X, Y)) fx = 1;
     if (fx) v = p = 0;
     cf[t] = fx;
@@ -587,7 +593,12 @@ int setup2(stg_t* h) {
     auto body = [&]() -> int {
         for (int i = (int)lv.size() - 2; i >= 0; i--) {
             Level2 &c = lv[i], &f = lv[i + 1];
-            k2_coarsen<<<g1(c.g.size()), TPB, 0, h->st>>>(c.g, f.g, f.fixed, f.vol, f.pen, c.fixed, c.vol, c.pen, c.vol32, c.pen32);
+            if (h->hier_flow)
+                k2_coarsen<true><<<g1(c.g.size()), TPB, 0, h->st>>>(c.g, f.g, f.fixed, f.vol, f.pen, c.fixed, c.vol, c.pen, c.vol32,
+                                                                      c.pen32);
+            else
+                k2_coarsen<false><<<g1(c.g.size()), TPB, 0, h->st>>>(c.g, f.g, f.fixed, f.vol, f.pen, c.fixed, c.vol, c.pen, c.vol32,
+                                                                       c.pen32);
             STG_LAUNCH_CK();
         }
         Level2& C = lv[0];
@@ -597,7 +608,7 @@ int setup2(stg_t* h) {
         return gj_invert(h->st, nd, h->c2->aug0, h->c2->aug1, h->c2->info, &h->c2->inv);
     };
     GraphCache& G = h->sgraph;
-    STG_TRY(graphed(h, G, h->closed ? 2 : 1, body, [&](bool save) {
+    STG_TRY(graphed(h, G, (h->closed ? 2 : 1) | (h->hier_flow ? 4 : 0), body, [&](bool save) {
         if (save)
             G.saved = h->c2->inv;
         else

@@ -873,7 +873,7 @@ int stg_net_train(stg_t* h, int steps, double lr, uint64_t seed, float* losses) 
     if (!stg::net_grid_ok(h->n)) return stg::set_error("stg_net_train: grid %d (needs n >= 8, n %% 4 == 0)", h->n), STG_E_INVALID;
     if (steps < 0) return stg::set_error("stg_net_train: steps < 0"), STG_E_INVALID;
     NetState& N = *h->net;
-    if (!h->updated) STG_TRY(h->setup(h));
+    STG_TRY(stg::ensure_setup(h, false));
     STG_TRY(stg::net_buffers(N, h->n, true));
     std::vector<double> dl(steps > 0 ? steps : 1);
     double* d_losses = nullptr;

@@ -15,12 +15,15 @@ oracle_loop2d_n64.npz  the oracle's 20-iteration design loop of the 2D 64^2 benc
                        volume fraction 0.3, BP law, filter radius 1.5, OC with move limit 0.2,
                        every solve to FP64 relative residual 1e-11): objective per iteration
                        and the design of the last iteration (before its update).
+oracle_loop3d_n32.npz  the same for the 3D loop at 32^3 (parabolic inlet on a centred 8x8
+                       patch, uniform 0.15 start, volume fraction 0.15), 8 iterations; from
+                       iteration 5 the designs are high-contrast.
 ref_mma.npz            six updates of the reference's own MMA solver (oracle/_ref/libref_mma.so,
                        built from simplex/ext/mma by oracle/ref_build.sh) on a seeded problem
                        with the reference optimizer's settings (one volume constraint with
                        coefficient 1e4, move limit 0.2, bounds [0.01, 1]).
 
-usage: python tests/golden/make_golden.py [3d] [2d] [mma] [loop2d]
+usage: python tests/golden/make_golden.py [3d] [2d] [mma] [loop2d] [loop3d]
 """
 import ctypes
 import os
@@ -181,8 +184,41 @@ def oracle_loop2d(n=64, iters=20, frac=0.3, rmin=1.5):
     np.savez_compressed(os.path.join(HERE, "oracle_loop2d_n64.npz"), objective=np.array(Js), x_last=x_last)
 
 
+def oracle_loop3d(n=32, iters=8, frac=0.15, rmin=1.5):
+    """The 3D design loop (parabolic inlet on a centred n/4 square, OC, filter 1.5, BP alpha
+    1e4) for `iters` iterations; from iteration 5 the designs are high-contrast (density
+    down to 1e-6 .. 1e-8) and each solve takes over a hundred GMRES steps."""
+    from oracle import pyoracle as po
+
+    po.build()
+    b = po.bc_parabolic(n)
+    vw = po.filt(np.ones((n, n, n)), rmin, transpose=True)
+    x = np.full((n, n, n), frac)
+    Js = []
+    for it in range(iters):
+        x_last = x.copy()
+        phys = po.filt(x, rmin)
+        fp = po.face_penalty(phys, 1, [1e4])
+        o = po.Steady3D(n)
+        o.init_boundary(b)
+        o.update_penalty(np.zeros((n, n, n)), fp)
+        o.update_b(b.cell_b, b.face_b)
+        o.setup()
+        u, _ = o.solve(max_iter=60, abs_thr=0.0, rel_thr=1e-13, norm_thr=0.0, restarts=10, true_tol=1e-11)
+        Js.append(o.energy(u))
+        o.set_b_blocked(o.apply_E(u))
+        lam, _ = o.solve(max_iter=60, abs_thr=0.0, rel_thr=1e-13, norm_thr=0.0, restarts=10, true_tol=1e-11)
+        _, uf = po.blocked_to_field(n, u)
+        _, lf = po.blocked_to_field(n, lam)
+        sens = po.sensitivity(phys, 1, [1e4], uf, lf)
+        dc = po.filt(sens, rmin, transpose=True)
+        x = po.oc_update(x, dc, vw / n ** 3, vw, frac)[0].reshape(n, n, n)
+        print("loop3d", it, Js[-1], flush=True)
+    np.savez_compressed(os.path.join(HERE, "oracle_loop3d_n32.npz"), objective=np.array(Js), x_last=x_last)
+
+
 if __name__ == "__main__":
-    what = sys.argv[1:] or ["3d", "2d", "mma", "loop2d"]
+    what = sys.argv[1:] or ["3d", "2d", "mma", "loop2d", "loop3d"]
     if "3d" in what:
         ref_index_tables()
         oracle_regression()
@@ -193,4 +229,6 @@ if __name__ == "__main__":
         ref_mma()
     if "loop2d" in what:
         oracle_loop2d()
+    if "loop3d" in what:
+        oracle_loop3d()
     print("wrote", os.listdir(HERE))
