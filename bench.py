@@ -190,25 +190,29 @@ def ncu_traffic():
     return out
 
 
-def design_loop_2d(driver, iters=20):
-    """Runs the fluid_topo driver on the 2D 64^2 problem (no frames written) and returns
-    the median time per design iteration (two solves, sensitivity, filter, OC update) over
-    iterations 1..iters-1, from the driver's own log."""
+def design_loop(driver, dim, n, frac, iters):
+    """Runs the fluid_topo driver's design loop (test 1: parabolic inlet, uniform start at
+    the volume fraction, filter 1.5, OC with move 0.2, no frames written) and returns the
+    time per design iteration (two solves, sensitivity, filter, OC update) from the
+    driver's own log."""
     import tempfile
 
     with tempfile.TemporaryDirectory() as d:
-        cmd = [driver, "-driver", "0", "-test", "1", "-s", "64", "-frac", "0.3", "-lf", str(iters), "-frames", "0",
-               "-o", d]
+        cmd = [driver, "-driver", "0" if dim == 2 else "1", "-test", "1", "-s", str(n), "-frac", str(frac), "-lf", str(iters),
+               "-frames", "0", "-o", d]
         r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True)
         if r.returncode != 0:
             return {"error": r.stderr.strip()[-300:]}
         log = np.genfromtxt(os.path.join(d, "log.csv"), delimiter=",", names=True)
     it_ms = np.atleast_1d(log["iteration_ms"])
-    vc = np.atleast_1d(log["v_cycles_forward"]) + np.atleast_1d(log["v_cycles_adjoint"])
-    return {"workload": "2D 64^2 design loop (fluid_topo -driver 0 -test 1 -s 64 -frac 0.3), OC, filter 1.5, solves to 1e-10",
+    vf, va = np.atleast_1d(log["v_cycles_forward"]), np.atleast_1d(log["v_cycles_adjoint"])
+    tol = "1e-10" if dim == 2 else "1e-8"
+    return {"workload": f"{dim}D {n}^{dim} design loop (fluid_topo -driver {0 if dim == 2 else 1} -test 1 -s {n} -frac {frac}), "
+                        f"OC, filter 1.5, every solve to FP64 rel. residual {tol}",
             "iterations": int(iters), "total_s": round(float(np.sum(it_ms)) / 1e3, 3),
             "ms_per_iteration_median": round(float(np.median(it_ms[1:])), 3),
-            "v_cycles_per_iteration_median": float(np.median(vc[1:])),
+            "v_cycles_per_iteration_median": float(np.median((vf + va)[1:])),
+            "v_cycles_per_solve_max": int(max(vf.max(), va.max())),
             "final_objective": float(np.atleast_1d(log["objective"])[-1])}
 
 
@@ -415,11 +419,13 @@ def run_ours(args):
         methods["learned"] = r
         sv.close()
 
-    # ---- the 2D 64^2 design loop (fluid_topo -driver 0 -test 1: parabolic inlet, uniform 0.3
-    # start, filter 1.5, OC, solves to 1e-10), the latency-bound configuration
-    loop2d = None
+    # ---- design loops through the fluid_topo driver: the 2D 64^2 one (uniform 0.3 start, solves
+    # to 1e-10; latency-bound) and the 3D 128^3 one at fraction 0.15, 40 iterations (from
+    # iteration 5 on high-contrast designs)
+    loop2d = loop3d = None
     if rank == 0 and world == 1 and not args.no_methods:
-        loop2d = design_loop_2d(build.DRIVER)
+        loop2d = design_loop(build.DRIVER, 2, 64, 0.3, 20)
+        loop3d = design_loop(build.DRIVER, 3, 128, 0.15, 40)
 
     # ---- roofline of the dominant kernel class, measured over the timed region
     peak, peak_kind = measured_peak()
@@ -461,6 +467,7 @@ def run_ours(args):
                        "final_rel_residual_max": max(st["rel_residual"] for st in stats)},
             "methods": methods,
             "design_loop_2d": loop2d,
+            "design_loop_3d": loop3d,
             "kernels": kernel_table,
         }
         print(json.dumps(line), flush=True)

@@ -22,6 +22,8 @@
 //   -amax a     BP law maximum (1e4);  -move m  OC move limit (0.2)
 //   -tol t      FP64 relative residual of every solve (1e-8 in 3D, 1e-10 in 2D)
 //   -method plain|mixed   solver precision form (plain)
+//   -inner m    FGMRES basis size per refinement step (30); each step of the basis holds two
+//               FP32 vectors (V and Z), 32 bytes per cell in 3D: 4.4 GB at 512^3
 //   -warm 0|1   start each forward / adjoint solve from the previous one (default 1; the
 //               reference starts from zero, which -warm 0 reproduces)
 //   -init uniform|noise   initial design: frac everywhere, or seeded smoothed noise
@@ -66,7 +68,7 @@ struct Args {
 Args parse(int argc, char** argv) {
     static const char* known[] = {"-o",   "-s",    "-test", "-driver", "-lf",  "-frac",   "-rmin",  "-law",   "-amax",
                                   "-move", "-tol", "-method", "-init", "-seed", "-sigma", "-frames", "-verbose",
-                                  "-dump_boundary", "-opt", "-warm"};
+                                  "-dump_boundary", "-opt", "-warm", "-inner"};
     Args a;
     for (int i = 1; i < argc; i++) {
         std::string k = argv[i];
@@ -121,6 +123,7 @@ int run(const Args& a) {
     opts.method = a.get("-method", "plain") == "mixed" ? STG_METHOD_MIXED : STG_METHOD_PLAIN;
     opts.verbose = a.geti("-verbose", 0);
     opts.warm_start = a.geti("-warm", 1);
+    opts.inner_max = a.geti("-inner", opts.inner_max);
 
     stg_alpha law{};
     if (law_s == "ref") {
