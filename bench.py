@@ -213,6 +213,8 @@ def design_loop(driver, dim, n, frac, iters):
             "ms_per_iteration_median": round(float(np.median(it_ms[1:])), 3),
             "v_cycles_per_iteration_median": float(np.median((vf + va)[1:])),
             "v_cycles_per_solve_max": int(max(vf.max(), va.max())),
+            "rel_residual_max": float(max(np.max(np.atleast_1d(log["rel_residual_forward"])),
+                                          np.max(np.atleast_1d(log["rel_residual_adjoint"])))),
             "final_objective": float(np.atleast_1d(log["objective"])[-1])}
 
 

@@ -62,8 +62,8 @@ typedef struct stg_opts {
                             reference smoother. */
     int warm_start;      /* 1: start each solve from the previous solution of the same
                             equation (the forward one for stg_solve, the adjoint one for
-                            stg_adjoint_sensitivity) instead of zero; 0 (default): zero, as
-                            the reference */
+                            stg_adjoint_sensitivity) instead of zero, unless its residual
+                            exceeds ||b|| (then zero); 0 (default): zero, as the reference */
 } stg_opts;
 
 typedef struct stg_stats {

@@ -145,13 +145,25 @@ void orc_filter(int dim, int n, double rmin, const double* in, double* out, int 
 // ---------------------------------------------------------------- optimality criteria
 // x_new = clamp(x * sqrt(max(0,-dc) / (lambda dv)), max(lo, x - move), min(hi, x + move));
 // lambda by bisection so that sum_j vw_j x_new_j (the volume of the filtered design,
-// vw_j = sum_i w_ij / W_i) equals frac * ncell. Stops when (l2-l1) <= tol (l1+l2).
+// vw_j = sum_i w_ij / W_i) equals frac * ncell, on [0, 1e9] widened by decades while its
+// upper end still overshoots the volume. Stops when (l2-l1) <= tol (l1+l2).
 // Returns the number of bisection steps; lam_out receives the final lambda.
 int orc_oc_update(int ncell, const double* x, const double* dc, const double* dv, const double* vw, double frac, double move,
                   double lo, double hi, double tol, int max_steps, double* x_new, double* lam_out) {
     double l1 = 0.0, l2 = 1e9;
     int steps = 0;
     double target = frac * ncell, lmid = 0;
+    for (int k = 0; k < 60; k++) {
+        double vol = 0;
+        for (int i = 0; i < ncell; i++) {
+            double B = std::max(0.0, -dc[i]) / (dv[i] * l2);
+            double xn = x[i] * std::sqrt(B);
+            vol += vw[i] * std::min(std::min(hi, x[i] + move), std::max(std::max(lo, x[i] - move), xn));
+        }
+        if (vol <= target) break;
+        l1 = l2;
+        l2 *= 10.0;
+    }
     while ((l2 - l1) > tol * (l1 + l2) && steps < max_steps) {
         lmid = 0.5 * (l1 + l2);
         double vol = 0;

@@ -67,10 +67,13 @@ struct DF {
 // x64 += sum_q (alpha y_q) z_q. The sum runs in double-float arithmetic, not FP64: an FP32
 // sum of the basis loses the outer refinement step's accuracy to cancellation among the
 // terms, and GB300's FP64 pipe is far slower than HBM for this stream; only the final
-// addition to x is FP64.
+// addition to x is FP64. e (optional): the FP32 value of the sum over alpha is stored
+// (first = true) or added; e may be one of the z_q, since each element is read before it is
+// written.
 template <int NV>
 __global__ void __launch_bounds__(TPB) k_axpy_multi_32to64(long long n4, Tab z, const double* __restrict__ y, double alpha,
-                                                           d4* __restrict__ x, float4* __restrict__ xh, float4* __restrict__ xl) {
+                                                           d4* __restrict__ x, float4* __restrict__ xh, float4* __restrict__ xl,
+                                                           float4* e, bool first) {
     float ch[NV], cl[NV];
 #pragma unroll
     for (int q = 0; q < NV; q++) {
@@ -90,12 +93,25 @@ __global__ void __launch_bounds__(TPB) k_axpy_multi_32to64(long long n4, Tab z, 
         }
         double2* xp = reinterpret_cast<double2*>(x + t);
         double2 a = xp[0], b = xp[1];
-        a.x += s0.value();
-        a.y += s1.value();
-        b.x += s2.value();
-        b.y += s3.value();
+        const double d0 = s0.value(), d1 = s1.value(), d2 = s2.value(), d3 = s3.value();
+        a.x += d0;
+        a.y += d1;
+        b.x += d2;
+        b.y += d3;
         xp[0] = a;
         xp[1] = b;
+        if (e) {
+            const double ia = 1.0 / alpha;
+            float4 ev = make_float4((float)(d0 * ia), (float)(d1 * ia), (float)(d2 * ia), (float)(d3 * ia));
+            if (!first) {
+                const float4 o = e[t];
+                ev.x += o.x;
+                ev.y += o.y;
+                ev.z += o.z;
+                ev.w += o.w;
+            }
+            e[t] = ev;
+        }
         if (xh) {
             const float4 hv = make_float4((float)a.x, (float)a.y, (float)b.x, (float)b.y);
             xh[t] = hv;
@@ -322,8 +338,9 @@ static void dispatch_nv(int nb, A&&... args) {
 
 template <int NV>
 struct AxpyL {
-    static void run(cudaStream_t st, long long n4, const Tab& t, const double* y, double alpha, d4* x, float4* xh, float4* xl) {
-        k_axpy_multi_32to64<NV><<<rgrid(n4), TPB, 0, st>>>(n4, t, y, alpha, x, xh, xl);
+    static void run(cudaStream_t st, long long n4, const Tab& t, const double* y, double alpha, d4* x, float4* xh, float4* xl,
+                    float4* e, bool first) {
+        k_axpy_multi_32to64<NV><<<rgrid(n4), TPB, 0, st>>>(n4, t, y, alpha, x, xh, xl, e, first);
     }
 };
 template <int NV>
@@ -346,14 +363,21 @@ struct ProjL {
     }
 };
 
+int axpy_last_chunk(int nz) { return nz > 0 ? ((nz - 1) / MAXV) * MAXV : 0; }
+
+// Chunks of MAXV vectors from the last one down: e (when one of the z_q, a slot at the end
+// of the basis) is written by the first chunk, which holds it, and only added to by the
+// later ones; the double-float copy of x is written by the last chunk.
 int axpy_multi_32to64(cudaStream_t st, long long n4, const float4* const* z, const double* y, int nz, double alpha, d4* x,
-                      float4* xh, float4* xl) {
-    for (int j0 = 0; j0 < nz; j0 += MAXV) {
+                      float4* xh, float4* xl, float4* e) {
+    const int nchunk = (nz + MAXV - 1) / MAXV;
+    for (int c = nchunk - 1; c >= 0; c--) {
+        const int j0 = c * MAXV;
         int nb = nz - j0 < MAXV ? nz - j0 : MAXV;
         Tab t{};
         for (int q = 0; q < nb; q++) t.p[q] = z[j0 + q];
-        const bool last = j0 + MAXV >= nz;  // the copy is written by the last chunk
-        dispatch_nv<AxpyL>(nb, st, n4, t, y + j0, alpha, x, last ? xh : nullptr, last ? xl : nullptr);
+        const bool last = c == 0;
+        dispatch_nv<AxpyL>(nb, st, n4, t, y + j0, alpha, x, last ? xh : nullptr, last ? xl : nullptr, e, c == nchunk - 1);
         STG_LAUNCH_CK();
     }
     return STG_OK;

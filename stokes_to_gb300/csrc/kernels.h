@@ -80,9 +80,12 @@ int fill_bytes(cudaStream_t st, void* p, size_t bytes);
 int f64_to_f32(cudaStream_t st, long long n4, const d4* a, double scale, float4* out);
 int f32_to_f64(cudaStream_t st, long long n4, const float4* a, d4* out);
 // x64 += alpha * sum_j y[j] z[j]  (z FP32 vectors), y on device (nz entries); with xh / xl
-// non-null also writes the double-float copy of the new x there
+// non-null also writes the double-float copy of the new x there; with e non-null the FP32
+// value of sum_j y[j] z[j] goes to e, which may be one of z[j] for j >= axpy_last_chunk(nz)
 int axpy_multi_32to64(cudaStream_t st, long long n4, const float4* const* z, const double* y, int nz, double alpha, d4* x,
-                      float4* xh = nullptr, float4* xl = nullptr);
+                      float4* xh = nullptr, float4* xl = nullptr, float4* e = nullptr);
+// first index of the last group of vectors axpy_multi_32to64 sums in one pass
+int axpy_last_chunk(int nz);
 // h[j] = <v_j, w> for j < nv (FP32 per-thread partials, FP64 block and grid sums),
 // and <w, w> into *ww when ww != nullptr
 

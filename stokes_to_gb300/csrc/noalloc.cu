@@ -146,14 +146,26 @@ extern "C" int stg_oc_update_noalloc(int n, double rmin, const double* d_x, cons
     double l1 = 0.0, l2 = 1e9, lmid = 0.0, target = frac * (double)nc;
     int steps = 0;
     const double tol = 1e-9;
-    while ((l2 - l1) > tol * (l1 + l2) && steps < 200) {
-        lmid = 0.5 * (l1 + l2);
-        k_oc_noalloc<<<grid, TPB, 0, st>>>(n, rmin, R, d_x, d_dc, lmid, move, lo, hi, nullptr, part);
+    auto volume = [&](double lam, double* vol) -> int {
+        k_oc_noalloc<<<grid, TPB, 0, st>>>(n, rmin, R, d_x, d_dc, lam, move, lo, hi, nullptr, part);
         STG_LAUNCH_CK();
         STG_TRY(reduce_parts(st, part, grid, sum));
-        double vol = 0;
-        STG_CK(cudaMemcpyAsync(&vol, sum, sizeof(double), cudaMemcpyDeviceToHost, st));
+        STG_CK(cudaMemcpyAsync(vol, sum, sizeof(double), cudaMemcpyDeviceToHost, st));
         STG_CK(cudaStreamSynchronize(st));
+        return STG_OK;
+    };
+    // bracket widened by decades while its upper end overshoots the volume (stg_oc_update)
+    for (int k = 0; k < 60; k++) {
+        double vol = 0;
+        STG_TRY(volume(l2, &vol));
+        if (vol <= target) break;
+        l1 = l2;
+        l2 *= 10.0;
+    }
+    while ((l2 - l1) > tol * (l1 + l2) && steps < 200) {
+        lmid = 0.5 * (l1 + l2);
+        double vol = 0;
+        STG_TRY(volume(lmid, &vol));
         if (vol > target)
             l1 = lmid;
         else

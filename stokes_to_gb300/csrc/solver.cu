@@ -438,6 +438,14 @@ int solve_core(stg_t* h, const d4* b, d4* x, stg_stats* stats) {
     STG_CK(cudaStreamSynchronize(h->st));
     const double bn = std::sqrt(bn2);
     const int m = h->m;
+    // Augmented restarts (as LGMRES): the corrections of the last refinement steps that ran
+    // out of basis are kept in the last basis slots Z[m-1], Z[m-2], ... and take the place
+    // of the last Krylov steps of the following refinement steps. Restarted FGMRES discards
+    // the few slow directions it had found on every restart; the stored corrections carry
+    // them over (the iteration-5 design of the 256^3 loop at fraction 0.15: 600 V-cycles
+    // without, 270 with four). The slots must lie in the first group the update sums.
+    const int naug = std::max(0, std::min({4, m / 2, m - axpy_last_chunk(m)}));
+    int have_aug = 0, aug_next = 0;  // filled slots Z[m-have_aug .. m-1]; next to overwrite
     struct BoostGuard {
         stg_t* h;
         ~BoostGuard() { h->boost = false; }
@@ -447,7 +455,7 @@ int solve_core(stg_t* h, const d4* b, d4* x, stg_stats* stats) {
     double rel = 0, rn = 0;
     int status = STG_E_NOT_CONVERGED;
     // a zero start makes the first residual b itself (fixed rows cleared in the Laplacian form)
-    const bool x_zero = !(h->opts.warm_start && h->has_x0(x));
+    bool x_zero = !(h->opts.warm_start && h->has_x0(x));
     // double-float copies of x and b for the FP64 residual (3D Laplacian form)
     const bool df = h->dim == 3 && fast(h, fine(h));
     h->df_x = h->df_b = nullptr;
@@ -466,6 +474,19 @@ int solve_core(stg_t* h, const d4* b, d4* x, stg_stats* stats) {
         double rn2 = 0;
         STG_TRY(h->resid64(h, b, (outer == 0 && x_zero && h->dim == 3) ? nullptr : x, h->r64, &rn2));
         rn = std::sqrt(rn2);
+        if (outer == 0 && !x_zero && rn > bn) {
+            // the previous solution is further from this one than zero is (the design moved
+            // a lot, e.g. when it first turns into a channel): start from zero instead
+            if (h->opts.verbose) fprintf(stderr, "[stg] warm start rejected (||b-Ax0||/||b|| = %.3e)\n", bn > 0 ? rn / bn : 0.0);
+            x_zero = true;
+            STG_CK(cudaMemsetAsync(x, 0, sizeof(d4) * n4, h->st));
+            if (df) {
+                STG_CK(cudaMemsetAsync(h->xh, 0, sizeof(float4) * n4, h->st));
+                STG_CK(cudaMemsetAsync(h->xl, 0, sizeof(float4) * n4, h->st));
+            }
+            STG_TRY(h->resid64(h, b, h->dim == 3 ? nullptr : x, h->r64, &rn2));
+            rn = std::sqrt(rn2);
+        }
         rel = bn > 0 ? rn / bn : 0.0;
         if (!std::isfinite(rn)) {
             status = STG_E_NONFINITE;
@@ -499,8 +520,11 @@ int solve_core(stg_t* h, const d4* b, d4* x, stg_stats* stats) {
         STG_CK(cudaMemcpyAsync(h->dsig2, &one, sizeof(double), cudaMemcpyHostToDevice, h->st));
         double prev_est = beta;
         for (int j = 0; j < m; j++) {
-            if (h->net_on) S.learned_iters++;
-            STG_TRY(h->precond(h, h->V[j], h->Z[j]));
+            const bool aug_step = j >= m - have_aug;  // Z[j] holds a stored correction
+            if (!aug_step) {
+                if (h->net_on) S.learned_iters++;
+                STG_TRY(h->precond(h, h->V[j], h->Z[j]));
+            }
             // Arnoldi on the shifted operator A M - I, written as w = V_j - A Z_j: same Krylov
             // space, and a good preconditioner (A M near I) no longer leaves w dominated by
             // V_j, whose removal cancelled most of w and forced the second projection pass
@@ -578,7 +602,7 @@ int solve_core(stg_t* h, const d4* b, d4* x, stg_stats* stats) {
             // first step of a refinement step is not judged: its reduction depends on how
             // the right-hand side lies (a boundary-driven b gives about 2% with plain
             // multigrid too).
-            if (h->net_on && j > 0 && est > 0.8 * prev_est) {
+            if (h->net_on && j > 0 && !aug_step && est > 0.8 * prev_est) {
                 h->net_on = false;
                 S.fallbacks++;
             }
@@ -594,12 +618,22 @@ int solve_core(stg_t* h, const d4* b, d4* x, stg_stats* stats) {
         }
         for (int q = 0; q < k; q++) y[q] *= sig[q];  // z_q = sig_q Z_q
         STG_CK(cudaMemcpyAsync(h->dy, y.data(), sizeof(double) * k, cudaMemcpyHostToDevice, h->st));
-        PROF(h, 6, (16.0 * k + 64.0) * n4,
-             axpy_multi_32to64(h->st, n4, h->Z.data(), h->dy, k, rn, x, df ? h->xh : nullptr, df ? h->xl : nullptr));
-        // the step used the whole basis short of its target: the V-cycle is too weak for this
-        // design (high-contrast optimised densities), so the rest of the solve smooths twice
-        // per colour (about 1.5x the V-cycle's cost for 1.5-2x fewer V-cycles there)
-        if (h->dim == 3 && k == m && std::fabs(g[k]) > itol * beta) h->boost = true;
+        // the step used the whole basis short of its target
+        const bool stalled = k == m && std::fabs(g[k]) > itol * beta;
+        float4* keep = nullptr;
+        if (stalled && naug > 0) {
+            // the oldest stored correction (or a free slot) takes this step's correction for
+            // a unit residual, so that A Z_j is of the order of the basis vector it is taken from
+            keep = h->Z[m - 1 - aug_next];
+            aug_next = (aug_next + 1) % naug;
+            have_aug = std::min(naug, have_aug + 1);
+        }
+        PROF(h, 6, (16.0 * k + 64.0 + (keep ? 16.0 : 0.0)) * n4,
+             axpy_multi_32to64(h->st, n4, h->Z.data(), h->dy, k, rn, x, df ? h->xh : nullptr, df ? h->xl : nullptr, keep));
+        // a stalled step means the V-cycle is too weak for this design (high-contrast
+        // optimised densities): the rest of the solve smooths twice per colour (about 1.5x
+        // the V-cycle's cost for 1.5-2x fewer V-cycles there)
+        if (h->dim == 3 && stalled) h->boost = true;
     }
     h->df_x = h->df_b = nullptr;  // finish() changes x; adapters must not see the copies
     if (h->finish) STG_TRY(h->finish(h, b, x));
@@ -1168,13 +1202,26 @@ int stg_oc_update(stg_t* h, double rmin, const double* x, const double* dc, doub
     double l1 = 0.0, l2 = 1e9, lmid = 0.0, target = frac * nc;
     int steps = 0, np = 0;
     const double tol = 1e-9;
+    auto volume = [&](double lam, double* vol) -> int {
+        STG_TRY(oc_volume(h->st, nc, h->d_design, ddc, h->d_vw, lam, move, lo, hi, nullptr, h->d_parts, &np));
+        STG_TRY(reduce_parts(h->st, h->d_parts, np, h->dnrm));
+        STG_CK(cudaMemcpyAsync(vol, h->dnrm, sizeof(double), cudaMemcpyDeviceToHost, h->st));
+        STG_CK(cudaStreamSynchronize(h->st));
+        return STG_OK;
+    };
+    // the multiplier grows with the sensitivities (with the objective, i.e. with the grid:
+    // above 1e9 at 512^3): widen the bracket by decades until its upper end undershoots
+    for (int k = 0; k < 60; k++) {
+        double vol = 0;
+        STG_TRY(volume(l2, &vol));
+        if (vol <= target) break;
+        l1 = l2;
+        l2 *= 10.0;
+    }
     while ((l2 - l1) > tol * (l1 + l2) && steps < 200) {
         lmid = 0.5 * (l1 + l2);
-        STG_TRY(oc_volume(h->st, nc, h->d_design, ddc, h->d_vw, lmid, move, lo, hi, nullptr, h->d_parts, &np));
-        STG_TRY(reduce_parts(h->st, h->d_parts, np, h->dnrm));
         double vol = 0;
-        STG_CK(cudaMemcpyAsync(&vol, h->dnrm, sizeof(double), cudaMemcpyDeviceToHost, h->st));
-        STG_CK(cudaStreamSynchronize(h->st));
+        STG_TRY(volume(lmid, &vol));
         if (vol > target)
             l1 = lmid;
         else

@@ -24,13 +24,16 @@
 //   -method plain|mixed   solver precision form (plain)
 //   -inner m    FGMRES basis size per refinement step (30); each step of the basis holds two
 //               FP32 vectors (V and Z), 32 bytes per cell in 3D: 4.4 GB at 512^3
+//   -maxouter k FP64 refinement steps per solve (20); a solve that ends without reaching
+//               -tol is logged with its residual and the loop goes on
 //   -warm 0|1   start each forward / adjoint solve from the previous one (default 1; the
 //               reference starts from zero, which -warm 0 reproduces)
 //   -init uniform|noise   initial design: frac everywhere, or seeded smoothed noise
 //   -seed s -sigma g      noise seed and Gaussian width in cells (1, 4)
 //   -frames k   write a frame every k iterations (default 1, as the reference; 0: none)
 //   -dump_boundary dir   write the boundary arrays of the test to dir and exit (no GPU)
-// Output in -o: log.csv (iteration, objective, volume, change, V-cycles, solve times)
+// Output in -o: log.csv (iteration, objective, volume, change, V-cycles, solve times, the
+// final FP64 relative residuals of both solves)
 // and frames in the reference drivers' layout and binary format (frame k = design k
 // with the velocity of its forward solve): k/x, k/velocity, k/psi_D, k/psi_N, 0/grid,
 // 0/last_frame.txt.
@@ -68,7 +71,7 @@ struct Args {
 Args parse(int argc, char** argv) {
     static const char* known[] = {"-o",   "-s",    "-test", "-driver", "-lf",  "-frac",   "-rmin",  "-law",   "-amax",
                                   "-move", "-tol", "-method", "-init", "-seed", "-sigma", "-frames", "-verbose",
-                                  "-dump_boundary", "-opt", "-warm", "-inner"};
+                                  "-dump_boundary", "-opt", "-warm", "-inner", "-maxouter"};
     Args a;
     for (int i = 1; i < argc; i++) {
         std::string k = argv[i];
@@ -124,6 +127,7 @@ int run(const Args& a) {
     opts.verbose = a.geti("-verbose", 0);
     opts.warm_start = a.geti("-warm", 1);
     opts.inner_max = a.geti("-inner", opts.inner_max);
+    opts.max_outer = a.geti("-maxouter", opts.max_outer);
 
     stg_alpha law{};
     if (law_s == "ref") {
@@ -176,7 +180,8 @@ int run(const Args& a) {
     make_dir(out);
     std::ofstream log(out + "/log.csv");
     log.precision(17);
-    log << "iteration,objective,volume,change,v_cycles_forward,v_cycles_adjoint,solve_ms,iteration_ms\n";
+    log << "iteration,objective,volume,change,v_cycles_forward,v_cycles_adjoint,solve_ms,iteration_ms,rel_residual_forward,"
+           "rel_residual_adjoint\n";
     std::printf("fluid_topo %dD N=%d test %d: %s, %s law, rmin %.2f, frac %.3f, %d iterations, tol %.1e, %s\n", d, n, test,
                 opt.c_str(), law_s.c_str(), rmin, frac, iters, opts.tol, stg_version());
 
@@ -189,7 +194,7 @@ int run(const Args& a) {
         stg::check(stg_set_density(h, nullptr, &law));
         const stg_stats& fs = fluid.solve(true);
         const int vf = fs.inner_iters;
-        const double sms = fs.solve_ms;
+        const double sms = fs.solve_ms, rf = fs.rel_residual;
         J = energy.compute_energy();
         // adjoint solve and chain rule (Update_Grad), then H^T for the filter
         stg_stats as{};
@@ -212,7 +217,7 @@ int run(const Args& a) {
         vol /= (double)nc;
         const double tms = now_ms() - t0;
         log << it << "," << J << "," << vol << "," << change << "," << vf << "," << as.inner_iters << "," << sms + as.solve_ms
-            << "," << tms << "\n";
+            << "," << tms << "," << rf << "," << as.rel_residual << "\n";
         std::printf("iter %4d  J %.6e  vol %.4f  change %.3e  V-cycles %d+%d  %.1f ms\n", it, J, vol, change, vf,
                     as.inner_iters, tms);
         if (opt == "mma" && change <= 1e-3) break;  // Optimize_MMA's stopping test (tol 1e-3)

@@ -218,12 +218,15 @@ def test_filter_oc_and_noise(oracle, stg):
     g = np.random.default_rng(9).standard_normal((n, n, n))
     gt = s.filter(1.5, g, transpose=True)
     assert relerr(gt, oracle.filt(g, 1.5, transpose=True)) < 1e-14
-    dc = -np.abs(np.random.default_rng(10).standard_normal((n, n, n)))
-    xn, lam = s.oc_update(1.5, rho, dc, 0.3)
     vw = oracle.filt(np.ones((n, n, n)), 1.5, transpose=True)
-    xn_ref, lam_ref, _ = oracle.oc_update(rho, dc, vw / n ** 3, vw, 0.3)
-    assert relerr(xn, xn_ref.reshape(n, n, n)) < 1e-9
-    assert abs(np.sum(vw * xn) / n ** 3 - 0.3) < 1e-6
+    # scale 1e8: the multiplier lies above the initial bracket [0, 1e9] (as at 512^3)
+    for scale in (1.0, 1e8):
+        dc = -np.abs(np.random.default_rng(10).standard_normal((n, n, n))) * scale
+        xn, lam = s.oc_update(1.5, rho, dc, 0.3)
+        xn_ref, lam_ref, _ = oracle.oc_update(rho, dc, vw / n ** 3, vw, 0.3)
+        assert relerr(xn, xn_ref.reshape(n, n, n)) < 1e-9
+        assert abs(lam - lam_ref) <= 1e-9 * lam_ref
+        assert abs(np.sum(vw * xn) / n ** 3 - 0.3) < 1e-6
 
 
 def test_errors_are_reported(stg):
@@ -248,7 +251,7 @@ def test_warm_start_reaches_the_same_solution(oracle, stg):
     n = 32
     b, rho, phys, fp, o, s = build_pair(oracle, stg, n, tol=1e-10, warm_start=1)
     s.solve()
-    fp2 = [f * 1.01 for f in fp]
+    fp2 = [f * 1.001 for f in fp]
     s.set_penalty(np.zeros((n, n, n)), fp2)
     p_w, vel_w, st_w = s.solve()
     cold = stg.Solver(n, tol=1e-10)

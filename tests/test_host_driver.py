@@ -185,6 +185,7 @@ def test_driver_3d_loop_matches_oracle_fixture(driver, tmp_path):
     subprocess.run([driver, "-driver", "1", "-test", "1", "-s", str(n), "-frac", "0.15", "-lf", str(iters), "-tol", "1e-10",
                     "-frames", str(iters - 1), "-o", str(out)], check=True)
     log = np.genfromtxt(out / "log.csv", delimiter=",", names=True)
+    assert np.all(log["rel_residual_forward"] <= 1e-10) and np.all(log["rel_residual_adjoint"] <= 1e-10)
     assert np.allclose(log["objective"], g["objective"], rtol=1e-6, atol=0)
     assert relerr(read_field(out / str(iters - 1) / "x", n, 3), g["x_last"]) < 1e-4
 
@@ -195,7 +196,7 @@ def test_driver_3d_high_contrast_solves_converge(driver, tmp_path):
     channels with density 1 in solid 1e-8 .. 1e-30 (penalty contrast 1e4). With the
     reference's coarse penalties (sums over the children) the restarted solve stagnated
     there (relative residual 0.21 after 20 x 30 V-cycles at iteration 5); the solver's flow
-    rule keeps every solve converged in well under a hundred V-cycles."""
+    rule keeps every solve converged to 1e-8 in well under the cap."""
     n, iters = 64, 12
     out = tmp_path / "run"
     subprocess.run([driver, "-driver", "1", "-test", "1", "-s", str(n), "-frac", "0.15", "-lf", str(iters), "-frames", "0",
@@ -203,6 +204,7 @@ def test_driver_3d_high_contrast_solves_converge(driver, tmp_path):
     log = np.genfromtxt(out / "log.csv", delimiter=",", names=True)
     assert len(log) == iters
     assert np.all(np.diff(log["objective"]) < 0), log["objective"]
-    # the refinement cap is 20 x 30 = 600 V-cycles: a solve that stopped far below it converged
+    assert np.all(log["rel_residual_forward"] <= 1e-8) and np.all(log["rel_residual_adjoint"] <= 1e-8)
+    # the refinement cap is 20 x 30 = 600 V-cycles
     assert np.max(log["v_cycles_forward"]) <= 150, log["v_cycles_forward"]
     assert np.max(log["v_cycles_adjoint"]) <= 150, log["v_cycles_adjoint"]

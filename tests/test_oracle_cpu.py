@@ -190,6 +190,12 @@ def test_filter_and_oc(oracle):
     xn, lam, steps = oracle.oc_update(x, dc, vw / n ** 3, vw, 0.3)
     assert abs((vw.ravel() * xn).sum() / n ** 3 - 0.3) < 1e-8
     assert np.all(np.abs(xn - x.ravel()) <= 0.2 + 1e-15)
+    # sensitivities of a large grid's objective put the multiplier above the initial
+    # bracket [0, 1e9]: the widened bracket still meets the volume
+    xb, lamb, _ = oracle.oc_update(x, dc * 1e8, vw / n ** 3, vw, 0.3)
+    assert lamb > 1e9
+    assert abs((vw.ravel() * xb).sum() / n ** 3 - 0.3) < 1e-8
+    assert np.allclose(xb, xn, rtol=1e-7, atol=1e-9)
 
 
 def test_density_noise_statistics(oracle):
