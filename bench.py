@@ -435,6 +435,14 @@ def run_ours(args):
     d = prof[dom]
     achieved = d["bytes"] / (d["ms"] * 1e-3) / 1e9
     traffic = ncu_traffic().get(dom)
+    # the V-cycle as a whole (every level's sweeps, the transfers and the coarsest GEMV):
+    # algorithmic bytes over CUDA-event time, against the same measured peak
+    vc_cls = [k for k in ("sweep32", "sweep32_coarse", "restrict32", "prolong32", "coarse") if k in prof]
+    vc_ms = sum(prof[k]["ms"] for k in vc_cls)
+    vc_bytes = sum(prof[k]["bytes"] for k in vc_cls)
+    vcycle = {"classes": vc_cls, "ms_per_solve": round(vc_ms / PROFILED_SOLVES, 3),
+              "achieved_GBps": round(vc_bytes / (vc_ms * 1e-3) / 1e9, 1) if vc_ms > 0 else None,
+              "frac": round(vc_bytes / (vc_ms * 1e-3) / 1e9 / peak, 4) if vc_ms > 0 else None}
     kernel_table = {k: {"launches": v["launches"], "ms": round(v["ms"], 3),
                         "GBps": round(v["bytes"] / (v["ms"] * 1e-3) / 1e9, 1) if v["ms"] > 0 and v["bytes"] > 0 else None}
                     for k, v in prof.items() if v["launches"]}
@@ -463,6 +471,7 @@ def run_ours(args):
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                          "frac": round(achieved / peak, 4), "peak_source": peak_kind,
                          "traffic": traffic, "algorithmic_bytes_per_launch": d["bytes"] / d["launches"]},
+            "vcycle_hbm": vcycle,
             "cpu_baseline": cpu,
             "clocks": clocks,
             "solver": {"v_cycles_per_solve": vc, "outer_per_solve": statistics.mean(st["outer_iters"] for st in stats),
