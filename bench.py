@@ -335,7 +335,10 @@ def run_ours(args):
             barrier()
         ms = e0.elapsed_time(e1)
         launches = capi.kernel_launches() - l0
-        prof = s.profile_read() if profile else None
+        prof = None
+        if profile:
+            prof = s.profile_read()
+            s.profile(False)  # the later measurements run with the CUDA graphs, unprofiled
         return ms, stats, launches, clk.summary(), prof
 
     # ---- headline: plain method, inputs resident (no per-kernel events in this region)
