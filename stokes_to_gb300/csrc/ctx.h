@@ -20,6 +20,7 @@ struct Level {
     int cur = 0;  // which of xa/xb holds the current correction
     bool lap = false;  // Laplacian-form operator valid on this level (stencil.cuh)
     __nv_bfloat16* xbf = nullptr;
+    __half* P16 = nullptr;    // FP16 copy of P32 / its scale for the solver's own sweeps (set-up)
     d4 *t0 = nullptr, *t1 = nullptr;  // FP64 adapter buffers (allocated on first use)
     float4* x() { return cur ? xb : xa; }
     float4* other() { return cur ? xa : xb; }
@@ -87,6 +88,9 @@ struct stg_ctx {
     // solve in progress (valid while df_x / df_b name them), the low words of the finest
     // penalty (its high words are the level's P32)
     float4 *xh = nullptr, *xl = nullptr, *bh = nullptr, *bl = nullptr, *Plo = nullptr;
+    // per-level scales of the FP16 penalty copies (device, level 0 coarsest) and scratch
+    float* d_pscale = nullptr;
+    unsigned* d_pmax = nullptr;
     const stg::d4 *df_x = nullptr, *df_b = nullptr;
     // fine-level FP64
     stg::d4 *b64 = nullptr, *x64 = nullptr, *r64 = nullptr, *t64 = nullptr, *lam64 = nullptr;

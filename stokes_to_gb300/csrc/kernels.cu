@@ -2,6 +2,7 @@
 // residual + restriction, prolongation, coarse re-discretisation and layout conversions.
 // (The smoothing sweep lives in sweep.cu.)
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 
 #include "kernels.h"
 #include "stencil.cuh"
@@ -208,6 +209,45 @@ __global__ void k_to_bf16(Geom g, const float4* __restrict__ x, __nv_bfloat16* _
     __nv_bfloat162* h = reinterpret_cast<__nv_bfloat162*>(y + 4ll * s);
     h[0] = __floats2bfloat162_rn(v.x, v.y);
     h[1] = __floats2bfloat162_rn(v.z, v.w);
+}
+
+// y = FP16(x / *scale) on the box slots (the sweeps' staged penalty copy)
+__global__ void k_to_f16(Geom g, const float4* __restrict__ x, const float* __restrict__ scale, __half* __restrict__ y) {
+    long long t = (long long)blockIdx.x * TPB + threadIdx.x;
+    if (t >= g.box()) return;
+    int i, j, k;
+    g.box_ijk(t, i, j, k);
+    int s = g.slot(i, j, k);
+    const float4 v = __ldg(x + s);
+    const float inv = 1.f / __ldg(scale);
+    __half2* h = reinterpret_cast<__half2*>(y + 4ll * s);
+    h[0] = __floats2half2_rn(v.x * inv, v.y * inv);
+    h[1] = __floats2half2_rn(v.z * inv, v.w * inv);
+}
+
+// largest |x| over the box slots, as the bits of a non-negative float (atomicMax on them
+// orders as the values do)
+__global__ void k_absmax(Geom g, const float4* __restrict__ x, unsigned* __restrict__ out) {
+    long long t = (long long)blockIdx.x * TPB + threadIdx.x;
+    float a = 0.f;
+    if (t < g.box()) {
+        int i, j, k;
+        g.box_ijk(t, i, j, k);
+        const float4 v = __ldg(x + g.slot(i, j, k));
+        a = fmaxf(fmaxf(fabsf(v.x), fabsf(v.y)), fmaxf(fabsf(v.z), fabsf(v.w)));
+    }
+    for (int o = 16; o > 0; o >>= 1) a = fmaxf(a, __shfl_xor_sync(0xffffffffu, a, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(out, __float_as_uint(a));
+}
+
+// per-level FP16 scales: a power of two that brings the finest level's largest penalty to at
+// most 2^15 (FP16 holds up to 65504), times 8 per level down (a coarse penalty is at most 8 x
+// the largest of the finer level's)
+__global__ void k_pscale(int nlev, const unsigned* __restrict__ maxbits, float* __restrict__ scale) {
+    const float mx = __uint_as_float(*maxbits);
+    float s = 1.f;
+    while (s < 1e30f && mx > 32768.f * s) s *= 2.f;
+    for (int l = nlev - 1; l >= 0; l--, s *= 8.f) scale[l] = s;
 }
 
 __global__ void k_restrict64(Geom gc, Geom gf, const d4* __restrict__ rf, const uint8_t* __restrict__ mc, d4* __restrict__ rc) {
@@ -687,6 +727,21 @@ int prolong_add32(cudaStream_t st, const Geom& gf, const Geom& gc, const float4*
 
 int prolong_add_bf16(cudaStream_t st, const Geom& gf, const Geom& gc, const __nv_bfloat16* xc, const uint8_t* mf, float4* xf) {
     k_prolong_add32<__nv_bfloat16><<<grid_for(gf.box(), TPB), TPB, 0, st>>>(gf, gc, xc, mf, xf);
+    STG_LAUNCH_CK();
+    return STG_OK;
+}
+
+int to_f16(cudaStream_t st, const Geom& g, const float4* x, const float* scale, __half* y) {
+    k_to_f16<<<grid_for(g.box(), TPB), TPB, 0, st>>>(g, x, scale, y);
+    STG_LAUNCH_CK();
+    return STG_OK;
+}
+
+int penalty_scales(cudaStream_t st, const Geom& fine, const float4* P, int nlev, unsigned* scratch, float* scale) {
+    STG_CK(cudaMemsetAsync(scratch, 0, sizeof(unsigned), st));
+    k_absmax<<<grid_for(fine.box(), TPB), TPB, 0, st>>>(fine, P, scratch);
+    STG_LAUNCH_CK();
+    k_pscale<<<1, 1, 0, st>>>(nlev, scratch, scale);
     STG_LAUNCH_CK();
     return STG_OK;
 }

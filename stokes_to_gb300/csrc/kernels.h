@@ -1,6 +1,7 @@
 // Host-side launchers of the grid kernels (kernels.cu, dense.cu, blas.cu, topo.cu).
 #pragma once
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include "internal.cuh"
@@ -25,7 +26,7 @@ int apply32(cudaStream_t st, const Geom& g, float vol, const float4* x, const ui
 // One colour of the box-Vanka block-Jacobi step on the residual equation, fused with the
 // residual: xout = xin + SHATTER(B^-1 GATHER(r - A xin)) (sweep.cu). xin == nullptr: xin = 0.
 int sweep32(cudaStream_t st, const Geom& g, float vol, const float4* r, const float4* xin, float4* xout, const uint8_t* m,
-            const float4* P, int flag, bool lap = false);
+            const float4* P, int flag, bool lap = false, const __half* P16 = nullptr, const float* p16_scale = nullptr);
 // 1 in *timed_out when a sweep with TMA staging gave up waiting for its loads (sticky)
 int sweep_status(cudaStream_t st, int* timed_out);
 // rc = R (rf - A xf) with R the 8-child sum masked by the coarse mask (xf == nullptr: rc = R rf).
@@ -48,6 +49,10 @@ int prolong_add32(cudaStream_t st, const Geom& gf, const Geom& gc, const float4*
 // same with BF16-stored coarse correction
 int prolong_add_bf16(cudaStream_t st, const Geom& gf, const Geom& gc, const __nv_bfloat16* xc, const uint8_t* mf, float4* xf);
 int to_bf16(cudaStream_t st, const Geom& g, const float4* x, __nv_bfloat16* y);
+// y = FP16(x / *scale) on the box slots; the per-level scales (level 0 coarsest) from the
+// finest level's penalties: scale[l] = 8^(nlev-1-l) x the power of two that keeps them below 2^15
+int to_f16(cudaStream_t st, const Geom& g, const float4* x, const float* scale, __half* y);
+int penalty_scales(cudaStream_t st, const Geom& fine, const float4* P, int nlev, unsigned* scratch, float* scale);
 // coarse descriptor from the fine one (updateSubSystem + finish); flow: velocity penalties
 // by 8 x the smallest free child instead of the sum (the solver's own hierarchy)
 int coarsen(cudaStream_t st, const Geom& gc, const Geom& gf, const uint8_t* mf, const d4* Pf, uint8_t* mc, d4* Pc64,

@@ -158,6 +158,10 @@ int update(stg_t* h) {
     }
     // coarse boundary faces have fixed children, so the Laplacian form carries down
     for (auto& L : h->lv) L.lap = h->lap_ok;
+    // FP16 copies of the penalties for the solver's own sweeps, each level divided by a scale
+    // that keeps it in FP16's range (11 significant bits: the V-cycle count is the FP32 one)
+    PROF(h, 8, 0.0, penalty_scales(h->st, fine(h).g, fine(h).P32, h->L, h->d_pmax, h->d_pscale));
+    for (int i = 0; i < h->L; i++) PROF(h, 8, 0.0, to_f16(h->st, h->lv[i].g, h->lv[i].P32, h->d_pscale + i, h->lv[i].P16));
     // low words of the finest penalty for the double-float residual (P32 holds the high)
     PROF(h, 8, 0.0, split64(h->st, fine(h).g.nslot, fine(h).P64, nullptr, h->Plo));
     // the coarsest set-up (one launch per Gauss-Jordan pivot) reads and writes fixed buffers:
@@ -194,12 +198,16 @@ int sweep(stg_t* h, Level& L, const float4* r, int flag, bool first) {
     float vol = (float)L.vol;
     // profile class 1: sweeps of the finest level; 10: of the coarser levels
     const int cls = &L == &fine(h) ? 1 : 10;
+    // the adapters keep the FP32 penalty and residual (the reference smoother to FP32
+    // rounding); the solver's sweeps stage both in BF16 (sweep.cu SmemT)
+    const __half* P16 = h->reference_cycle ? nullptr : L.P16;
+    const float* psc = h->d_pscale + (&L - h->lv.data());
     if (first) {
         // x = 0: the residual is r itself
-        PROF(h, cls, 49.0 * L.g.box(), sweep32(h->st, L.g, vol, r, nullptr, L.x(), L.m, L.P32, flag, fast(h, L)));
+        PROF(h, cls, 41.0 * L.g.box(), sweep32(h->st, L.g, vol, r, nullptr, L.x(), L.m, L.P32, flag, fast(h, L), P16, psc));
         return STG_OK;
     }
-    PROF(h, cls, 65.0 * L.g.box(), sweep32(h->st, L.g, vol, r, L.x(), L.other(), L.m, L.P32, flag, fast(h, L)));
+    PROF(h, cls, 57.0 * L.g.box(), sweep32(h->st, L.g, vol, r, L.x(), L.other(), L.m, L.P32, flag, fast(h, L), P16, psc));
     L.cur ^= 1;
     return STG_OK;
 }
@@ -304,7 +312,7 @@ int coarse_cycle(stg_t* h) {
     // the coarsest inverse lives in one of two buffers (fixed per handle): part of the key
     const long long key = (long long)per | ((long long)(h->opts.method == STG_METHOD_MIXED) << 3) |
                           ((long long)fast(h, h->lv[top]) << 4) | ((long long)(h->dense.inv == h->dense.Ainv) << 5) |
-                          ((long long)h->L << 6);
+                          ((long long)h->L << 6) | ((long long)h->reference_cycle << 12);  // adapters: FP32 sweeps
     GraphCache& G = h->boost && !h->reference_cycle ? h->vgraph_boost : h->vgraph;
     return graphed(h, G, key, [&] { return vcycle_levels(h, top, nullptr); },
                    [&](bool save) {
@@ -815,7 +823,7 @@ int stg_create(int dim, int n, const stg_opts* opts, stg_t** out) {
         size_t ns = L.g.nslot;
         if ((rc = dalloc(&L.m, ns)) || (rc = dalloc(&L.P64, ns)) || (rc = dalloc(&L.P32, ns)) || (rc = dalloc(&L.r, ns)) ||
             (rc = dalloc(&L.xa, ns)) || (rc = dalloc(&L.xb, ns)) || (rc = dalloc(&L.rr, ns)) ||
-            (rc = dalloc(&L.xbf, 4 * ns)))
+            (rc = dalloc(&L.xbf, 4 * ns)) || (rc = dalloc(&L.P16, 4 * ns)))
             return fail(rc);
         // halo and absent unknowns fixed; the box is rewritten by set_boundary / coarsen
         if ((rc = mask_from_field(h->st, L.g, nullptr, nullptr, nullptr, nullptr, L.m))) return fail(rc);
@@ -845,7 +853,7 @@ int stg_create(int dim, int n, const stg_opts* opts, stg_t** out) {
     if ((rc = dalloc(&h->b64, ns)) || (rc = dalloc(&h->x64, ns)) || (rc = dalloc(&h->r64, ns)) || (rc = dalloc(&h->t64, ns)) ||
         (rc = dalloc(&h->lam64, ns)) || (rc = dalloc(&h->w, ns)) ||
         (dim == 3 && ((rc = dalloc(&h->xh, ns)) || (rc = dalloc(&h->xl, ns)) || (rc = dalloc(&h->bh, ns)) || (rc = dalloc(&h->bl, ns)) ||
-                      (rc = dalloc(&h->Plo, ns)))))
+                      (rc = dalloc(&h->Plo, ns)) || (rc = dalloc(&h->d_pscale, (size_t)h->L)) || (rc = dalloc(&h->d_pmax, 1)))))
         return fail(rc);
     h->V.assign(h->m + 1, nullptr);
     h->Z.assign(h->m, nullptr);
@@ -883,6 +891,7 @@ int stg_destroy(stg_t* h) {
         cudaFree(L.xb);
         cudaFree(L.rr);
         cudaFree(L.xbf);
+        cudaFree(L.P16);
         cudaFree(L.t0);
         cudaFree(L.t1);
     }
@@ -890,6 +899,8 @@ int stg_destroy(stg_t* h) {
     for (d4* p : {h->b64, h->x64, h->r64, h->t64, h->lam64}) cudaFree(p);
     cudaFree(h->w);
     for (float4* p : {h->xh, h->xl, h->bh, h->bl, h->Plo}) cudaFree(p);
+    cudaFree(h->d_pscale);
+    cudaFree(h->d_pmax);
     for (auto p : h->V) cudaFree(p);
     for (auto p : h->Z) cudaFree(p);
     for (double* p : {h->dscr, h->dh, h->dnrm, h->dy, h->dsig2, h->stage, h->d_design, h->d_phys, h->d_sens, h->d_sens_design, h->d_vw,

@@ -24,6 +24,9 @@
 // leaves them. If the Schur complement is 0 (the reference's LU meets a zero pivot) the
 // pressure is left unchanged.
 #include <cuda.h>
+#include <cuda_fp16.h>
+
+#include <type_traits>
 
 #include "kernels.h"
 #include "stencil.cuh"
@@ -647,10 +650,22 @@ __global__ void __launch_bounds__(NT, 3) k_sweep_lap(Geom g, float vol, const fl
 // mbarrier counting the bytes, instead of every thread issuing 16-byte copies. The boxes
 // read zero outside the allocation, as the copies did. Everything else is k_sweep_lap.
 constexpr int RNP = 344;  // r / P ring slot in float4s: RN padded to 128 bytes (TMA destinations)
-constexpr unsigned XBYTES = XN * 16, RBYTES = RN * 16;
+constexpr int RNP16 = 352;  // P ring slot in BF16 quadruples (8 bytes): RN padded to 128 bytes
+constexpr unsigned XBYTES = XN * 16, RBYTES = RN * 16, RBYTES16 = RN * 8;
 static_assert(RNP >= RN && (RNP * 16) % 128 == 0 && (XN * 16) % 128 == 0, "TMA ring slots must be 128-byte aligned");
+static_assert(RNP16 >= RN && (RNP16 * 8) % 128 == 0, "TMA ring slots must be 128-byte aligned");
 
-struct SmemT {
+// PB = false: P in FP32, separate rings for r and the computed residual rr (the adapters,
+// which reproduce the reference smoother to FP32 rounding). PB = true (the solver's own
+// sweeps): P staged from its BF16 copy, and rr written over r in place in a three-slot ring
+// (rr(i), r(i+1) turning into rr(i+1), r(i+2) in flight): 68.4 -> 55.2 KB of shared memory,
+// so four blocks (32 warps) share an SM instead of three. The kernel is latency- and
+// issue-bound, and the extra warps hide the per-plane barriers. The smoother works with P
+// to 2^-9 relative; the V-cycle is a preconditioner inside FP64 refinement.
+template <bool PB>
+struct SmemT;
+template <>
+struct SmemT<false> {
     float4 x[4 * XN];
     float4 P[3 * RNP];
     float4 r[2 * RNP];
@@ -660,6 +675,25 @@ struct SmemT {
     uint8_t m[4 * XN];
     unsigned long long bar;
 };
+template <>
+struct SmemT<true> {
+    float4 x[4 * XN];
+    uint2 P[3 * RNP16];
+    float4 r[3 * RNP];  // r and rr in one ring
+    float dp[DJ * DK];
+    float dpp[SJ * SK];
+    uint8_t m[4 * XN];
+    unsigned long long bar;
+};
+
+// a staged penalty quadruple as float4: FP32 as it is, or four FP16 values (x, y in the
+// first word, z, w in the second, low half first) times the level's scale
+__device__ __forceinline__ float4 ldv(const float4& v, float) { return v; }
+__device__ __forceinline__ float4 ldv(const uint2& v, float sc) {
+    const float2 a = __half22float2(*reinterpret_cast<const __half2*>(&v.x)), b = __half22float2(*reinterpret_cast<const __half2*>(&v.y));
+    return make_float4(a.x * sc, a.y * sc, b.x * sc, b.y * sc);
+}
+
 
 // 3D box load of the tensor map at coordinates (c0, c1, c2) into shared memory, counted on bar
 __device__ __forceinline__ void tma3(unsigned dst, const CUtensorMap* map, int c0, int c1, int c2, unsigned bar) {
@@ -696,13 +730,23 @@ __device__ __forceinline__ void fail(int* err) {
     if (threadIdx.x == 0 && threadIdx.y == 0) atomicExch(err, 1);
 }
 
-template <bool HAS_X>
-__global__ void __launch_bounds__(NT, 3) k_sweep_tma(const __grid_constant__ CUtensorMap tmx, const __grid_constant__ CUtensorMap tmr,
-                                                    const __grid_constant__ CUtensorMap tmp, Geom g, float vol,
-                                                    float4* __restrict__ xout, const uint8_t* __restrict__ m, int flag, int chunk,
-                                                    int* __restrict__ err) {
+template <bool HAS_X, bool PB>
+__global__ void __launch_bounds__(NT, PB ? 4 : 3) k_sweep_tma(const __grid_constant__ CUtensorMap tmx,
+                                                             const __grid_constant__ CUtensorMap tmr,
+                                                             const __grid_constant__ CUtensorMap tmp, Geom g, float vol,
+                                                             float4* __restrict__ xout, const uint8_t* __restrict__ m, int flag,
+                                                             int chunk, int* __restrict__ err, const float* __restrict__ pscale) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    SmemT& S = *reinterpret_cast<SmemT*>(smem_raw);
+    SmemT<PB>& S = *reinterpret_cast<SmemT<PB>*>(smem_raw);
+    float4* RR;  // the residual ring: its own array, or the r ring itself
+    if constexpr (PB)
+        RR = S.r;
+    else
+        RR = S.rr;
+    constexpr int PSTR = PB ? RNP16 : RNP;               // P ring slot, elements
+    constexpr unsigned PESZ = PB ? 8u : 16u;             // P element bytes
+    constexpr unsigned PBYTES = PB ? RBYTES16 : RBYTES;  // bytes one P box load delivers
+    const float psc = PB ? __ldg(pscale) : 1.f;          // the FP16 copy's scale
     const int n = g.n;
     const int tk = threadIdx.x, tj = threadIdx.y, tid = tj * SK + tk;
     const int k0 = blockIdx.x * SK, j0 = blockIdx.y * SJ, i0 = blockIdx.z * chunk;
@@ -746,6 +790,7 @@ __global__ void __launch_bounds__(NT, 3) k_sweep_tma(const __grid_constant__ CUt
     const uint32_t bar = (uint32_t)__cvta_generic_to_shared(&S.bar);
     auto tma_x = [&](int slot, int p) { tma3(sx + 16u * slot, &tmx, 4 * (k0 - 1), j0 - 1, p + 1, bar); };
     auto tma_r = [&](unsigned base, int slot, int p, const CUtensorMap* tm) { tma3(base + 16u * slot, tm, 4 * k0, j0, p + 1, bar); };
+    auto tma_p = [&](int slot, int p) { tma3(sP + PESZ * slot, &tmp, 4 * k0, j0, p + 1, bar); };
     uint32_t phase = 0;
     // every thread waits for the current phase; a wait that gives up (about a second) makes
     // the whole block record the error and leave at the next barrier
@@ -777,7 +822,7 @@ __global__ void __launch_bounds__(NT, 3) k_sweep_tma(const __grid_constant__ CUt
                         const float4 v = S.x[idx];
                         return Q4<float>{v.x, v.y, v.z, v.w};
                     };
-                    const float4 pv = S.P[ps + e];
+                    const float4 pv = ldv(S.P[ps + e], psc);
                     float o[4];
                     lap_core<float>(q(xb + xi), q(xa + xi), q(xc + xi), q(xb + xi - XK), q(xb + xi + XK), q(xb + xi - 1),
                                     q(xb + xi + 1), Q4<float>{pv.x, pv.y, pv.z, pv.w}, vol, o);
@@ -791,7 +836,7 @@ __global__ void __launch_bounds__(NT, 3) k_sweep_tma(const __grid_constant__ CUt
                     out = rv;  // r is zero on fixed unknowns
                 }
             }
-            S.rr[rrs + e] = out;
+            RR[rrs + e] = out;
         };
         one(re0, rx0, rb0);
         if (re1 < RN) one(re1, rx1, rb1);
@@ -803,12 +848,12 @@ __global__ void __launch_bounds__(NT, 3) k_sweep_tma(const __grid_constant__ CUt
         if (!(b ? pok1 : pok0) || p < 0 || p >= n) return;
         const int dk = b ? pdk1 : pdk0;
         const int ri = pdj * RK + dk, xi = (pdj + 1) * XK + (dk + 1);
-        const float4 rc = S.rr[rr0 + ri], pc = S.P[p0 + ri];
+        const float4 rc = RR[rr0 + ri], pc = ldv(S.P[p0 + ri], psc);
         const uint8_t mo = S.m[m0s + xi];
         const float rL[3] = {rc.y, rc.z, rc.w}, pL[3] = {pc.y, pc.z, pc.w};
         const uint8_t mhi[3] = {S.m[m1s + xi], S.m[m0s + xi + XK], S.m[m0s + xi + 1]};
-        const float rh[3] = {S.rr[rr1 + ri].y, S.rr[rr0 + ri + RK].z, S.rr[rr0 + ri + 1].w};
-        const float ph[3] = {S.P[p1 + ri].y, S.P[p0 + ri + RK].z, S.P[p0 + ri + 1].w};
+        const float rh[3] = {RR[rr1 + ri].y, RR[rr0 + ri + RK].z, RR[rr0 + ri + 1].w};
+        const float ph[3] = {ldv(S.P[p1 + ri], psc).y, ldv(S.P[p0 + ri + RK], psc).z, ldv(S.P[p0 + ri + 1], psc).w};
         const uint8_t bit[3] = {MU, MV, MW};
         float num = rc.x, den = 2.f * pc.x;
 #pragma unroll
@@ -823,9 +868,13 @@ __global__ void __launch_bounds__(NT, 3) k_sweep_tma(const __grid_constant__ CUt
 
     // ring slots as element offsets (rotated each plane)
     int xm1 = 0 * XN, x0 = 1 * XN, x1 = 2 * XN, x2 = 3 * XN;  // x(i-1), x(i), x(i+1), x(i+2)
-    int pm1 = 0 * RNP, p0 = 1 * RNP, p1 = 2 * RNP;            // P(i-1), P(i), P(i+1)
+    int pm1 = 0 * PSTR, p0 = 1 * PSTR, p1 = 2 * PSTR;         // P(i-1), P(i), P(i+1)
     int r0 = 0 * RNP, r1 = 1 * RNP;                           // r(i), r(i+1)
     int rrm1 = 0 * RN, rr0 = 1 * RN;                          // rr(i-1), rr(i)
+    if constexpr (PB) {  // rr written over r in place: one ring of three slots
+        rrm1 = r0;
+        rr0 = r1;
+    }
     int mm1 = 0 * XN, m0 = 1 * XN, m1 = 2 * XN, m2 = 3 * XN;  // masks of planes i-1 .. i+2
 
     // prologue: planes i0-2 .. i0+1 of x, i0-1 .. i0+1 of P, i0-1 and i0 of r, masks i0-1 .. i0+2
@@ -835,16 +884,16 @@ __global__ void __launch_bounds__(NT, 3) k_sweep_tma(const __grid_constant__ CUt
     }
     __syncthreads();
     if (tid == 0) {
-        arm_tx(bar, (HAS_X ? 4 * XBYTES : 0) + 5 * RBYTES);
+        arm_tx(bar, (HAS_X ? 4 * XBYTES : 0) + 3 * PBYTES + 2 * RBYTES);
         if (HAS_X) {
             tma_x(xm1, i0 - 2);
             tma_x(x0, i0 - 1);
             tma_x(x1, i0);
             tma_x(x2, i0 + 1);
         }
-        tma_r(sP, pm1, i0 - 1, &tmp);
-        tma_r(sP, p0, i0, &tmp);
-        tma_r(sP, p1, i0 + 1, &tmp);
+        tma_p(pm1, i0 - 1);
+        tma_p(p0, i0);
+        tma_p(p1, i0 + 1);
         tma_r(sr, r0, i0 - 1, &tmr);
         tma_r(sr, r1, i0, &tmr);
     }
@@ -866,7 +915,7 @@ __global__ void __launch_bounds__(NT, 3) k_sweep_tma(const __grid_constant__ CUt
         asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
         arm_tx(bar, (HAS_X ? XBYTES : 0) + RBYTES);
         if (HAS_X) tma_x(xm1, i0 + 2);  // x(i0+2) replaces x(i0-2)
-        tma_r(sr, r0, i0 + 1, &tmr);    // r(i0+1) replaces r(i0-1)
+        tma_r(sr, PB ? 2 * RNP : r0, i0 + 1, &tmr);  // r(i0+1): the third slot, or replaces r(i0-1)
     }
     // residual of i0: x(i0-1, i0, i0+1) = (x0, x1, x2), r(i0) = r1, P(i0) = p0, mask(i0) = m0
     residual(i0, x0, x1, x2, r1, p0, m0, rr0);
@@ -883,9 +932,15 @@ __global__ void __launch_bounds__(NT, 3) k_sweep_tma(const __grid_constant__ CUt
         x0 = x1;
         x1 = x2;
         x2 = t;
-        t = r0;
-        r0 = r1;
-        r1 = t;
+        if constexpr (PB) {  // rr(i0) in slot 1, r(i0+1) in slot 2, slot 0 (rr(i0-1)) free
+            r0 = 0;
+            r1 = rrm1 = 2 * RNP;
+            rr0 = RNP;
+        } else {
+            t = r0;
+            r0 = r1;
+            r1 = t;
+        }
     }
     gm += 4 * plane;  // plane i0+3
     float4* gout = xout + (i0 + 1) * plane + out_jk;
@@ -894,9 +949,9 @@ __global__ void __launch_bounds__(NT, 3) k_sweep_tma(const __grid_constant__ CUt
         // stream x(i+3) into the slot of x(i-1), P(i+2) into P(i-1), r(i+2) into r(i)
         if (tid == 0) {
             asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-            arm_tx(bar, (HAS_X ? XBYTES : 0) + 2 * RBYTES);
+            arm_tx(bar, (HAS_X ? XBYTES : 0) + PBYTES + RBYTES);
             if (HAS_X) tma_x(xm1, i + 3);
-            tma_r(sP, pm1, i + 2, &tmp);
+            tma_p(pm1, i + 2);
             tma_r(sr, r0, i + 2, &tmr);
         }
         fetch_m(i + 3, gm);
@@ -906,7 +961,7 @@ __global__ void __launch_bounds__(NT, 3) k_sweep_tma(const __grid_constant__ CUt
         __syncthreads();
         if (out_ok) {
             float4 xo = HAS_X ? S.x[x0 + oxi] : make_float4(0.f, 0.f, 0.f, 0.f);
-            const float4 rv = S.rr[rr0 + ori], pv = S.P[p0 + ori];
+            const float4 rv = RR[rr0 + ori], pv = ldv(S.P[p0 + ori], psc);
             const uint8_t mo = S.m[m0 + oxi];
             const bool cell = jk_cell && i < n;
             const bool own_col = ((i & 1) ^ opar) == 0;  // (i + j + k + flag) even
@@ -947,12 +1002,19 @@ __global__ void __launch_bounds__(NT, 3) k_sweep_tma(const __grid_constant__ CUt
             pm1 = p0;
             p0 = p1;
             p1 = t;
-            t = r0;
-            r0 = r1;
-            r1 = t;
-            t = rrm1;
-            rrm1 = rr0;
-            rr0 = t;
+            if constexpr (PB) {  // (rr(i), r(i+1), free) <- (r(i+1) now rr(i+1), r(i+2), rr(i))
+                t = rr0;
+                rr0 = r1;
+                r1 = rrm1 = r0;
+                r0 = t;
+            } else {
+                t = r0;
+                r0 = r1;
+                r1 = t;
+                t = rrm1;
+                rrm1 = rr0;
+                rr0 = t;
+            }
             t = mm1;
             mm1 = m0;
             m0 = m1;
@@ -998,6 +1060,15 @@ bool slot_map(EncodeTiled enc, CUtensorMap* map, const void* base, const Geom& g
                CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+// the same for an FP16 slot array (four 2-byte values per slot)
+bool slot_map16(EncodeTiled enc, CUtensorMap* map, const void* base, const Geom& g, int bk, int bj) {
+    const cuuint64_t dims[3] = {(cuuint64_t)g.sz * 4, (cuuint64_t)g.sy, (cuuint64_t)g.sx};
+    const cuuint64_t strides[2] = {(cuuint64_t)g.sz * 8, (cuuint64_t)g.sy * g.sz * 8};
+    const cuuint32_t box[3] = {(cuuint32_t)(4 * bk), (cuuint32_t)bj, 1}, es[3] = {1, 1, 1};
+    return enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 3, const_cast<void*>(base), dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+               CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 // per device: kernel attributes set, and the flag a TMA sweep sets when its wait gave up
 bool g_attr_set[MAX_DEVICES] = {}, g_tattr_set[MAX_DEVICES] = {};
 int* g_sweep_err[MAX_DEVICES] = {};
@@ -1014,7 +1085,7 @@ int sweep_status(cudaStream_t st, int* timed_out) {
 }
 
 int sweep32(cudaStream_t st, const Geom& g, float vol, const float4* r, const float4* xin, float4* xout, const uint8_t* m,
-            const float4* P, int flag, bool lap) {
+            const float4* P, int flag, bool lap, const __half* P16, const float* p16_scale) {
     const int dev = device_slot();
     if (dev < 0) {
         set_error("sweep32: device ordinal beyond %d", MAX_DEVICES - 1);
@@ -1033,22 +1104,31 @@ int sweep32(cudaStream_t st, const Geom& g, float vol, const float4* r, const fl
     const int chunk = g.n >= 192 ? 32 : g.n >= 96 ? 8 : g.n >= 48 ? 4 : g.n >= 24 ? 2 : 1;
     dim3 grid((g.n + SK) / SK, (g.n + SJ) / SJ, (g.n + chunk) / chunk), block(SK, SJ);
     if (lap && encoder()) {
-        const int smem_t = (int)sizeof(SmemT);
+        const int smem_t = (int)sizeof(SmemT<false>), smem_b = (int)sizeof(SmemT<true>);
         if (!g_tattr_set[dev]) {
-            STG_CK(cudaFuncSetAttribute(k_sweep_tma<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_t));
-            STG_CK(cudaFuncSetAttribute(k_sweep_tma<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_t));
+            STG_CK(cudaFuncSetAttribute(k_sweep_tma<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_t));
+            STG_CK(cudaFuncSetAttribute(k_sweep_tma<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_t));
+            STG_CK(cudaFuncSetAttribute(k_sweep_tma<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_b));
+            STG_CK(cudaFuncSetAttribute(k_sweep_tma<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_b));
             STG_CK(cudaMalloc((void**)&g_sweep_err[dev], sizeof(int)));
             STG_CK(cudaMemset(g_sweep_err[dev], 0, sizeof(int)));
             g_tattr_set[dev] = true;
         }
         CUtensorMap mx{}, mr{}, mp{};
         const EncodeTiled enc = encoder();
-        const bool ok = (!xin || slot_map(enc, &mx, xin, g, XK, XJ)) && slot_map(enc, &mr, r, g, RK, RJ) && slot_map(enc, &mp, P, g, RK, RJ);
+        if (P16 && !p16_scale) P16 = nullptr;  // the FP16 copy needs its scale
+        const bool ok = (!xin || slot_map(enc, &mx, xin, g, XK, XJ)) && slot_map(enc, &mr, r, g, RK, RJ) &&
+                        (P16 ? slot_map16(enc, &mp, P16, g, RK, RJ) : slot_map(enc, &mp, P, g, RK, RJ));
         if (ok) {
-            if (xin)
-                k_sweep_tma<true><<<grid, block, smem_t, st>>>(mx, mr, mp, g, vol, xout, m, flag, chunk, g_sweep_err[dev]);
+            int* err = g_sweep_err[dev];
+            if (P16 && xin)
+                k_sweep_tma<true, true><<<grid, block, smem_b, st>>>(mx, mr, mp, g, vol, xout, m, flag, chunk, err, p16_scale);
+            else if (P16)
+                k_sweep_tma<false, true><<<grid, block, smem_b, st>>>(mr, mr, mp, g, vol, xout, m, flag, chunk, err, p16_scale);
+            else if (xin)
+                k_sweep_tma<true, false><<<grid, block, smem_t, st>>>(mx, mr, mp, g, vol, xout, m, flag, chunk, err, nullptr);
             else
-                k_sweep_tma<false><<<grid, block, smem_t, st>>>(mr, mr, mp, g, vol, xout, m, flag, chunk, g_sweep_err[dev]);
+                k_sweep_tma<false, false><<<grid, block, smem_t, st>>>(mr, mr, mp, g, vol, xout, m, flag, chunk, err, nullptr);
             STG_LAUNCH_CK();
             return STG_OK;
         }
