@@ -198,8 +198,8 @@ int sweep(stg_t* h, Level& L, const float4* r, int flag, bool first) {
     float vol = (float)L.vol;
     // profile class 1: sweeps of the finest level; 10: of the coarser levels
     const int cls = &L == &fine(h) ? 1 : 10;
-    // the adapters keep the FP32 penalty and residual (the reference smoother to FP32
-    // rounding); the solver's sweeps stage both in BF16 (sweep.cu SmemT)
+    // the adapters keep the FP32 penalty (the reference smoother to FP32 rounding); the
+    // solver's sweeps stage the level's FP16 copy with its scale (sweep.cu SmemT)
     const __half* P16 = h->reference_cycle ? nullptr : L.P16;
     const float* psc = h->d_pscale + (&L - h->lv.data());
     if (first) {
@@ -522,7 +522,7 @@ int solve_core(stg_t* h, const d4* b, d4* x, stg_stats* stats) {
         // d2 = V^T V_{j+1}; pass 3 (classical Gram-Schmidt's second sweep, only when the
         // first cancelled nearly all of w: ||V_{j+1}|| < 0.1 ||w||) V_{j+1} -= sum sig^2 d2 V.
         // The looser trigger than the usual 0.7 costs orthogonality of order 1e-6 in FP32,
-        // far below the 1e-4 an inner solve is asked for; the FP64 refinement is the judge.
+        // far below the 1e-4 an inner solve is asked for; the FP64 refinement decides.
         sig[0] = 1.0;
         const double one = 1.0;
         STG_CK(cudaMemcpyAsync(h->dsig2, &one, sizeof(double), cudaMemcpyHostToDevice, h->st));
@@ -607,7 +607,7 @@ int solve_core(stg_t* h, const d4* b, d4* x, stg_stats* stats) {
             if (h->opts.verbose > 1) fprintf(stderr, "[stg]   inner %d  est %.3e\n", j, est);
             // a learned step that cut the estimate by less than 20% ends the network's use in
             // this solve (FGMRES is flexible, so the basis built so far stays valid). The
-            // first step of a refinement step is not judged: its reduction depends on how
+            // first step of a refinement step is not assessed: its reduction depends on how
             // the right-hand side lies (a boundary-driven b gives about 2% with plain
             // multigrid too).
             if (h->net_on && j > 0 && !aug_step && est > 0.8 * prev_est) {
