@@ -155,7 +155,7 @@ def ref_mma():
     np.savez_compressed(os.path.join(HERE, "ref_mma.npz"), dfdx=np.array(dfs), x=xs)
 
 
-def oracle_loop2d(n=64, iters=20, frac=0.3, rmin=1.5):
+def oracle_loop2d(n=64, iters=20, frac=0.3, rmin=1.5, save=True):
     from oracle import pyoracle as po
 
     po.build()
@@ -181,10 +181,12 @@ def oracle_loop2d(n=64, iters=20, frac=0.3, rmin=1.5):
         dc = po.filt(sens, rmin, transpose=True)
         x = po.oc_update(x, dc, vw / n ** 2, vw, frac)[0].reshape(n, n)
         print("loop2d", it, Js[-1], flush=True)
-    np.savez_compressed(os.path.join(HERE, "oracle_loop2d_n64.npz"), objective=np.array(Js), x_last=x_last)
+    if save:
+        np.savez_compressed(os.path.join(HERE, "oracle_loop2d_n64.npz"), objective=np.array(Js), x_last=x_last)
+    return np.array(Js), x_last
 
 
-def oracle_loop3d(n=32, iters=8, frac=0.15, rmin=1.5):
+def oracle_loop3d(n=32, iters=8, frac=0.15, rmin=1.5, save=True):
     """The 3D design loop (parabolic inlet on a centred n/4 square, OC, filter 1.5, BP alpha
     1e4) for `iters` iterations; from iteration 5 the designs are high-contrast (density
     down to 1e-6 .. 1e-8) and each solve takes over a hundred GMRES steps."""
@@ -214,7 +216,9 @@ def oracle_loop3d(n=32, iters=8, frac=0.15, rmin=1.5):
         dc = po.filt(sens, rmin, transpose=True)
         x = po.oc_update(x, dc, vw / n ** 3, vw, frac)[0].reshape(n, n, n)
         print("loop3d", it, Js[-1], flush=True)
-    np.savez_compressed(os.path.join(HERE, "oracle_loop3d_n32.npz"), objective=np.array(Js), x_last=x_last)
+    if save:
+        np.savez_compressed(os.path.join(HERE, "oracle_loop3d_n32.npz"), objective=np.array(Js), x_last=x_last)
+    return np.array(Js), x_last
 
 
 if __name__ == "__main__":

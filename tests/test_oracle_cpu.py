@@ -202,3 +202,16 @@ def test_density_noise_statistics(oracle):
     r = oracle.density_noise(16, 0, 4.0)
     assert r.min() >= 0 and r.max() <= 1 and abs(r.mean() - 0.5) < 0.05
     assert np.array_equal(r, oracle.density_noise(16, 0, 4.0))
+
+
+def test_design_loop_fixtures_are_the_oracles():
+    """The committed design-loop fixtures (tests/golden/oracle_loop*_n*.npz) are what the
+    oracle's loops produce: their first iterations reproduce the stored objectives."""
+    from tests.golden import make_golden as mg
+
+    J2, _ = mg.oracle_loop2d(iters=3, save=False)
+    g2 = np.load(os.path.join(os.path.dirname(__file__), "golden", "oracle_loop2d_n64.npz"))
+    assert np.allclose(J2, g2["objective"][:3], rtol=1e-9, atol=0)
+    J3, _ = mg.oracle_loop3d(iters=2, save=False)
+    g3 = np.load(os.path.join(os.path.dirname(__file__), "golden", "oracle_loop3d_n32.npz"))
+    assert np.allclose(J3, g3["objective"][:2], rtol=1e-9, atol=0)
