@@ -268,6 +268,50 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+# ------------------------------------------------------------------ replicas
+class Ranks:
+    """Bookkeeping of N independent replicas (one process per GPU, no data-path
+    collective): barriers around the timed region and the max / sum of per-rank scalars.
+    The timing reductions run on `device` ("cuda" with NCCL on the GPU boxes, "cpu" with
+    gloo in the tests)."""
+
+    def __init__(self, world, rank, device="cuda"):
+        self.world, self.rank, self.device = world, rank, device
+
+    def barrier(self):
+        import torch
+
+        if self.world > 1:
+            torch.distributed.barrier()
+        if self.device == "cuda":
+            torch.cuda.synchronize()
+
+    def _reduce(self, v, op):
+        import torch
+
+        if self.world == 1:
+            return v
+        t = torch.tensor([v], dtype=torch.float64, device=self.device)
+        torch.distributed.all_reduce(t, op=op)
+        return float(t.item())
+
+    def max(self, v):
+        import torch
+
+        return self._reduce(v, torch.distributed.ReduceOp.MAX if self.world > 1 else None)
+
+    def sum(self, v):
+        import torch
+
+        return self._reduce(v, torch.distributed.ReduceOp.SUM if self.world > 1 else None)
+
+
+def whole_job_seconds_per_solve(t_max_s, steps, world):
+    """Weak scaling: every rank solves `steps` problems of its own; the job's time per solve
+    is the slowest rank's time over all ranks' solves."""
+    return t_max_s / (steps * world)
+
+
 # ------------------------------------------------------------------ our arm
 def run_ours(args):
     import torch
@@ -284,24 +328,8 @@ def run_ours(args):
     n = args.n
     cell_vol, cell_fixed, cell_b, face_vol, face_fixed, face_b = parabolic_bc(n)
 
-    def barrier():
-        if world > 1:
-            torch.distributed.barrier()
-        torch.cuda.synchronize()
-
-    def max_over_ranks(v):
-        if world == 1:
-            return v
-        t = torch.tensor([v], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        return float(t.item())
-
-    def sum_over_ranks(v):
-        if world == 1:
-            return v
-        t = torch.tensor([v], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(t)
-        return float(t.item())
+    ranks = Ranks(world, rank, "cuda")
+    barrier, max_over_ranks, sum_over_ranks = ranks.barrier, ranks.max, ranks.sum
 
     stream = torch.cuda.current_stream()
 
@@ -345,7 +373,7 @@ def run_ours(args):
     s = make_solver(capi.STG_METHOD_PLAIN)
     ms, stats, launches, clocks, _ = timed_device(s, args.steps, args.warmup, profile=False)
     t_max = max_over_ranks(ms / 1e3)
-    value = t_max / (args.steps * world)
+    value = whole_job_seconds_per_solve(t_max, args.steps, world)
     launches = int(sum_over_ranks(launches))
     # per-kernel-class CUDA-event timing of separate solves, for the roofline and the table
     _, _, _, _, prof = timed_device(s, PROFILED_SOLVES, 0, profile=True)
@@ -382,7 +410,7 @@ def run_ours(args):
     e1.record(stream)
     barrier()
     e2e_ms = max(e0.elapsed_time(e1), (time.perf_counter() - t0) * 1e3)
-    e2e_value = max_over_ranks(e2e_ms / 1e3) / (args.steps * world)
+    e2e_value = whole_job_seconds_per_solve(max_over_ranks(e2e_ms / 1e3), args.steps, world)
     h2d = sum(f.nbytes for f in fpen_p) + cb_p.nbytes + sum(f.nbytes for f in fb_p)
     d2h = p_out.nbytes + sum(v.nbytes for v in v_out)
 
@@ -393,7 +421,7 @@ def run_ours(args):
 
         def leg(sv):
             ms_, st_, _, _, _ = timed_device(sv, k, 1)
-            return {"s_per_solve": max_over_ranks(ms_ / 1e3) / (k * world),
+            return {"s_per_solve": whole_job_seconds_per_solve(max_over_ranks(ms_ / 1e3), k, world),
                     "v_cycles": statistics.mean(x["inner_iters"] for x in st_),
                     "max_rel_residual": max(x["rel_residual"] for x in st_)}
 
