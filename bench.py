@@ -12,6 +12,12 @@ Borrvall-Petersson alpha law (amax 1e4). Working set is ~27 GB, far above the 12
   methods  the same solve with the reference's two sweeps per colour, the mixed form (BF16
          coarse corrections) and the learned form (U-Net trained on the GPU at 64^3 on the
          same problem family, applied at 256^3); training time reported, not in the timed region
+  design_loop_2d / design_loop_3d  the fluid_topo driver's design loops (2D 64^2, 20
+         iterations; 3D 128^3 at fraction 0.15, 40 iterations), every solve to its FP64
+         tolerance, with the largest final residual of any solve
+  roofline / vcycle_hbm  the dominant kernel class and the whole V-cycle: algorithmic bytes
+         over CUDA-event time against the measured copy bandwidth; traffic from the
+         committed ncu summary
   --impl reference: the CPU reference restatement (oracle) on the host cores.
 
 N>1 (torchrun): independent replicas, one per GPU, barrier + max over ranks.
