@@ -79,8 +79,10 @@ struct stg_ctx {
     // rather than the reference's sums, which the component adapters reproduce
     bool hier_flow = false;
     // a refinement step of the solve in progress ended at the basis limit short of its
-    // target: the rest of the solve smooths with at least two sweeps per colour
-    bool boost = false;
+    // target: the rest of the solve smooths with at least two sweeps per colour; a solve
+    // that boosted makes the next solve of the handle start boosted (design loops alternate
+    // forward and adjoint solves on the same, slowly changing, operator)
+    bool boost = false, boost_next = false;
     bool x0_valid[2] = {false, false};  // x64 / lam64 hold a previous solution (warm start)
     bool has_x0(const stg::d4* x) const { return (x == x64 && x0_valid[0]) || (x == lam64 && x0_valid[1]); }
     int* dflag = nullptr;

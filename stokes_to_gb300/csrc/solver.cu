@@ -454,11 +454,16 @@ int solve_core(stg_t* h, const d4* b, d4* x, stg_stats* stats) {
     // without, 270 with four). The slots must lie in the first group the update sums.
     const int naug = std::max(0, std::min({4, m / 2, m - axpy_last_chunk(m)}));
     int have_aug = 0, aug_next = 0;  // filled slots Z[m-have_aug .. m-1]; next to overwrite
+    bool stalled_any = false;  // a refinement step of this solve ran out of basis
     struct BoostGuard {
         stg_t* h;
-        ~BoostGuard() { h->boost = false; }
-    } boost_guard{h};
-    h->boost = false;
+        const bool& stalled;
+        ~BoostGuard() {
+            h->boost_next = stalled;
+            h->boost = false;
+        }
+    } boost_guard{h, stalled_any};
+    h->boost = h->boost_next && h->dim == 3 && !h->net_on;
     std::vector<double> H((size_t)(m + 1) * m), cs(m), sn(m), g(m + 1), y(m), hcol(m + 2), sig(m + 1);
     double rel = 0, rn = 0;
     int status = STG_E_NOT_CONVERGED;
@@ -641,7 +646,7 @@ int solve_core(stg_t* h, const d4* b, d4* x, stg_stats* stats) {
         // a stalled step means the V-cycle is too weak for this design (high-contrast
         // optimised densities): the rest of the solve smooths twice per colour (about 1.5x
         // the V-cycle's cost for 1.5-2x fewer V-cycles there)
-        if (h->dim == 3 && stalled) h->boost = true;
+        if (h->dim == 3 && stalled) h->boost = stalled_any = true;
     }
     h->df_x = h->df_b = nullptr;  // finish() changes x; adapters must not see the copies
     if (h->finish) STG_TRY(h->finish(h, b, x));
