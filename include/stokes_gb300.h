@@ -58,8 +58,8 @@ typedef struct stg_opts {
                             colour reaches the same FP64 tolerance in as many V-cycles at
                             2/3 of the time. A refinement step that uses the whole basis
                             without reaching its target raises it to 2 for the rest of
-                            the solve (3D). The LinearMapping adapters always run the
-                            reference smoother. */
+                            the solve and for the handle's next solve (3D). The
+                            LinearMapping adapters always run the reference smoother. */
     int warm_start;      /* 1: start each solve from the previous solution of the same
                             equation (the forward one for stg_solve, the adjoint one for
                             stg_adjoint_sensitivity) instead of zero, unless its residual
