@@ -650,18 +650,20 @@ __global__ void __launch_bounds__(NT, 3) k_sweep_lap(Geom g, float vol, const fl
 // mbarrier counting the bytes, instead of every thread issuing 16-byte copies. The boxes
 // read zero outside the allocation, as the copies did. Everything else is k_sweep_lap.
 constexpr int RNP = 344;  // r / P ring slot in float4s: RN padded to 128 bytes (TMA destinations)
-constexpr int RNP16 = 352;  // P ring slot in BF16 quadruples (8 bytes): RN padded to 128 bytes
+constexpr int RNP16 = 352;  // P ring slot in FP16 quadruples (8 bytes): RN padded to 128 bytes
 constexpr unsigned XBYTES = XN * 16, RBYTES = RN * 16, RBYTES16 = RN * 8;
 static_assert(RNP >= RN && (RNP * 16) % 128 == 0 && (XN * 16) % 128 == 0, "TMA ring slots must be 128-byte aligned");
 static_assert(RNP16 >= RN && (RNP16 * 8) % 128 == 0, "TMA ring slots must be 128-byte aligned");
 
 // PB = false: P in FP32, separate rings for r and the computed residual rr (the adapters,
 // which reproduce the reference smoother to FP32 rounding). PB = true (the solver's own
-// sweeps): P staged from its BF16 copy, and rr written over r in place in a three-slot ring
-// (rr(i), r(i+1) turning into rr(i+1), r(i+2) in flight): 68.4 -> 55.2 KB of shared memory,
-// so four blocks (32 warps) share an SM instead of three. The kernel is latency- and
+// sweeps): P staged from the level's FP16 copy (divided by a per-level power-of-two scale,
+// multiplied back on reading), and rr written over r in place in a three-slot ring (rr(i),
+// r(i+1) turning into rr(i+1), r(i+2) in flight): 68.4 -> 55.2 KB of shared memory, so
+// four blocks (32 warps) share an SM instead of three. The kernel is latency- and
 // issue-bound, and the extra warps hide the per-plane barriers. The smoother works with P
-// to 2^-9 relative; the V-cycle is a preconditioner inside FP64 refinement.
+// to 2^-11 relative, which keeps the FP32 smoother's V-cycle count (BF16's 2^-8 did not);
+// the V-cycle is a preconditioner inside FP64 refinement.
 template <bool PB>
 struct SmemT;
 template <>
@@ -693,7 +695,6 @@ __device__ __forceinline__ float4 ldv(const uint2& v, float sc) {
     const float2 a = __half22float2(*reinterpret_cast<const __half2*>(&v.x)), b = __half22float2(*reinterpret_cast<const __half2*>(&v.y));
     return make_float4(a.x * sc, a.y * sc, b.x * sc, b.y * sc);
 }
-
 
 // 3D box load of the tensor map at coordinates (c0, c1, c2) into shared memory, counted on bar
 __device__ __forceinline__ void tma3(unsigned dst, const CUtensorMap* map, int c0, int c1, int c2, unsigned bar) {
