@@ -63,6 +63,11 @@ def test_driver_rejects_bad_flags(driver, tmp_path):
     assert r.returncode == 2 and "-frac" in r.stderr
     r = subprocess.run([driver, "-bogus", "1"], capture_output=True, text=True)
     assert r.returncode == 2 and "unknown flag" in r.stderr
+    # the solver flags are known (parsed before the boundary dump, which needs no GPU)
+    out = tmp_path / "dump"
+    r = subprocess.run([driver, "-driver", "1", "-test", "1", "-s", "16", "-frac", "0.15", "-inner", "24", "-maxouter", "40",
+                        "-warm", "0", "-dump_boundary", str(out)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
 
 
 def test_driver_fails_loudly_without_gpu(driver, tmp_path):
