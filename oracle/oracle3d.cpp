@@ -287,6 +287,33 @@ void update_subsystem(Descr& c, const Descr& f) {
     c.finish();
 }
 
+// The GPU solver's own coarse penalties (its "flow rule", not in the reference): a coarse
+// face takes 8 x the smallest penalty among its present, free children instead of the sum;
+// cell penalties keep the sum. Applied after update_subsystem, which fixes the coarse
+// unknowns, so fixed coarse faces stay at zero.
+void flow_penalties(Descr& c, const Descr& f) {
+    for (int d = 0; d < 3; d++) {
+        double* cp = c.penalty.data() + c.g.face_off(d);
+        const double* fp = f.penalty.data() + f.g.face_off(d);
+        const uint8_t* ff = f.fixed.data() + f.g.face_off(d);
+        const uint8_t* cf = c.fixed.data() + c.g.face_off(d);
+        for (int i = 0; i < c.g.face_size(d); i++) {
+            if (cf[i]) continue;
+            int x, y, z;
+            c.g.ind_face(i, d, x, y, z);
+            double lo = -1.0;
+            for (int k = 0; k < 8; k++) {
+                const int fx = 2 * x + (k & 1), fy = 2 * y + ((k >> 1) & 1), fz = 2 * z + ((k >> 2) & 1);
+                if (!f.g.face_valid(fx, fy, fz, d)) continue;
+                const int j = f.g.face_ind(fx, fy, fz, d);
+                if (ff[j]) continue;
+                if (lo < 0.0 || fp[j] < lo) lo = fp[j];
+            }
+            if (lo >= 0.0) cp[i] = 8.0 * lo;
+        }
+    }
+}
+
 // StokeFlowDownSample3D::applyMapping (stoke/StokeFlowSubSystem3D.cu:32-52).
 void restrict_r(const Descr& c, const Descr& f, double* rc, const double* rf) {
     down_sample<double>(c.g, f.g, rc, rf, [](double* v, int) {
@@ -586,8 +613,11 @@ void hierarchy_init(Hierarchy& H, int n) {
 
 // FluidSteadyState3D::solve set-up half (stoke/FluidSteadyState3D.cpp:152-156):
 // coarse descriptors, smoother blocks, coarsest LU.
-void hierarchy_update(Hierarchy& H) {
-    for (int i = H.l - 2; i >= 0; i--) update_subsystem(H.lv[i], H.lv[i + 1]);
+void hierarchy_update(Hierarchy& H, bool flow) {
+    for (int i = H.l - 2; i >= 0; i--) {
+        update_subsystem(H.lv[i], H.lv[i + 1]);
+        if (flow) flow_penalties(H.lv[i], H.lv[i + 1]);
+    }
     for (int i = 1; i < H.l; i++) {
         vanka_setup(H.lv[i], 0, H.red[i], H.w);
         vanka_setup(H.lv[i], 1, H.black[i], H.w);

@@ -102,7 +102,9 @@ void dense_setup(const Descr& ds, bool closed, Dense& D, Work& w);
 void dense_apply(const Dense& D, double* out, const double* r);
 int level_count(int n);
 void hierarchy_init(Hierarchy& H, int n);
-void hierarchy_update(Hierarchy& H);
+// flow: the GPU solver's coarse penalties (8 x the smallest free child) instead of the sums
+void flow_penalties(Descr& c, const Descr& f);
+void hierarchy_update(Hierarchy& H, bool flow = false);
 void vcycle(Hierarchy& H);
 void mg_apply(Hierarchy& H, double* out, const double* in);
 void gmres_solve(Hierarchy& H, const double* b, double* x, int max_iter, double abs_thres, double rel_thres,

@@ -152,6 +152,8 @@ void orc3_set_b_blocked(void* p, const double* b) {
 
 // FluidSteadyState3D::solve set-up half (:152-156).
 void orc3_setup(void* p) { hierarchy_update(((Handle*)p)->H); }
+// The same with the GPU solver's coarse penalties (not the reference's).
+void orc3_setup_flow(void* p) { hierarchy_update(((Handle*)p)->H, true); }
 
 // GMRES::Solve with the reference thresholds passed in (common_cpx/GMRES.cpp:20-110).
 // stats = {iters, restarts, rel_true, abs_true, precond_res, seconds}

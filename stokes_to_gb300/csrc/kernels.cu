@@ -297,7 +297,8 @@ __global__ void k_prolong64(Geom gf, Geom gc, const d4* __restrict__ xc, const u
 // On the 3D loop's iteration-5 design (fraction 0.15) the sum left the residual at 0.21
 // (64^3) and 0.71 (128^3) after 600 V-cycles; the smallest penalty converges in 68 and 180.
 // Harmonic and geometric means and a per-layer minimum (mean along the face normal) did no
-// better; smooth (noise) densities take the same V-cycle count under every rule.
+// better; smooth (noise) densities take the same V-cycle count under every rule. The
+// oracle restates the rule (oracle/oracle3d.cpp flow_penalties).
 template <bool FLOW>
 __global__ void k_coarsen(Geom gc, Geom gf, const uint8_t* __restrict__ mf, const d4* __restrict__ Pf, uint8_t* __restrict__ mc,
                           d4* __restrict__ Pc64, float4* __restrict__ Pc32) {

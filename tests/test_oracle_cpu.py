@@ -215,3 +215,30 @@ def test_design_loop_fixtures_are_the_oracles():
     J3, _ = mg.oracle_loop3d(iters=2, save=False)
     g3 = np.load(os.path.join(os.path.dirname(__file__), "golden", "oracle_loop3d_n32.npz"))
     assert np.allclose(J3, g3["objective"][:2], rtol=1e-9, atol=0)
+
+
+def test_flow_rule_coarse_penalties_keep_channels_open(oracle):
+    """The GPU solver's coarse penalties (8 x the smallest free child instead of the sum),
+    restated in the oracle: on a high-contrast design of the 32^3 loop (iteration 7 of the
+    committed fixture) the reference-smoother GMRES converges in a fraction of the
+    iterations the reference's sums need; on a smooth noise density both take the same."""
+    n = 32
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "oracle_loop3d_n32.npz"))
+    b = oracle.bc_parabolic(n)
+
+    def iters(fp, flow):
+        o = oracle.Steady3D(n)
+        o.init_boundary(b)
+        o.update_penalty(np.zeros((n, n, n)), fp)
+        o.update_b(b.cell_b, b.face_b)
+        o.setup(flow=flow)
+        _, st = o.solve(max_iter=60, abs_thr=0.0, rel_thr=1e-13, norm_thr=0.0, restarts=10, true_tol=1e-9)
+        assert st["rel_true"] <= 1e-9
+        return st["iters"]
+
+    fp_channel = oracle.face_penalty(oracle.filt(g["x_last"], 1.5), 1, [1e4])
+    ref, flow = iters(fp_channel, False), iters(fp_channel, True)
+    assert flow < 0.5 * ref, (ref, flow)
+    fp_noise = oracle.face_penalty(oracle.filt(oracle.density_noise(n, 1, 4.0), 1.5), 1, [1e4])
+    ref, flow = iters(fp_noise, False), iters(fp_noise, True)
+    assert abs(flow - ref) <= 2, (ref, flow)
