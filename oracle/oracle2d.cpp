@@ -212,6 +212,30 @@ void update_subsystem(Descr2& c, const Descr2& f) {
     c.finish();
 }
 
+// The GPU solver's own coarse penalties (its "flow rule", not in the reference): a coarse
+// face that is not fixed takes 4 x the smallest penalty among its present children (none of
+// which is fixed then: fixed is the OR of the children) instead of the sum.
+void flow_penalties(Descr2& c, const Descr2& f) {
+    const G2 &cg = c.g, &fg = f.g;
+    for (int d = 0; d < 2; d++) {
+        const int XX = d == 0 ? cg.nx + 8 : cg.nx, YY = d == 0 ? cg.ny : cg.ny + 8;
+        for (int X = 0; X < XX; X++)
+            for (int Y = 0; Y < YY; Y++) {
+                if (!cg.face_valid(X, Y, d)) continue;
+                const int i = cg.face_off(d) + cg.face_ind(X, Y, d);
+                if (c.fixed[i]) continue;
+                double lo = -1.0;
+                for (int q = 0; q < 4; q++) {
+                    const int x = 2 * X + (q & 1), y = 2 * Y + (q >> 1);
+                    if (!fg.face_valid(x, y, d)) continue;
+                    const double v = f.pen[fg.face_off(d) + fg.face_ind(x, y, d)];
+                    if (lo < 0.0 || v < lo) lo = v;
+                }
+                if (lo >= 0.0) c.pen[i] = 4.0 * lo;
+            }
+    }
+}
+
 void restrict_r(const Descr2& c, const Descr2& f, double* rc, const double* rf) {
     down2<double>(c.g, f.g, rc, rf, [](double* v, int) { return v[0] + v[1] + v[2] + v[3]; });
     for (int i = 0; i < c.g.size(); i++)
@@ -417,6 +441,7 @@ void dense_apply(const Dense2& M, double* out, const double* r) {
 // ---------------------------------------------------------------- hierarchy, V-cycle
 struct H2 {
     int l = 0;
+    bool flow = false;  // coarse penalties by the GPU solver's rule instead of the sums
     std::vector<Descr2> lv;
     Descr2 energy;
     Dense2 dense;
@@ -587,11 +612,18 @@ void orc2_update_penalty(void* p, const double* cell_pen, const double* fp0, con
     const double* fp[2] = {fp0, fp1};
     field_to_blocked2(D.g, cell_pen, fp, D.pen.data());
     D.finish();
-    for (int i = H->l - 2; i >= 0; i--) orc2::update_subsystem(H->lv[i], H->lv[i + 1]);
+    for (int i = H->l - 2; i >= 0; i--) {
+        orc2::update_subsystem(H->lv[i], H->lv[i + 1]);
+        if (H->flow) orc2::flow_penalties(H->lv[i], H->lv[i + 1]);
+    }
     orc2::dense_setup(H->lv[0], H->closed, H->dense);
     H->energy.pen = D.pen;
     H->energy.finish();
 }
+
+// Selects the coarse penalties of the next orc2_update_penalty: the reference's sums (0) or
+// the GPU solver's rule (1).
+void orc2_set_flow(void* p, int flow) { ((H2*)p)->flow = flow != 0; }
 
 void orc2_update_b(void* p, const double* cell_b, const double* fb0, const double* fb1) {
     H2* H = (H2*)p;

@@ -335,13 +335,15 @@ def _lib2():
         L.orc2_energy.argtypes = [P, DP]
         L.orc2_coarse_info.restype = I
         L.orc2_coarse_info.argtypes = [P]
-        for name in ["orc2_init_boundary", "orc2_update_penalty", "orc2_update_b", "orc2_set_b_blocked", "orc2_apply_A",
+        for name in ["orc2_init_boundary", "orc2_update_penalty", "orc2_set_flow", "orc2_update_b", "orc2_set_b_blocked",
+                     "orc2_apply_A",
                      "orc2_apply_E", "orc2_level_descr", "orc2_restrict", "orc2_prolong", "orc2_smooth_colour",
                      "orc2_smooth", "orc2_coarse_apply", "orc2_vcycle", "orc2_field_to_blocked", "orc2_blocked_to_field",
                      "orc_bc_test0_2d"]:
             getattr(L, name).restype = None
         L.orc2_init_boundary.argtypes = [P, DP, IP, DP, DP, IP, IP, I]
         L.orc2_update_penalty.argtypes = [P, DP, DP, DP]
+        L.orc2_set_flow.argtypes = [P, I]
         L.orc2_update_b.argtypes = [P, DP, DP, DP]
         L.orc2_set_b_blocked.argtypes = [P, DP]
         L.orc2_apply_A.argtypes = [P, I, DP, DP]
@@ -414,8 +416,11 @@ class Steady2D:
                                   ip(np.ascontiguousarray(b.cell_fixed, dtype=np.int32)), dp(fv[0]), dp(fv[1]), ip(ff[0]),
                                   ip(ff[1]), 1 if b.closed else 0)
 
-    def update_penalty(self, cell_pen, face_pen):
+    def update_penalty(self, cell_pen, face_pen, flow=False):
+        """The penalty with the coarse levels and coarsest matrix; flow=True builds the GPU
+        solver's coarse penalties (4 x the smallest child) instead of the reference's sums."""
         fp = [np.ascontiguousarray(x, dtype=np.float64) for x in face_pen]
+        self.L.orc2_set_flow(self.h, 1 if flow else 0)
         self.L.orc2_update_penalty(self.h, dp(np.ascontiguousarray(cell_pen, dtype=np.float64)), dp(fp[0]), dp(fp[1]))
 
     def update_b(self, cell_b, face_b):

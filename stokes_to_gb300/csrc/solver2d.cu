@@ -247,7 +247,8 @@ __device__ __forceinline__ bool padded2(const G2d& g, int kind, int x, int y) {
 
 // FLOW (the solver's own hierarchy): a coarse face takes 4 x the smallest penalty of its
 // children instead of the sum, so channels narrower than a coarse cell stay open on the
-// coarse levels (the 3D k_coarsen gives the reason).
+// coarse levels (the 3D k_coarsen gives the reason; oracle/oracle2d.cpp flow_penalties
+// restates the rule).
 template <bool FLOW>
 __global__ void k2_coarsen(G2d gc, G2d gf, const uint8_t* __restrict__ ff, const double* __restrict__ fvol,
                            const double* __restrict__ fpen, uint8_t* __restrict__ cf, double* __restrict__ cvol,

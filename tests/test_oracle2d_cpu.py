@@ -194,3 +194,29 @@ def test_filter_and_noise_2d(oracle):
     r = oracle.density_noise(32, 0, 3.0, dim=2)
     assert r.shape == (32, 32) and r.min() >= 0 and r.max() <= 1
     assert np.array_equal(r, oracle.density_noise(32, 0, 3.0, dim=2))
+
+
+def test_flow_rule_coarse_penalties_keep_channels_open_2d(oracle):
+    """The 2D form of the GPU solver's coarse penalties (4 x the smallest child), restated
+    in the oracle: on the last design of the committed 64^2 loop the reference V-cycle's
+    GMRES needs far fewer iterations than with the reference's sums; on a smooth noise
+    density the same."""
+    n = 64
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "oracle_loop2d_n64.npz"))
+    b = oracle.bc_parabolic(n, 2, width=n // 4)
+
+    def iters(fp, flow):
+        o = oracle.Steady2D(n)
+        o.init_boundary(b)
+        o.update_penalty(np.zeros((n, n)), fp, flow=flow)
+        o.update_b(b.cell_b, b.face_b)
+        _, st = o.solve(max_iter=60, abs_thr=0.0, rel_thr=1e-13, norm_thr=0.0, restarts=10, true_tol=1e-10)
+        assert st["rel_true"] <= 1e-10
+        return st["iters"]
+
+    fp = oracle.face_penalty(oracle.filt(g["x_last"], 1.5), 1, [1e4], dim=2)
+    ref, flow = iters(fp, False), iters(fp, True)
+    assert flow < 0.5 * ref, (ref, flow)
+    fp = oracle.face_penalty(oracle.filt(oracle.density_noise(n, 1, 4.0, dim=2), 1.5), 1, [1e4], dim=2)
+    ref, flow = iters(fp, False), iters(fp, True)
+    assert abs(flow - ref) <= 2, (ref, flow)
