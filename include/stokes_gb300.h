@@ -94,7 +94,8 @@ int stg_profile(stg_t* h, int enable); /* enabling also clears the counters */
 int stg_profile_read(stg_t* h, int cls, int64_t* launches, double* ms, double* bytes);
 const char* stg_profile_name(int cls);
 
-/* Fills *o with the defaults (PLAIN, tol 1e-8, 20 outer, 30 inner, 1e-4, 2 sweeps). */
+/* Fills *o with the defaults (PLAIN, tol 1e-8, 20 outer, 30 inner, 1e-4, 1 sweep per colour,
+   no warm start). */
 void stg_default_opts(stg_opts* o);
 
 /* Message of the last failure on this thread ("" if none). */
