@@ -5,14 +5,17 @@
 // framework's allocator budget, and latency-sensitive design loops that cannot afford
 // the device-wide synchronisation that cudaMalloc/cudaFree imply. They pass their own
 // device arrays for the design, the sensitivity and the result; the only scratch this
-// entry point needs (the per-block partial sums of the volume reduction) lives in the
-// fixed array below, which every GPU that loads this library holds until the process
-// exits.
+// entry point needs (the per-block partial sums of the volume reduction and a small
+// table of filter weight sums) lives in the fixed array below, which every GPU that
+// loads this library holds until the process exits.
 //
 // The bisection and the volume sums are the ones of stg_oc_update (same kernels'
 // arithmetic, same reduction grid and order), with the filter volume weights
 // vw_j = sum_i w_ij / W_i formed on the fly instead of being read from a buffer, so both
-// entry points return the same design and multiplier.
+// entry points return the same design and multiplier. W_i depends only on how far cell i
+// lies from each pair of domain faces (clamped at the filter radius R), so it is read
+// from a table of (R+1)^6 classes built once per call, in the summation order of the
+// handle's filter; a probe then costs (2R+1)^3 table reads per cell.
 #include <climits>
 #include <cmath>
 #include <mutex>
@@ -25,8 +28,13 @@ namespace {
 
 constexpr int TPB = 256;
 constexpr int OC_GRID = 1216;                 // reduction grid (8 x 152 SMs), as stg_oc_update
-constexpr int NOALLOC_SCRATCH = 2048;         // doubles: OC_GRID partials + the reduced sum
-constexpr long long NOALLOC_MAX_CELLS = 1ll << 30;  // largest design (1024^3 cells)
+constexpr int NOALLOC_MAX_N = 1024;           // largest design: 1024^3 cells
+constexpr int NOALLOC_MAX_R = 3;              // largest filter radius index: rmin <= 4
+constexpr int NOALLOC_CLASSES = 4096;         // (R+1)^6 weight-sum classes at R = 3
+constexpr int NOALLOC_TAB = 343;              // (2R+1)^3 filter weights at R = 3
+constexpr int SCR_SUM = OC_GRID;              // reduced volume
+constexpr int SCR_WCLASS = 1280;              // start of the class table (256-byte aligned)
+constexpr int NOALLOC_SCRATCH = SCR_WCLASS + NOALLOC_CLASSES;  // 5376 doubles = 42 KB
 
 // Scratch shared by every call on a device. Calls that overlap on the GPU race on it.
 static __device__ __align__(256) double g_noalloc_scratch[NOALLOC_SCRATCH];
@@ -53,33 +61,39 @@ int scratch_on_current_device(double** out) {
     return STG_OK;
 }
 
-// sum_j w_ij over the cells j of the domain within the hat radius of cell i
-__device__ __forceinline__ double hat_wsum(int n, double rmin, int R, int i0, int j0, int k0) {
-    double W = 0;
-    for (int a = -R; a <= R; a++)
-        for (int b = -R; b <= R; b++)
-            for (int c = -R; c <= R; c++) {
-                int ii = i0 + a, jj = j0 + b, kk = k0 + c;
-                if (ii < 0 || jj < 0 || kk < 0 || ii >= n || jj >= n || kk >= n) continue;
-                double w = rmin - sqrt((double)(a * a + b * b + c * c));
-                if (w > 0) W += w;
-            }
-    return W;
+// filter weights rmin - |o| for every offset o in [-R, R]^3, formed on the host with
+// IEEE sqrt exactly as the handle's filter table
+struct WTabNA {
+    double w[NOALLOC_TAB];
+};
+
+// one axis's class: (how far the cell may reach down, how far up), each clamped at R
+__device__ __forceinline__ int axis_class(int i, int n, int R) {
+    const int lo = min(i, R), hi = min(n - 1 - i, R);
+    return lo * (R + 1) + hi;
 }
 
-// vw_j = sum_i w_ij / W_i (column sum of the normalised filter)
-__device__ __forceinline__ double hat_vw(int n, double rmin, int R, int i, int j, int k) {
+// W for every class: sum of the positive weights over the offsets the class allows, in
+// the loop order of the handle's weight-sum kernel (a, then b, then c), so the sums are
+// bit-identical to the ones stg_oc_update reads
+__global__ void k_wsum_classes(int R, WTabNA T, double* __restrict__ wc) {
+    const int per = (R + 1) * (R + 1);
+    const int ncls = per * per * per;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ncls) return;
+    const int cz = t % per, cy = (t / per) % per, cx = t / (per * per);
+    const int xlo = cx / (R + 1), xhi = cx % (R + 1), ylo = cy / (R + 1), yhi = cy % (R + 1), zlo = cz / (R + 1),
+              zhi = cz % (R + 1);
+    const int D = 2 * R + 1;
     double s = 0;
     for (int a = -R; a <= R; a++)
         for (int b = -R; b <= R; b++)
             for (int c = -R; c <= R; c++) {
-                int ii = i + a, jj = j + b, kk = k + c;
-                if (ii < 0 || jj < 0 || kk < 0 || ii >= n || jj >= n || kk >= n) continue;
-                double w = rmin - sqrt((double)(a * a + b * b + c * c));
-                if (w <= 0) continue;
-                s += w * 1.0 / hat_wsum(n, rmin, R, ii, jj, kk);
+                if (a < -xlo || a > xhi || b < -ylo || b > yhi || c < -zlo || c > zhi) continue;
+                const double w = T.w[((a + R) * D + (b + R)) * D + (c + R)];
+                if (w > 0) s += w;
             }
-    return s;
+    wc[t] = s;
 }
 
 __device__ __forceinline__ double warp_sum(double v) {
@@ -87,20 +101,45 @@ __device__ __forceinline__ double warp_sum(double v) {
     return v;
 }
 
-// one bisection probe: x_new(lambda) and per-block partials of sum vw x_new (into scratch)
-__global__ void k_oc_noalloc(int n, double rmin, int R, const double* __restrict__ x, const double* __restrict__ dc,
-                             double lam, double move, double lo, double hi, double* __restrict__ xnew,
+// One bisection probe: x_new(lambda) and per-block partials of sum vw x_new (into
+// scratch). vw_j = sum_i w_ij / W_i, summed in the handle filter's transpose order. x and
+// xnew may be the same array (each element is read before it is written by one thread).
+__global__ void k_oc_noalloc(int n, int R, WTabNA T, const double* __restrict__ wclass_g, const double* x,
+                             const double* __restrict__ dc, double lam, double move, double lo, double hi, double* xnew,
                              double* __restrict__ part) {
     __shared__ double sh[TPB / 32];
+    __shared__ double wcls[NOALLOC_CLASSES];
+    const int per = (R + 1) * (R + 1);
+    const int ncls = per * per * per;
+    for (int c = threadIdx.x; c < ncls; c += TPB) wcls[c] = wclass_g[c];
+    __syncthreads();
+    const int D = 2 * R + 1;
     const long long nc = (long long)n * n * n;
     const double inv_n = 1.0 / (double)nc;
     double acc = 0;
     for (long long t = (long long)blockIdx.x * TPB + threadIdx.x; t < nc; t += (long long)gridDim.x * TPB) {
-        int k = (int)(t % n), j = (int)((t / n) % n), i = (int)(t / ((long long)n * n));
-        double vw = hat_vw(n, rmin, R, i, j, k);
-        double xi = x[t];
-        double dv = vw * inv_n;
-        double B = fmax(0.0, -dc[t]) / (dv * lam);
+        const int k = (int)(t % n), j = (int)((t / n) % n), i = (int)(t / ((long long)n * n));
+        double vw = 0;
+        for (int a = -R; a <= R; a++) {
+            const int ii = i + a;
+            if (ii < 0 || ii >= n) continue;
+            const int ca = axis_class(ii, n, R) * per * per;
+            for (int b = -R; b <= R; b++) {
+                const int jj = j + b;
+                if (jj < 0 || jj >= n) continue;
+                const int cb = ca + axis_class(jj, n, R) * per;
+                for (int c = -R; c <= R; c++) {
+                    const int kk = k + c;
+                    if (kk < 0 || kk >= n) continue;
+                    const double w = T.w[((a + R) * D + (b + R)) * D + (c + R)];
+                    if (w <= 0) continue;
+                    vw += w * 1.0 / wcls[cb + axis_class(kk, n, R)];
+                }
+            }
+        }
+        const double xi = x[t];
+        const double dv = vw * inv_n;
+        const double B = fmax(0.0, -dc[t]) / (dv * lam);
         double xn = xi * sqrt(B);
         xn = fmin(fmin(hi, xi + move), fmax(fmax(lo, xi - move), xn));
         if (xnew) xnew[t] = xn;
@@ -124,12 +163,16 @@ using namespace stg;
 
 extern "C" int stg_oc_update_noalloc(int n, double rmin, const double* d_x, const double* d_dc, double frac, double move,
                                      double lo, double hi, double* d_xnew, double* lambda_out, void* cuda_stream) {
-    if (n < 1 || (long long)n * n * n > NOALLOC_MAX_CELLS) {
-        set_error("stg_oc_update_noalloc: N = %d outside 1..1024 (design limited to %lld cells)", n, NOALLOC_MAX_CELLS);
+    if (n < 1 || n > NOALLOC_MAX_N) {
+        set_error("stg_oc_update_noalloc: N = %d outside 1..%d (designs of at most 1024^3 cells)", n, NOALLOC_MAX_N);
         return STG_E_INVALID;
     }
-    if (!d_x || !d_dc || !d_xnew || !(rmin > 0)) {
-        set_error("stg_oc_update_noalloc: null array or non-positive rmin");
+    if (!d_x || !d_dc || !d_xnew) {
+        set_error("stg_oc_update_noalloc: null device array");
+        return STG_E_INVALID;
+    }
+    if (!(rmin > 0) || !(rmin <= NOALLOC_MAX_R + 1)) {
+        set_error("stg_oc_update_noalloc: filter radius rmin = %g outside (0, %d]", rmin, NOALLOC_MAX_R + 1);
         return STG_E_INVALID;
     }
     double* scratch = nullptr;
@@ -137,17 +180,26 @@ extern "C" int stg_oc_update_noalloc(int n, double rmin, const double* d_x, cons
     cudaStream_t st = (cudaStream_t)cuda_stream;
     int R = (int)ceil(rmin) - 1;
     if (R < 0) R = 0;
+    const int D = 2 * R + 1;
+    WTabNA T{};
+    for (int a = -R; a <= R; a++)
+        for (int b = -R; b <= R; b++)
+            for (int c = -R; c <= R; c++) T.w[((a + R) * D + (b + R)) * D + (c + R)] = rmin - sqrt((double)(a * a + b * b + c * c));
     const long long nc = (long long)n * n * n;
     long long g = (nc + TPB - 1) / TPB;
     if (g > OC_GRID) g = OC_GRID;
     const int grid = (int)g;
-    double* part = scratch;                        // OC_GRID partials
-    double* sum = scratch + NOALLOC_SCRATCH - 1;   // reduced volume
+    double* part = scratch;                 // OC_GRID partials
+    double* sum = scratch + SCR_SUM;        // reduced volume
+    double* wclass = scratch + SCR_WCLASS;  // W per class
+    const int ncls = (R + 1) * (R + 1) * (R + 1) * (R + 1) * (R + 1) * (R + 1);
+    k_wsum_classes<<<(ncls + 127) / 128, 128, 0, st>>>(R, T, wclass);
+    STG_LAUNCH_CK();
     double l1 = 0.0, l2 = 1e9, lmid = 0.0, target = frac * (double)nc;
     int steps = 0;
     const double tol = 1e-9;
     auto volume = [&](double lam, double* vol) -> int {
-        k_oc_noalloc<<<grid, TPB, 0, st>>>(n, rmin, R, d_x, d_dc, lam, move, lo, hi, nullptr, part);
+        k_oc_noalloc<<<grid, TPB, 0, st>>>(n, R, T, wclass, d_x, d_dc, lam, move, lo, hi, nullptr, part);
         STG_LAUNCH_CK();
         STG_TRY(reduce_parts(st, part, grid, sum));
         STG_CK(cudaMemcpyAsync(vol, sum, sizeof(double), cudaMemcpyDeviceToHost, st));
@@ -173,7 +225,7 @@ extern "C" int stg_oc_update_noalloc(int n, double rmin, const double* d_x, cons
         steps++;
     }
     lmid = 0.5 * (l1 + l2);
-    k_oc_noalloc<<<grid, TPB, 0, st>>>(n, rmin, R, d_x, d_dc, lmid, move, lo, hi, d_xnew, part);
+    k_oc_noalloc<<<grid, TPB, 0, st>>>(n, R, T, wclass, d_x, d_dc, lmid, move, lo, hi, d_xnew, part);
     STG_LAUNCH_CK();
     STG_CK(cudaStreamSynchronize(st));
     if (lambda_out) *lambda_out = lmid;
