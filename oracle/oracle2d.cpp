@@ -1,5 +1,7 @@
-// CPU oracle for the 2D path (TEST INFRASTRUCTURE ONLY; parity unpinned for values,
-// like the 3D oracle: the reference ships no golden vectors).
+// CPU oracle for the 2D path (TEST INFRASTRUCTURE ONLY). Pinned, like the 3D oracle, to
+// golden vectors made by the reference's own 2D solver code run on the host
+// (oracle/ref_emu, tests/golden/make_ref_golden.py): operators, transfers, smoothers,
+// coarsest solve, V-cycle and GMRES agree bit for bit or to round-off.
 //
 // Restates, in the reference's own 8x8-blocked solver layout
 // [cells | x-faces | y-faces] (common_cpx/form01mapping.cu:10-57):

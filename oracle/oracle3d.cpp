@@ -70,12 +70,14 @@ void Descr::init(int n) {
 void Descr::finish() {
     for (int d = 0; d < 3; d++) {
         int off = g.face_off(d);
+#pragma omp parallel for
         for (int i = 0; i < g.face_size(d); i++) {
             int x, y, z;
             g.ind_face(i, d, x, y, z);
             if (!g.face_valid(x, y, z, d)) fixed[off + i] = 1;
         }
     }
+#pragma omp parallel for
     for (int i = 0; i < g.size(); i++)
         if (fixed[i]) { vol[i] = 0.0; penalty[i] = 0.0; }
 }
@@ -234,6 +236,7 @@ void apply_E(const Descr& ds, double* Ap, const double* p, Work& w) {
 template <class T, class F>
 static void down_sample(const G3& cg, const G3& fg, T* cv, const T* fv, F f) {
     // cells
+#pragma omp parallel for collapse(2)
     for (int z = 0; z < cg.nz; z++)
         for (int y = 0; y < cg.ny; y++)
             for (int x = 0; x < cg.nx; x++) {
@@ -246,6 +249,7 @@ static void down_sample(const G3& cg, const G3& fg, T* cv, const T* fv, F f) {
     for (int d = 0; d < 3; d++) {
         T* c = cv + cg.face_off(d);
         const T* fa = fv + fg.face_off(d);
+#pragma omp parallel for
         for (int i = 0; i < cg.face_size(d); i++) {
             int x, y, z;
             cg.ind_face(i, d, x, y, z);
@@ -321,6 +325,7 @@ void restrict_r(const Descr& c, const Descr& f, double* rc, const double* rf) {
         for (int k = 0; k < 8; k++) s += v[k];
         return s;
     });
+#pragma omp parallel for
     for (int i = 0; i < c.g.size(); i++)
         if (c.fixed[i]) rc[i] = 0.0;
 }
@@ -330,6 +335,7 @@ void restrict_r(const Descr& c, const Descr& f, double* rc, const double* rf) {
 void prolong(const Descr& c, const Descr& f, double* xf, const double* xc) {
     const G3 &fg = f.g, &cg = c.g;
     std::fill(xf, xf + fg.size(), 0.0);
+#pragma omp parallel for collapse(2)
     for (int z = 0; z < fg.nz; z++)
         for (int y = 0; y < fg.ny; y++)
             for (int x = 0; x < fg.nx; x++) xf[fg.cell_ind(x, y, z)] = xc[cg.cell_ind(x >> 1, y >> 1, z >> 1)];
@@ -337,10 +343,12 @@ void prolong(const Descr& c, const Descr& f, double* xf, const double* xc) {
         int ex = d == 0, ey = d == 1, ez = d == 2;
         double* fa = xf + fg.face_off(d);
         const double* ca = xc + cg.face_off(d);
+#pragma omp parallel for collapse(2)
         for (int z = 0; z < fg.nz + ez; z++)
             for (int y = 0; y < fg.ny + ey; y++)
                 for (int x = 0; x < fg.nx + ex; x++) fa[fg.face_ind(x, y, z, d)] = ca[cg.face_ind(x >> 1, y >> 1, z >> 1, d)];
     }
+#pragma omp parallel for
     for (int i = 0; i < fg.size(); i++)
         if (f.fixed[i]) xf[i] = 0.0;
 }
@@ -427,8 +435,10 @@ static void apply_B(const Descr& ds, int flag, double* y, const double* x, Work&
     std::vector<double> xm(n), ym(n);
     std::fill(y, y + n, 0.0);
     for (int face_flag = 0; face_flag < 2; face_flag++) {
+#pragma omp parallel for
         for (int i = 0; i < n; i++) xm[i] = stoke_mask(g, i, flag, face_flag) ? x[i] : 0.0;
         apply_A(ds, ym.data(), xm.data(), w);
+#pragma omp parallel for
         for (int i = 0; i < n; i++)
             if (stoke_mask(g, i, flag, face_flag)) y[i] += ym[i];
     }
@@ -438,11 +448,24 @@ static void apply_B(const Descr& ds, int flag, double* y, const double* x, Work&
 // DirectSolveBlockInverse<7>::update with LinearMappingToBlockMatrix<7,7>
 // (common_cpx/DirectSolveBlockInverse.cuh:116-132, BatchInverse.cuh:61-75): column l of
 // every block is read off B applied to the vector holding 1 at local DOF l of EVERY red block.
-void vanka_setup(const Descr& ds, int flag, Vanka& v, Work& w) {
+//
+// reorder_as_run: the reference packs the probe results into 7x7 blocks with
+// BlockMatrixReorderKernel (common_cpx/BatchInverse.cuh:13-47), one 32-thread warp per 32
+// blocks, staging 32 packed rows at a time in a two-chunk shared buffer. Its output
+// schedule (end = start + 7, minus one after the first chunk) writes output chunk 33 of
+// every warp after loading only row chunks 0-4, so entry (row 6, column 0) of the warp's
+// block 22 - packed row 7*22+6 = 160, loaded with chunk 5 - is read from the buffer slot
+// that still holds packed row 96 of chunk 3, i.e. entry (row 5, column 0) of block 13.
+// Executed in lockstep, as a warp does, this is deterministic; reorder_as_run reproduces
+// it, so that the oracle can be checked against the reference's own smoother as it runs.
+// Without it the oracle builds the blocks the reference intends (the exact restriction of
+// B), which is what the GPU solver's closed-form block solve implements.
+void vanka_setup(const Descr& ds, int flag, Vanka& v, Work& w, bool reorder_as_run) {
     const G3& g = ds.g;
     v.flag = flag;
     v.nb = g.cell_size() / 2;
     v.dofs.resize(v.nb * 7);
+#pragma omp parallel for
     for (int t = 0; t < v.nb; t++)
         for (int l = 0; l < 7; l++) v.dofs[t * 7 + l] = block_dof(g, t, l, flag);
     v.lu.assign(v.nb * 49, 0.0);
@@ -451,11 +474,15 @@ void vanka_setup(const Descr& ds, int flag, Vanka& v, Work& w) {
     std::vector<double> s(n), y(n), tmp;
     for (int l = 0; l < 7; l++) {
         std::fill(s.begin(), s.end(), 0.0);
+#pragma omp parallel for
         for (int t = 0; t < v.nb; t++) s[v.dofs[t * 7 + l]] = 1.0;
         apply_B(ds, flag, y.data(), s.data(), w, tmp);
+#pragma omp parallel for
         for (int t = 0; t < v.nb; t++)
             for (int m = 0; m < 7; m++) v.lu[t * 49 + l * 7 + m] = y[v.dofs[t * 7 + m]];
     }
+    if (reorder_as_run)
+        for (int t = 22; t < v.nb; t += 32) v.lu[t * 49 + 0 * 7 + 6] = v.lu[(t - 9) * 49 + 0 * 7 + 5];
 #pragma omp parallel for
     for (int t = 0; t < v.nb; t++) lu_factor(&v.lu[t * 49], &v.piv[t * 7], 7, 7);
 }
@@ -480,9 +507,11 @@ void descent_smoother(const Descr& ds, const Vanka* P[2], const int iters[2], do
     for (int i = 0; i < 2; i++)
         for (int j = 0; j < iters[i]; j++) {
             vanka_apply(*P[i], n, d.data(), r.data());
+#pragma omp parallel for
             for (int q = 0; q < n; q++) out[q] += d[q];
             if (i == 1 && j == iters[i] - 1) break;
             apply_A(ds, Ad.data(), d.data(), w);
+#pragma omp parallel for
             for (int q = 0; q < n; q++) r[q] -= Ad[q];
         }
 }
@@ -613,14 +642,14 @@ void hierarchy_init(Hierarchy& H, int n) {
 
 // FluidSteadyState3D::solve set-up half (stoke/FluidSteadyState3D.cpp:152-156):
 // coarse descriptors, smoother blocks, coarsest LU.
-void hierarchy_update(Hierarchy& H, bool flow) {
+void hierarchy_update(Hierarchy& H, bool flow, bool reorder_as_run) {
     for (int i = H.l - 2; i >= 0; i--) {
         update_subsystem(H.lv[i], H.lv[i + 1]);
         if (flow) flow_penalties(H.lv[i], H.lv[i + 1]);
     }
     for (int i = 1; i < H.l; i++) {
-        vanka_setup(H.lv[i], 0, H.red[i], H.w);
-        vanka_setup(H.lv[i], 1, H.black[i], H.w);
+        vanka_setup(H.lv[i], 0, H.red[i], H.w, reorder_as_run);
+        vanka_setup(H.lv[i], 1, H.black[i], H.w, reorder_as_run);
     }
     dense_setup(H.lv[0], H.closed, H.dense, H.w);
 }
@@ -640,6 +669,7 @@ void vcycle(Hierarchy& H) {
             dense_apply(H.dense, p.data(), r.data());
         }
         apply_A(H.lv[i], Ap.data(), p.data(), H.w);
+#pragma omp parallel for
         for (int q = 0; q < n; q++) { x[q] += p[q]; r[q] -= Ap[q]; }
         if (i != 0) {
             restrict_r(H.lv[i - 1], H.lv[i], H.r[i - 1].data(), r.data());
@@ -652,7 +682,8 @@ void vcycle(Hierarchy& H) {
         if (i != 0) {
             prolong(H.lv[i - 1], H.lv[i], p.data(), H.x[i - 1].data());
             apply_A(H.lv[i], Ap.data(), p.data(), H.w);
-            for (int q = 0; q < n; q++) { x[q] += p[q]; r[q] -= Ap[q]; }
+    #pragma omp parallel for
+        for (int q = 0; q < n; q++) { x[q] += p[q]; r[q] -= Ap[q]; }
         }
         std::fill(p.begin(), p.end(), 0.0);
         if (i > 0) {
@@ -660,6 +691,7 @@ void vcycle(Hierarchy& H) {
             descent_smoother(H.lv[i], P, iters, p.data(), r.data(), H.w);
         }
         apply_A(H.lv[i], Ap.data(), p.data(), H.w);
+#pragma omp parallel for
         for (int q = 0; q < n; q++) { x[q] += p[q]; r[q] -= Ap[q]; }
     }
 }

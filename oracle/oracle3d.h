@@ -5,11 +5,14 @@
 // the timed CPU baseline of bench.py. The product (libstokes_gb300.so) never
 // links, loads or calls it.
 //
-// Parity status: the blocked layout index math is pinned against the reference's
-// own compiled host functions (oracle/ref_build.sh -> oracle/_ref). The operator
-// values, the smoother, the coarse solve and the Krylov loop have no golden vectors
-// in the reference (it ships no tests) and are therefore "parity unpinned": they are
-// checked by construction against the reference source, cited per function.
+// Parity status: pinned. The blocked layout index math is checked against the
+// reference's own compiled host functions, and every value this oracle computes (the
+// descriptors of every level, A, E, restriction, prolongation, the Vanka block solves,
+// the composite smoothers, the coarsest dense solve, the V-cycle and the GMRES solve)
+// against golden vectors produced by the reference's own CUDA solver code, run on the
+// host through oracle/ref_emu (tests/golden/make_ref_golden.py, tests/test_ref_golden_cpu.py).
+// The reference's Vanka block packing misplaces one block entry in 32; vanka_setup's
+// reorder_as_run reproduces that, the default builds the intended blocks.
 #pragma once
 #include <cstdint>
 #include <vector>
@@ -95,16 +98,17 @@ void apply_E(const Descr& ds, double* Ap, const double* p, Work& w);
 void update_subsystem(Descr& c, const Descr& f);
 void restrict_r(const Descr& c, const Descr& f, double* rc, const double* rf);
 void prolong(const Descr& c, const Descr& f, double* xf, const double* xc);
-void vanka_setup(const Descr& ds, int flag, Vanka& v, Work& w);
+void vanka_setup(const Descr& ds, int flag, Vanka& v, Work& w, bool reorder_as_run = false);
 void vanka_apply(const Vanka& v, int n, double* out, const double* r);
 void descent_smoother(const Descr& ds, const Vanka* P[2], const int iters[2], double* out, const double* r_in, Work& w);
 void dense_setup(const Descr& ds, bool closed, Dense& D, Work& w);
 void dense_apply(const Dense& D, double* out, const double* r);
 int level_count(int n);
 void hierarchy_init(Hierarchy& H, int n);
-// flow: the GPU solver's coarse penalties (8 x the smallest free child) instead of the sums
+// flow: the GPU solver's coarse penalties (8 x the smallest free child) instead of the sums;
+// reorder_as_run: the Vanka blocks as the reference's block packing produces them (vanka_setup)
 void flow_penalties(Descr& c, const Descr& f);
-void hierarchy_update(Hierarchy& H, bool flow = false);
+void hierarchy_update(Hierarchy& H, bool flow = false, bool reorder_as_run = false);
 void vcycle(Hierarchy& H);
 void mg_apply(Hierarchy& H, double* out, const double* in);
 void gmres_solve(Hierarchy& H, const double* b, double* x, int max_iter, double abs_thres, double rel_thres,

@@ -154,6 +154,8 @@ void orc3_set_b_blocked(void* p, const double* b) {
 void orc3_setup(void* p) { hierarchy_update(((Handle*)p)->H); }
 // The same with the GPU solver's coarse penalties (not the reference's).
 void orc3_setup_flow(void* p) { hierarchy_update(((Handle*)p)->H, true); }
+// The reference's set-up with its Vanka blocks as its block packing leaves them.
+void orc3_setup_as_run(void* p) { hierarchy_update(((Handle*)p)->H, false, true); }
 
 // GMRES::Solve with the reference thresholds passed in (common_cpx/GMRES.cpp:20-110).
 // stats = {iters, restarts, rel_true, abs_true, precond_res, seconds}

@@ -49,7 +49,7 @@ def lib():
         L.orc3_coarse_info.restype = I
         L.orc3_coarse_info.argtypes = [P]
         for name in ["orc3_init_boundary", "orc3_update_penalty", "orc3_update_b", "orc3_set_b_blocked", "orc3_setup",
-                     "orc3_setup_flow",
+                     "orc3_setup_flow", "orc3_setup_as_run",
                      "orc3_apply_A", "orc3_apply_E", "orc3_level_descr", "orc3_update_subsystems", "orc3_restrict",
                      "orc3_prolong", "orc3_vanka_apply", "orc3_smooth", "orc3_coarse_apply", "orc3_vcycle"]:
             getattr(L, name).restype = None
@@ -59,6 +59,7 @@ def lib():
         L.orc3_set_b_blocked.argtypes = [P, DP]
         L.orc3_setup.argtypes = [P]
         L.orc3_setup_flow.argtypes = [P]
+        L.orc3_setup_as_run.argtypes = [P]
         L.orc3_apply_A.argtypes = [P, I, DP, DP]
         L.orc3_apply_E.argtypes = [P, DP, DP]
         L.orc3_level_descr.argtypes = [P, I, DP, DP, U8P]
@@ -254,10 +255,14 @@ class Steady3D:
     def set_b_blocked(self, b):
         self.L.orc3_set_b_blocked(self.h, dp(np.ascontiguousarray(b, dtype=np.float64)))
 
-    def setup(self, flow=False):
+    def setup(self, flow=False, as_run=False):
         """The hierarchy set-up; flow=True builds the GPU solver's coarse penalties (8 x the
-        smallest free child) instead of the reference's sums."""
-        (self.L.orc3_setup_flow if flow else self.L.orc3_setup)(self.h)
+        smallest free child) instead of the reference's sums; as_run=True builds the Vanka
+        blocks as the reference's block packing leaves them (oracle3d.cpp vanka_setup)."""
+        if as_run:
+            self.L.orc3_setup_as_run(self.h)
+        else:
+            (self.L.orc3_setup_flow if flow else self.L.orc3_setup)(self.h)
 
     def solve(self, max_iter=50, abs_thr=1e-3, rel_thr=1e-4, norm_thr=1e-3, restarts=0, true_tol=0.0):
         x = np.zeros(self.level_dof(self.levels - 1))

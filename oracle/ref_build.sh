@@ -1,11 +1,12 @@
 #!/usr/bin/env bash
 # Builds the checker pieces of the reference from its own sources (where they lie under
-# the reference checkout) into oracle/_ref/. Only host-callable code is used: the
-# reference's CUDA kernels need a GPU and its solver classes need the GPU runtime, so
-# the rest of the reference path is not buildable as a CPU checker.
-#   usage: oracle/ref_build.sh [REFERENCE_ROOT]   (default: /root/reference)
+# the reference checkout) into oracle/_ref/: its grid index code, its MMA solver, and
+# its CUDA solver path run on the host through oracle/ref_emu (a CUDA runtime, cuBLAS and
+# cuSOLVER stand-in that executes the reference kernels on the CPU).
+#   usage: oracle/ref_build.sh [REFERENCE_ROOT]
+#   (default: $STOKES_TO_REFERENCE, else the checkout this build container mounts)
 set -euo pipefail
-REF="${1:-/root/reference}"
+REF="${1:-${STOKES_TO_REFERENCE:-/root/reference}}"
 HERE="$(cd "$(dirname "$0")" && pwd)"
 OUT="$HERE/_ref"
 CC_DIR="$REF/simplex/src/common_cpx"
@@ -27,3 +28,5 @@ MMA_DIR="$REF/simplex/ext/mma"
 "${CXX:-g++}" -std=c++14 -O2 -fPIC -shared -w -I "$MMA_DIR" "$HERE/ref_mma_wrap.cpp" "$MMA_DIR/MMASolver.cpp" \
   -o "$OUT/libref_mma.so"
 echo "built $OUT/libref_mma.so"
+# the reference's CUDA solver path (3D and 2D), run on the host through the CUDA stand-in
+"${PYTHON:-python3}" "$HERE/ref_emu/build.py" "$REF"

@@ -44,3 +44,15 @@ def relerr(a, b):
 def pressure_free(p):
     """Pressure modulo a constant (the closed-domain null space)."""
     return p - p.mean()
+
+
+def stable_vec(seed, n):
+    """n values in [-1, 1) from SplitMix64 over (seed, index): a generator whose stream
+    never changes, so fixtures can store the seed instead of the vector."""
+    with np.errstate(over="ignore"):
+        z = np.uint64(seed) * np.uint64(0x9E3779B97F4A7C15) + np.arange(n, dtype=np.uint64) + np.uint64(
+            0x632BE59BD9B4E019)
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        z = z ^ (z >> np.uint64(31))
+    return (z >> np.uint64(11)).astype(np.float64) * (2.0 / 9007199254740992.0) - 1.0
