@@ -165,46 +165,57 @@ __global__ void k2_apply(G2d g, Coef2<T> C, T lap, const T* __restrict__ v, cons
 }
 
 // ------------------------------------------------------------------ smoother colour
-// BlockInverse (stoke/StokeFlowSmoothing.cu:48-73)
-__device__ __forceinline__ void lap2x2inv(float* y, const float* x, float a, float b, float f) {
-    float s = 1.f / (a * b - f * f);
-    y[0] = (b * x[0] + f * x[1]) * s;
-    y[1] = (f * x[0] + a * x[1]) * s;
-}
+// One colour of the 2D box smoother (the operator of stoke/StokeFlowSmoothing.cu:74-140):
+// every cell of the colour solves for its 5 unknowns - the x-faces a (low) and b (high),
+// the y-faces c (low) and d (high), the pressure p - with the box matrix
+//
+//     | K    g  |  | u |   | r_u |       K = diag(K_x, K_y),  K_x = | 4L+P_a   -s_x |
+//     | g^T  P_p|  | p | = | r_p |                                  | -s_x   4L+P_b |
+//
+// where L is the level's Laplacian coefficient, s_x = L unless face a or b is fixed (0
+// then), K_y likewise, and g = (-vol_a, vol_b, -vol_c, vol_d) holds the divergence
+// weights. Block elimination: z = K^-1 r_u, w = K^-1 g, p = (r_p - g.z) / (P_p - g.w),
+// u = z - p w; a fixed cell keeps p = 0. Each 2x2 block of K is inverted once and applied
+// to both right-hand sides.
+struct SymInv2 {
+    float i00, i01, i11;  // inverse of [[d0, -s], [-s, d1]]
+    __device__ __forceinline__ SymInv2(float d0, float d1, float s) {
+        const float rdet = 1.f / (d0 * d1 - s * s);
+        i00 = d1 * rdet;
+        i11 = d0 * rdet;
+        i01 = s * rdet;
+    }
+    __device__ __forceinline__ void apply(float v0, float v1, float& o0, float& o1) const {
+        o0 = i00 * v0 + i01 * v1;
+        o1 = i01 * v0 + i11 * v1;
+    }
+};
 
 __global__ void k2_smooth(G2d g, Coef2<float> C, float lap, int flag, const float* __restrict__ r, float* __restrict__ dout) {
-    int c = blockIdx.x * TPB + threadIdx.x;
+    const int c = blockIdx.x * TPB + threadIdx.x;
     if (c >= g.nc()) return;
-    int x = (c / 64 % (g.n >> 3)) * 8 + (c & 7), y = (c / 64 / (g.n >> 3)) * 8 + ((c >> 3) & 7);
+    const int x = (c / 64 % (g.n >> 3)) * 8 + (c & 7), y = (c / 64 / (g.n >> 3)) * 8 + ((c >> 3) & 7);
     if ((((x & 1) ^ (y & 1) ^ flag)) != 0) return;
-    const int ind[5] = {g.face(x, y, 0), g.face(x + 1, y, 0), g.face(x, y, 1), g.face(x, y + 1, 1), g.cell(x, y)};
-    float lr[5], pen[5], div[4];
-    bool fx[5];
-    for (int q = 0; q < 5; q++) {
-        lr[q] = r[ind[q]];
-        pen[q] = C.pen[ind[q]];
-        fx[q] = C.fixed[ind[q]];
-    }
-    div[0] = -C.vol[ind[0]];
-    div[1] = C.vol[ind[1]];
-    div[2] = -C.vol[ind[2]];
-    div[3] = C.vol[ind[3]];
-    float f[2], vd[4], temp[4], xl[5], yv[4], pd = 0.f;
-    f[0] = (fx[0] || fx[1]) ? 0.f : lap;
-    f[1] = (fx[2] || fx[3]) ? 0.f : lap;
-    for (int i = 0; i < 4; i++) vd[i] = 4.f * lap + pen[i];
-    lap2x2inv(temp, div, vd[0], vd[1], f[0]);
-    lap2x2inv(temp + 2, div + 2, vd[2], vd[3], f[1]);
-    for (int i = 0; i < 4; i++) xl[i] = lr[i];
-    xl[4] = lr[4];
-    for (int i = 0; i < 4; i++) xl[4] -= temp[i] * lr[i];
-    lap2x2inv(yv, xl, vd[0], vd[1], f[0]);
-    lap2x2inv(yv + 2, xl + 2, vd[2], vd[3], f[1]);
-    for (int i = 0; i < 4; i++) pd += temp[i] * div[i];
-    pd = -pd + pen[4];
-    xl[4] = fx[4] ? 0.f : xl[4] / pd;
-    for (int i = 0; i < 4; i++) dout[ind[i]] = yv[i] - xl[4] * temp[i];
-    dout[ind[4]] = xl[4];
+    const int fa = g.face(x, y, 0), fb = g.face(x + 1, y, 0), fc = g.face(x, y, 1), fd = g.face(x, y + 1, 1);
+    const int cp = g.cell(x, y);
+    const float sx = (C.fixed[fa] || C.fixed[fb]) ? 0.f : lap;
+    const float sy = (C.fixed[fc] || C.fixed[fd]) ? 0.f : lap;
+    const SymInv2 Kx(4.f * lap + C.pen[fa], 4.f * lap + C.pen[fb], sx);
+    const SymInv2 Ky(4.f * lap + C.pen[fc], 4.f * lap + C.pen[fd], sy);
+    const float ga = -C.vol[fa], gb = C.vol[fb], gc = -C.vol[fc], gd = C.vol[fd];
+    float za, zb, zc, zd, wa, wb, wc, wd;
+    Kx.apply(r[fa], r[fb], za, zb);
+    Ky.apply(r[fc], r[fd], zc, zd);
+    Kx.apply(ga, gb, wa, wb);
+    Ky.apply(gc, gd, wc, wd);
+    const float schur = C.pen[cp] - (ga * wa + gb * wb + gc * wc + gd * wd);
+    const float rhs_p = r[cp] - (ga * za + gb * zb + gc * zc + gd * zd);
+    const float p = C.fixed[cp] ? 0.f : rhs_p / schur;
+    dout[fa] = za - p * wa;
+    dout[fb] = zb - p * wb;
+    dout[fc] = zc - p * wc;
+    dout[fd] = zd - p * wd;
+    dout[cp] = p;
 }
 
 // ------------------------------------------------------------------ transfers and coarsening
