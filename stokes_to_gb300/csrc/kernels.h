@@ -151,6 +151,10 @@ int sensitivity(cudaStream_t st, const Geom& g, const double* rho, const stg_alp
 int density_filter(cudaStream_t st, int dim, int n, double rmin, const double* in, double* out, int transpose, double* W);
 int oc_volume(cudaStream_t st, int ncell, const double* x, const double* dc, const double* vw, double lam, double move,
               double lo, double hi, double* xnew, double* parts, int* nparts);
+// The whole OC update (bracket, bisection, x_new) in one cooperative launch; parts: two
+// buffers of up to 1216 block partials; lambda_out: one device double.
+int oc_update_device(cudaStream_t st, int ncell, const double* x, const double* dc, const double* vw, double frac,
+                     double move, double lo, double hi, double* xnew, double* parts, double* lambda_out);
 int density_noise(cudaStream_t st, int dim, int n, uint64_t seed, const double* w, int R, double* out, double* tmp);
 
 }  // namespace stg

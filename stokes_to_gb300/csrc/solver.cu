@@ -1215,39 +1215,15 @@ int stg_oc_update(stg_t* h, double rmin, const double* x, const double* dc, doub
         STG_CK(cudaMemcpyAsync(h->d_sens, dc, sizeof(double) * h->ncell, cudaMemcpyHostToDevice, h->st));
         ddc = h->d_sens;
     }
-    double l1 = 0.0, l2 = 1e9, lmid = 0.0, target = frac * nc;
-    int steps = 0, np = 0;
-    const double tol = 1e-9;
-    auto volume = [&](double lam, double* vol) -> int {
-        STG_TRY(oc_volume(h->st, nc, h->d_design, ddc, h->d_vw, lam, move, lo, hi, nullptr, h->d_parts, &np));
-        STG_TRY(reduce_parts(h->st, h->d_parts, np, h->dnrm));
-        STG_CK(cudaMemcpyAsync(vol, h->dnrm, sizeof(double), cudaMemcpyDeviceToHost, h->st));
-        STG_CK(cudaStreamSynchronize(h->st));
-        return STG_OK;
-    };
     // the multiplier grows with the sensitivities (with the objective, i.e. with the grid:
-    // above 1e9 at 512^3): widen the bracket by decades until its upper end undershoots
-    for (int k = 0; k < 60; k++) {
-        double vol = 0;
-        STG_TRY(volume(l2, &vol));
-        if (vol <= target) break;
-        l1 = l2;
-        l2 *= 10.0;
-    }
-    while ((l2 - l1) > tol * (l1 + l2) && steps < 200) {
-        lmid = 0.5 * (l1 + l2);
-        double vol = 0;
-        STG_TRY(volume(lmid, &vol));
-        if (vol > target)
-            l1 = lmid;
-        else
-            l2 = lmid;
-        steps++;
-    }
-    lmid = 0.5 * (l1 + l2);
-    STG_TRY(oc_volume(h->st, nc, h->d_design, ddc, h->d_vw, lmid, move, lo, hi, h->d_tmp, h->d_parts, &np));
+    // above 1e9 at 512^3): the bracket is widened by decades until its upper end
+    // undershoots, then bisected - all of it in one cooperative launch, with no host
+    // round trip per multiplier step
+    STG_TRY(oc_update_device(h->st, nc, h->d_design, ddc, h->d_vw, frac, move, lo, hi, h->d_tmp, h->d_parts, h->dnrm));
     STG_CK(cudaMemcpyAsync(h->d_design, h->d_tmp, sizeof(double) * h->ncell, cudaMemcpyDeviceToDevice, h->st));
     if (x_new) STG_CK(cudaMemcpyAsync(x_new, h->d_design, sizeof(double) * h->ncell, cudaMemcpyDeviceToHost, h->st));
+    double lmid = 0;
+    STG_CK(cudaMemcpyAsync(&lmid, h->dnrm, sizeof(double), cudaMemcpyDeviceToHost, h->st));
     STG_CK(cudaStreamSynchronize(h->st));
     if (lambda_out) *lambda_out = lmid;
     return STG_OK;
@@ -1430,7 +1406,8 @@ int stg_apply_op_device(stg_t* h, int op, int level, double* d_out, const double
             if (level != 0) break;
             STG_TRY(blocked_to_slots64(h->st, L.g, d_in, L.t0));
             STG_TRY(dense_apply64(h->st, h->dense, L.g, L.t0, L.t1));
-            STG_TRY(slots_to_blocked64(h->st, L.g, L.t1, d_out, nullptr));
+            // padding entries of the reference layout are fixed identity rows of its matrix
+            STG_TRY(slots_to_blocked64(h->st, L.g, L.t1, d_out, d_in));
             STG_CK(cudaStreamSynchronize(h->st));
             return STG_OK;
         }

@@ -3,6 +3,7 @@
 // optimality-criteria volume pass and the seeded density generator.
 //
 // Cell arrays are in the simplex Field order: (i*N + j)*N + k in 3D, i*N + j in 2D.
+#include <cooperative_groups.h>
 #include <math.h>
 
 #include "alpha.cuh"
@@ -175,6 +176,97 @@ __global__ void k_blur(int n, long long nc, long long stride, const double* __re
     out[t] = clip ? fmin(1.0, fmax(0.0, acc)) : acc;
 }
 
+
+// x_new(lambda) of the OC update for the cells of this thread (grid-stride, as k_oc) and
+// the block's part of the filtered volume sum_j vw_j x_new_j.
+__device__ __forceinline__ double oc_block_volume(int ncell, const double* __restrict__ x, const double* __restrict__ dc,
+                                                  const double* __restrict__ vw, double lam, double move, double lo,
+                                                  double hi, double* __restrict__ xnew, double* sh) {
+    double acc = 0;
+    const double inv_n = 1.0 / ncell;
+    for (long long t = (long long)blockIdx.x * TPB + threadIdx.x; t < ncell; t += (long long)gridDim.x * TPB) {
+        const double xi = x[t];
+        const double dv = vw[t] * inv_n;
+        const double B = fmax(0.0, -dc[t]) / (dv * lam);
+        double xn = xi * sqrt(B);
+        xn = fmin(fmin(hi, xi + move), fmax(fmax(lo, xi - move), xn));
+        if (xnew) xnew[t] = xn;
+        acc += vw[t] * xn;
+    }
+    acc = warp_sum(acc);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    double r = 0;
+    if (threadIdx.x == 0)
+        for (int w = 0; w < TPB / 32; w++) r += sh[w];
+    __syncthreads();
+    return r;  // valid in thread 0
+}
+
+// Sum of the block partials in the order of the partial reduction kernel (threads stride
+// over the parts, warp tree, warps in order), formed by every block alike so that all
+// blocks take the same bisection decision.
+__device__ __forceinline__ double oc_reduce(const double* part, int nparts, double* sh) {
+    double s = 0;
+    for (int p = threadIdx.x; p < nparts; p += TPB) s += part[p];
+    s = warp_sum(s);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double r = 0;
+        for (int w = 0; w < TPB / 32; w++) r += sh[w];
+        sh[TPB / 32] = r;
+    }
+    __syncthreads();
+    const double r = sh[TPB / 32];
+    __syncthreads();
+    return r;
+}
+
+// The whole OC update in one cooperative launch: the multiplier bracket [0, 1e9] widened
+// by decades while its upper end still overshoots the volume, then bisection to relative
+// width 1e-9 (at most 200 steps), then x_new at the midpoint. One grid-wide barrier per
+// probe; the partials alternate between two buffers so a probe never overwrites the ones
+// the previous probe's reduction still reads.
+__global__ void __launch_bounds__(TPB) k_oc_bisect(int ncell, const double* __restrict__ x, const double* __restrict__ dc,
+                                                   const double* __restrict__ vw, double target, double move, double lo,
+                                                   double hi, double* __restrict__ xnew, double* __restrict__ part,
+                                                   double* __restrict__ lambda_out) {
+    namespace cg = cooperative_groups;
+    cg::grid_group grid = cg::this_grid();
+    __shared__ double sh[TPB / 32 + 1];
+    const int nparts = gridDim.x;
+    int buf = 0;
+    auto volume = [&](double lam) {
+        const double b = oc_block_volume(ncell, x, dc, vw, lam, move, lo, hi, nullptr, sh);
+        double* pp = part + buf * nparts;
+        if (threadIdx.x == 0) pp[blockIdx.x] = b;
+        grid.sync();
+        const double v = oc_reduce(pp, nparts, sh);
+        buf ^= 1;
+        return v;
+    };
+    double l1 = 0.0, l2 = 1e9;
+    for (int k = 0; k < 60; k++) {
+        if (volume(l2) <= target) break;
+        l1 = l2;
+        l2 *= 10.0;
+    }
+    const double tol = 1e-9;
+    int steps = 0;
+    while ((l2 - l1) > tol * (l1 + l2) && steps < 200) {
+        const double lmid = 0.5 * (l1 + l2);
+        if (volume(lmid) > target)
+            l1 = lmid;
+        else
+            l2 = lmid;
+        steps++;
+    }
+    const double lmid = 0.5 * (l1 + l2);
+    oc_block_volume(ncell, x, dc, vw, lmid, move, lo, hi, xnew, sh);
+    if (blockIdx.x == 0 && threadIdx.x == 0) *lambda_out = lmid;
+}
+
 }  // namespace
 
 int face_penalty_from_density(cudaStream_t st, const Geom& g, const double* rho, const stg_alpha& law, const uint8_t* m,
@@ -226,6 +318,27 @@ int oc_volume(cudaStream_t st, int ncell, const double* x, const double* dc, con
     *nparts = (int)g;
     k_oc<<<(unsigned)g, TPB, 0, st>>>(ncell, x, dc, vw, lam, move, lo, hi, xnew, parts);
     STG_LAUNCH_CK();
+    return STG_OK;
+}
+
+int oc_update_device(cudaStream_t st, int ncell, const double* x, const double* dc, const double* vw, double frac,
+                     double move, double lo, double hi, double* xnew, double* parts, double* lambda_out) {
+    // the grid of the probe kernel (k_oc), capped at what can be co-resident
+    long long g = (ncell + TPB - 1) / TPB;
+    if (g > 1216) g = 1216;
+    if (g < 1) g = 1;
+    int dev = 0, sms = 0, per_sm = 0;
+    STG_CK(cudaGetDevice(&dev));
+    STG_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    STG_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_oc_bisect, TPB, 0));
+    if (per_sm < 1) {
+        set_error("the OC bisection kernel cannot be made resident");
+        return STG_E_CUDA;
+    }
+    if (g > (long long)sms * per_sm) g = (long long)sms * per_sm;
+    double target = frac * ncell;
+    void* args[] = {&ncell, &x, &dc, &vw, &target, &move, &lo, &hi, &xnew, &parts, &lambda_out};
+    STG_CK(cudaLaunchCooperativeKernel((const void*)k_oc_bisect, dim3((unsigned)g), dim3(TPB), args, 0, st));
     return STG_OK;
 }
 
