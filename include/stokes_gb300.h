@@ -64,6 +64,12 @@ typedef struct stg_opts {
                             equation (the forward one for stg_solve, the adjoint one for
                             stg_adjoint_sensitivity) instead of zero, unless its residual
                             exceeds ||b|| (then zero); 0 (default): zero, as the reference */
+    int prolong;         /* coarse-correction transfer of the 3D solver's uniform-form V-cycle:
+                            0 the reference's piecewise-constant injection
+                            (StokeFlowUpSample3D); 1 face velocities interpolated - linearly
+                            along the face normal, 3/4 : 1/4 between the two nearest coarse
+                            faces along each tangent - and pressures injected. The
+                            LinearMapping adapters always inject. */
 } stg_opts;
 
 typedef struct stg_stats {
@@ -127,11 +133,14 @@ int64_t stg_level_dof(const stg_t* h, int level);
 /* FluidSteadyState3D::init_boundary(cell_vol, cell_fixed, face_vol, face_fixed, closed)
  * (stoke/FluidSteadyState3D.cpp:92-114) together with FluidEnergy3D::init_boundary
  * (fluid_topo/FluidEnergy3D.cpp:33-54); 2D: FluidSteadyState::init_boundary
- * (stoke/FluidSteadyState.cpp:87-108). face_* point to dim arrays. In 3D, returns
- * STG_E_UNSUPPORTED when the free faces do not share one vol value or a cell is
- * fixed (the 3D smoother is the uniform-coefficient one); when in addition every face
- * on the domain boundary is fixed, as in every reference test, the 3D kernels use the
- * 7-point Laplacian form of the operator (same matrix). 2D takes any vol and fixed cells. */
+ * (stoke/FluidSteadyState.cpp:87-108). face_* point to dim arrays. Any vol and fixed
+ * flags are accepted. In 3D, when the free faces share one vol value and no cell is
+ * fixed, the solver uses its uniform-coefficient form (closed-form Vanka blocks, FP32
+ * V-cycle; with every face on the domain boundary fixed, as in every reference test, the
+ * 7-point Laplacian form of the same matrix); otherwise the general-coefficient form
+ * (per-face vols, Vanka blocks probed and LU-factored like the reference's, FP64
+ * V-cycle), which STG_METHOD_LEARNED does not support. With fixed cells the reference's
+ * own coarsest matrix is singular; this library adds the fixed cells' identity rows. */
 int stg_set_boundary(stg_t* h, const double* cell_vol, const int32_t* cell_fixed, const double* const* face_vol,
                      const int32_t* const* face_fixed, int closed);
 

@@ -20,7 +20,7 @@ NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall", "--expt-relaxed-constexpr",
             "-I", os.path.join(ROOT, "include")]
-SOURCES = ["kernels.cu", "sweep.cu", "blas.cu", "dense.cu", "topo.cu", "solver.cu", "solver2d.cu", "mma.cu", "noalloc.cu",
+SOURCES = ["kernels.cu", "sweep.cu", "blas.cu", "dense.cu", "topo.cu", "solver.cu", "solver2d.cu", "mma.cu", "noalloc.cu", "general.cu",
            "unet_kernels.cu", "unet.cu"]
 
 

@@ -22,6 +22,13 @@ struct Level {
     __nv_bfloat16* xbf = nullptr;
     __half* P16 = nullptr;    // FP16 copy of P32 / its scale for the solver's own sweeps (set-up)
     d4 *t0 = nullptr, *t1 = nullptr;  // FP64 adapter buffers (allocated on first use)
+    // general-coefficient form (general.cu; allocated on first use): per-slot vols {cell,
+    // x-, y-, z-face}, the FP64 V-cycle's r, x, p, A p, and the LU-factored Vanka blocks of
+    // each colour (49 doubles and 7 pivots per cell of the colour)
+    d4* V64 = nullptr;
+    d4 *gr = nullptr, *gx = nullptr, *gp = nullptr, *gAp = nullptr;
+    double* vblk[2] = {nullptr, nullptr};
+    int8_t* vpiv[2] = {nullptr, nullptr};
     float4* x() { return cur ? xb : xa; }
     float4* other() { return cur ? xa : xb; }
 };
@@ -75,6 +82,10 @@ struct stg_ctx {
     // lap_ok: the boundary admits the Laplacian form; general: force the masked general
     // stencil (set while an adapter works on a vector that is nonzero on fixed unknowns)
     bool lap_ok = false, general = false, reference_cycle = false;
+    // gen: the boundary has non-uniform face vols or fixed cells, so the solver and the
+    // adapters run the general-coefficient form (general.cu); gtmp: its finest-size scratch
+    bool gen = false;
+    stg::d4* gtmp[3] = {nullptr, nullptr, nullptr};
     // the coarse levels hold the solver's own penalties (flow rule of kernels.cu k_coarsen)
     // rather than the reference's sums, which the component adapters reproduce
     bool hier_flow = false;
@@ -166,6 +177,20 @@ int apply3(stg_t* h, const float4* x, float4* y);
 // z += NN(r1): the learned correction (unet.cu); net_free releases the network
 int net_correct(stg_t* h, const float4* r1, float4* z);
 void net_free(stg_t* h);
+
+// General-coefficient form (general.cu): per-face vols and fixed cells
+int op64v(cudaStream_t st, const Geom& g, const d4* x, const uint8_t* m, const d4* P, const d4* V, const d4* b, d4* out,
+          int mode, double* part, int* nb_out);
+int vol_from_field(cudaStream_t st, const Geom& g, const double* cell, const double* f0, const double* f1, const double* f2,
+                   const uint8_t* m, d4* V);
+int gen_setup(stg_t* h);
+int gen_smooth(stg_t* h, Level& L, bool post, const d4* r_in, d4* out);
+int gen_vcycle(stg_t* h);
+int gen_vanka(stg_t* h, Level& L, int flag, const d4* r, d4* out);
+int gen_precond(stg_t* h, const float4* rhs, float4* out);
+int gen_apply32(stg_t* h, const float4* x, float4* y);
+int gen_shift32(stg_t* h, const float4* v, const float4* z, float4* out);
+int gen_resid64(stg_t* h, const d4* b, const d4* x, d4* r, double* nrm2_host);
 
 // MMA design update (mma.cu) on device cell arrays; d_xout may alias d_x
 int mma_update(stg_t* h, const double* d_x, const double* d_df, double frac, double coef, double lo, double hi, double movlim,

@@ -256,6 +256,32 @@ void dense_free(DenseCoarse& D) {
     D = DenseCoarse();
 }
 
+int op64v(cudaStream_t st, const Geom& g, const d4* x, const uint8_t* m, const d4* P, const d4* V, const d4* b, d4* out,
+          int mode, double* part, int* nb_out);
+
+int dense_setup_v(cudaStream_t st, DenseCoarse& D, const Geom& g, const d4* V, const uint8_t* m, const d4* P64, int closed,
+                  const std::function<int(double*, int)>& extra) {
+    const int nd = D.nd;
+    k_aug_init<<<grid_for(2ll * nd * nd, TPB), TPB, 0, st>>>(nd, D.A);
+    STG_LAUNCH_CK();
+    for (int kind = 0; kind < 2; kind++) {
+        int nflags = kind == 0 ? 2 : 7;
+        for (int f = 0; f < nflags; f++) {
+            k_probe<<<grid_for(g.box(), TPB), TPB, 0, st>>>(g, kind, f, D.probe);
+            STG_LAUNCH_CK();
+            STG_TRY(op64v(st, g, D.probe, m, P64, V, nullptr, D.image, 0, nullptr, nullptr));
+            k_scatter<<<grid_for(nd, TPB), TPB, 0, st>>>(g, kind, f, nd, D.slot_of, D.comp_of, D.dense_of, D.image, D.A);
+            STG_LAUNCH_CK();
+        }
+    }
+    if (closed) {
+        k_closed<<<grid_for((long long)nd * nd, TPB), TPB, 0, st>>>(nd, D.comp_of, D.A);
+        STG_LAUNCH_CK();
+    }
+    if (extra) STG_TRY(extra(D.A, nd));
+    return gj_invert(st, nd, D.A, D.Ainv, D.info, &D.inv);
+}
+
 int dense_setup(cudaStream_t st, DenseCoarse& D, const Geom& g, double vol, const uint8_t* m, const d4* P64, int closed) {
     const int nd = D.nd;
     k_aug_init<<<grid_for(2ll * nd * nd, TPB), TPB, 0, st>>>(nd, D.A);

@@ -181,7 +181,44 @@ __device__ __forceinline__ float4 parent_value<__nv_bfloat16>(const __nv_bfloat1
     return make_float4(a.x, a.y, b.x, b.y);
 }
 
+// Interpolated face value of component d (0 x, 1 y, 2 z) at fine slot (i, j, k): along the
+// face normal the fine face lies on a coarse face (even index: weight 1) or midway between
+// two (odd: 1/2 each); along each tangent the fine face centre lies a quarter of a coarse
+// cell from the coarse face centre of the same parent and three quarters from the next one
+// (weights 3/4 and 1/4). Coarse faces that are fixed, absent or in the halo hold zero.
 template <class C>
+__device__ __forceinline__ float face_interp(const C* xc, const Geom& gc, int d, int i, int j, int k) {
+    const int f[3] = {i, j, k};
+    int lo[3], hi[3];
+    float wl[3], wh[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        const int c = f[a] >> 1, b = f[a] & 1;
+        if (a == d) {
+            lo[a] = c;
+            hi[a] = c + 1;
+            wl[a] = b ? 0.5f : 1.f;
+            wh[a] = b ? 0.5f : 0.f;
+        } else {
+            lo[a] = c;
+            hi[a] = b ? c + 1 : c - 1;
+            wl[a] = 0.75f;
+            wh[a] = 0.25f;
+        }
+    }
+    float acc = 0.f;
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+        const int a0 = (q & 1) ? hi[0] : lo[0], a1 = (q & 2) ? hi[1] : lo[1], a2 = (q & 4) ? hi[2] : lo[2];
+        const float w = ((q & 1) ? wh[0] : wl[0]) * ((q & 2) ? wh[1] : wl[1]) * ((q & 4) ? wh[2] : wl[2]);
+        if (w == 0.f) continue;
+        const float4 v = parent_value<C>(xc, gc.slot(a0, a1, a2));
+        acc += w * (d == 0 ? v.y : d == 1 ? v.z : v.w);
+    }
+    return acc;
+}
+
+template <class C, bool LIN>
 __global__ void __launch_bounds__(TPB) k_prolong_add32(Geom gf, Geom gc, const C* __restrict__ xc,
                                                        const uint8_t* __restrict__ mf, float4* __restrict__ xf) {
     long long t = (long long)blockIdx.x * TPB + threadIdx.x;
@@ -190,6 +227,11 @@ __global__ void __launch_bounds__(TPB) k_prolong_add32(Geom gf, Geom gc, const C
     gf.box_ijk(t, i, j, k);
     int s = gf.slot(i, j, k);
     float4 v = parent_value<C>(xc, gc.slot(i >> 1, j >> 1, k >> 1));
+    if (LIN) {
+        v.y = face_interp<C>(xc, gc, 0, i, j, k);
+        v.z = face_interp<C>(xc, gc, 1, i, j, k);
+        v.w = face_interp<C>(xc, gc, 2, i, j, k);
+    }
     uint8_t mm = __ldg(mf + s);
     float4 x = xf[s];
     if (!(mm & MP)) x.x += v.x;
@@ -720,14 +762,22 @@ int restrict_resid32(cudaStream_t st, const Geom& gc, const Geom& gf, float volf
     return STG_OK;
 }
 
-int prolong_add32(cudaStream_t st, const Geom& gf, const Geom& gc, const float4* xc, const uint8_t* mf, float4* xf) {
-    k_prolong_add32<float4><<<grid_for(gf.box(), TPB), TPB, 0, st>>>(gf, gc, xc, mf, xf);
+int prolong_add32(cudaStream_t st, const Geom& gf, const Geom& gc, const float4* xc, const uint8_t* mf, float4* xf,
+                  bool linear) {
+    if (linear)
+        k_prolong_add32<float4, true><<<grid_for(gf.box(), TPB), TPB, 0, st>>>(gf, gc, xc, mf, xf);
+    else
+        k_prolong_add32<float4, false><<<grid_for(gf.box(), TPB), TPB, 0, st>>>(gf, gc, xc, mf, xf);
     STG_LAUNCH_CK();
     return STG_OK;
 }
 
-int prolong_add_bf16(cudaStream_t st, const Geom& gf, const Geom& gc, const __nv_bfloat16* xc, const uint8_t* mf, float4* xf) {
-    k_prolong_add32<__nv_bfloat16><<<grid_for(gf.box(), TPB), TPB, 0, st>>>(gf, gc, xc, mf, xf);
+int prolong_add_bf16(cudaStream_t st, const Geom& gf, const Geom& gc, const __nv_bfloat16* xc, const uint8_t* mf, float4* xf,
+                     bool linear) {
+    if (linear)
+        k_prolong_add32<__nv_bfloat16, true><<<grid_for(gf.box(), TPB), TPB, 0, st>>>(gf, gc, xc, mf, xf);
+    else
+        k_prolong_add32<__nv_bfloat16, false><<<grid_for(gf.box(), TPB), TPB, 0, st>>>(gf, gc, xc, mf, xf);
     STG_LAUNCH_CK();
     return STG_OK;
 }

@@ -4,6 +4,8 @@
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
+#include <functional>
+
 #include "internal.cuh"
 
 namespace stg {
@@ -44,10 +46,12 @@ int fixed_nonzero(cudaStream_t st, const Geom& g, const d4* x, const uint8_t* m,
 int zero_fixed(cudaStream_t st, const Geom& g, const uint8_t* m, d4* x);
 // x_f = b_f on every fixed unknown of the box (the fixed rows of A are the identity)
 int patch_fixed(cudaStream_t st, const Geom& g, const d4* b, const uint8_t* m, d4* x);
-// xf += fix_f (injection of xc)
-int prolong_add32(cudaStream_t st, const Geom& gf, const Geom& gc, const float4* xc, const uint8_t* mf, float4* xf);
+// xf += fix_f (injection of xc); linear: face values interpolated (stg_opts.prolong 1)
+int prolong_add32(cudaStream_t st, const Geom& gf, const Geom& gc, const float4* xc, const uint8_t* mf, float4* xf,
+                  bool linear = false);
 // same with BF16-stored coarse correction
-int prolong_add_bf16(cudaStream_t st, const Geom& gf, const Geom& gc, const __nv_bfloat16* xc, const uint8_t* mf, float4* xf);
+int prolong_add_bf16(cudaStream_t st, const Geom& gf, const Geom& gc, const __nv_bfloat16* xc, const uint8_t* mf, float4* xf,
+                     bool linear = false);
 int to_bf16(cudaStream_t st, const Geom& g, const float4* x, __nv_bfloat16* y);
 // y = FP16(x / *scale) on the box slots; the per-level scales (level 0 coarsest) from the
 // finest level's penalties: scale[l] = 8^(nlev-1-l) x the power of two that keeps them below 2^15
@@ -133,6 +137,10 @@ int dense_init(DenseCoarse& D, const Geom& g);
 void dense_free(DenseCoarse& D);
 // DirectSolve3D::update: probe assembly + (closed) all-ones p-block + inversion
 int dense_setup(cudaStream_t st, DenseCoarse& D, const Geom& g, double vol, const uint8_t* m, const d4* P64, int closed);
+// The same with per-slot face vols (general.cu op64v); extra(A, nd) may add entries to the
+// assembled matrix (row-major, row stride 2 nd) before the inversion
+int dense_setup_v(cudaStream_t st, DenseCoarse& D, const Geom& g, const d4* V, const uint8_t* m, const d4* P64, int closed,
+                  const std::function<int(double*, int)>& extra);
 // In-place Gauss-Jordan inversion of the row-major nd x 2nd [A | I] held in a (b is the
 // second buffer of the same size); *inv receives the inverse (row stride 2 nd), which
 // lies in whichever buffer the last step wrote. *info = first zero pivot + 1, or 0.

@@ -138,6 +138,7 @@ int fields_to_vec(stg_t* h, const double* dc, const double* const* df, d4* out) 
 int energy_op(stg_t* h, const d4* x, d4* out, double* part, int* nb) {
     if (h->dim == 2) return energy2d(h, x, out, part, nb);
     Level& F = fine(h);
+    if (h->gen) return op64v(h->st, F.g, x, F.m, F.P64, F.V64, nullptr, out, 2, part, nb);
     return op64(h->st, F.g, F.vol, x, F.m, F.P64, nullptr, out, 2, part, nb);
 }
 
@@ -158,6 +159,11 @@ int update(stg_t* h) {
     }
     // coarse boundary faces have fixed children, so the Laplacian form carries down
     for (auto& L : h->lv) L.lap = h->lap_ok;
+    if (h->gen) {
+        PROF(h, 8, 0.0, gen_setup(h));
+        h->updated = true;
+        return STG_OK;
+    }
     // FP16 copies of the penalties for the solver's own sweeps, each level divided by a scale
     // that keeps it in FP16's range (11 significant bits: the V-cycle count is the FP32 one)
     PROF(h, 8, 0.0, penalty_scales(h->st, fine(h).g, fine(h).P32, h->L, h->d_pmax, h->d_pscale));
@@ -235,6 +241,7 @@ int smooth(stg_t* h, Level& L, const float4* r, bool post, bool x_is_zero) {
 // `rhs`. The result is left in lv[top].x().
 int vcycle_levels(stg_t* h, int top, const float4* rhs) {
     const bool mixed = h->opts.method == STG_METHOD_MIXED;
+    const bool lin = h->opts.prolong == 1 && !h->reference_cycle;
     const int L = h->L;
     for (int i = top; i >= 1; i--) {
         Level& F = h->lv[i];
@@ -253,9 +260,9 @@ int vcycle_levels(stg_t* h, int top, const float4* rhs) {
         const float4* r = (i == L - 1) ? rhs : F.r;
         if (mixed) {
             PROF(h, 3, 24.0 * C.g.box(), to_bf16(h->st, C.g, C.x(), C.xbf));
-            PROF(h, 3, 8.0 * C.g.box() + 33.0 * F.g.box(), prolong_add_bf16(h->st, F.g, C.g, C.xbf, F.m, F.x()));
+            PROF(h, 3, 8.0 * C.g.box() + 33.0 * F.g.box(), prolong_add_bf16(h->st, F.g, C.g, C.xbf, F.m, F.x(), lin));
         } else {
-            PROF(h, 3, 16.0 * C.g.box() + 33.0 * F.g.box(), prolong_add32(h->st, F.g, C.g, C.x(), F.m, F.x()));
+            PROF(h, 3, 16.0 * C.g.box() + 33.0 * F.g.box(), prolong_add32(h->st, F.g, C.g, C.x(), F.m, F.x(), lin));
         }
         STG_TRY(smooth(h, F, r, true, false));
     }
@@ -312,7 +319,8 @@ int coarse_cycle(stg_t* h) {
     // the coarsest inverse lives in one of two buffers (fixed per handle): part of the key
     const long long key = (long long)per | ((long long)(h->opts.method == STG_METHOD_MIXED) << 3) |
                           ((long long)fast(h, h->lv[top]) << 4) | ((long long)(h->dense.inv == h->dense.Ainv) << 5) |
-                          ((long long)h->L << 6) | ((long long)h->reference_cycle << 12);  // adapters: FP32 sweeps
+                          ((long long)h->L << 6) | ((long long)h->reference_cycle << 12) |  // adapters: FP32 sweeps
+                          ((long long)(h->opts.prolong == 1) << 13);
     GraphCache& G = h->boost && !h->reference_cycle ? h->vgraph_boost : h->vgraph;
     return graphed(h, G, key, [&] { return vcycle_levels(h, top, nullptr); },
                    [&](bool save) {
@@ -337,11 +345,12 @@ int vcycle(stg_t* h, const float4* rhs) {
     STG_TRY(smooth(h, F, rhs, false, true));
     PROF(h, 2, 49.0 * F.g.box() + 17.0 * C.g.box(), restrict_resid32(h->st, C.g, F.g, (float)F.vol, rhs, F.x(), F.m, F.P32, C.m, C.r, fast(h, F)));
     STG_TRY(coarse_cycle(h));
+    const bool lin = h->opts.prolong == 1 && !h->reference_cycle;
     if (mixed) {
         PROF(h, 3, 24.0 * C.g.box(), to_bf16(h->st, C.g, C.x(), C.xbf));
-        PROF(h, 3, 8.0 * C.g.box() + 33.0 * F.g.box(), prolong_add_bf16(h->st, F.g, C.g, C.xbf, F.m, F.x()));
+        PROF(h, 3, 8.0 * C.g.box() + 33.0 * F.g.box(), prolong_add_bf16(h->st, F.g, C.g, C.xbf, F.m, F.x(), lin));
     } else {
-        PROF(h, 3, 16.0 * C.g.box() + 33.0 * F.g.box(), prolong_add32(h->st, F.g, C.g, C.x(), F.m, F.x()));
+        PROF(h, 3, 16.0 * C.g.box() + 33.0 * F.g.box(), prolong_add32(h->st, F.g, C.g, C.x(), F.m, F.x(), lin));
     }
     return smooth(h, F, rhs, true, false);
 }
@@ -721,6 +730,7 @@ void stg_default_opts(stg_opts* o) {
     o->verbose = 0;
     o->smooth_sweeps = 1;
     o->warm_start = 0;
+    o->prolong = 0;
 }
 
 const char* stg_last_error(void) { return g_err; }
@@ -899,7 +909,14 @@ int stg_destroy(stg_t* h) {
         cudaFree(L.P16);
         cudaFree(L.t0);
         cudaFree(L.t1);
+        cudaFree(L.V64);
+        for (d4* p : {L.gr, L.gx, L.gp, L.gAp}) cudaFree(p);
+        for (int c = 0; c < 2; c++) {
+            cudaFree(L.vblk[c]);
+            cudaFree(L.vpiv[c]);
+        }
     }
+    for (d4* p : h->gtmp) cudaFree(p);
     dense_free(h->dense);
     for (d4* p : {h->b64, h->x64, h->r64, h->t64, h->lam64}) cudaFree(p);
     cudaFree(h->w);
@@ -927,8 +944,12 @@ int stg_set_method(stg_t* h, int method) {
         set_error("stg_set_method: method %d not available for dim %d", method, h->dim);
         return STG_E_INVALID;
     }
+    if (h->gen && method == STG_METHOD_LEARNED) {
+        set_error("STG_METHOD_LEARNED needs uniform face vols and free cells");
+        return STG_E_UNSUPPORTED;
+    }
     h->opts.method = method;
-    if (h->dim == 3) h->precond = method == STG_METHOD_LEARNED ? precond_learned : precond3;
+    if (h->dim == 3 && !h->gen) h->precond = method == STG_METHOD_LEARNED ? precond_learned : precond3;
     return STG_OK;
 }
 
@@ -974,28 +995,28 @@ int stg_set_boundary(stg_t* h, const double* cell_vol, const int32_t* cell_fixed
         return STG_OK;
     }
     const int n = h->n;
-    // the uniform-coefficient smoother needs one vol value on the free faces and no fixed cell
+    // the uniform-coefficient form needs one vol value on the free faces and no fixed cell;
+    // anything else runs the general-coefficient form (general.cu)
     double v = NAN;
+    bool gen = false;
     for (int d = 0; d < 3; d++) {
         if (!face_vol[d] || !face_fixed[d]) {
             set_error("face arrays of axis %d missing", d);
             return STG_E_INVALID;
         }
-        for (size_t q = 0; q < h->nface; q++) {
+        for (size_t q = 0; q < h->nface && !gen; q++) {
             if (face_fixed[d][q]) continue;
             if (std::isnan(v)) v = face_vol[d][q];
-            if (face_vol[d][q] != v) {
-                set_error("free faces carry different vol values; this build implements uniform vol only");
-                return STG_E_UNSUPPORTED;
-            }
+            if (face_vol[d][q] != v) gen = true;
         }
     }
     if (cell_fixed)
-        for (size_t q = 0; q < h->ncell; q++)
-            if (cell_fixed[q]) {
-                set_error("fixed cells are not supported by this build");
-                return STG_E_UNSUPPORTED;
-            }
+        for (size_t q = 0; q < h->ncell && !gen; q++)
+            if (cell_fixed[q]) gen = true;
+    if (gen && h->opts.method == STG_METHOD_LEARNED) {
+        set_error("STG_METHOD_LEARNED needs uniform face vols and free cells");
+        return STG_E_UNSUPPORTED;
+    }
     // Laplacian form: every face on the domain boundary fixed (Field order, N+1 along d)
     bool bnd_fixed = true;
     for (int d = 0; d < 3 && bnd_fixed; d++)
@@ -1010,7 +1031,7 @@ int stg_set_boundary(stg_t* h, const double* cell_vol, const int32_t* cell_fixed
                     const size_t q = ((size_t)ijk[0] * (n + (d == 1)) + ijk[1]) * (n + (d == 2)) + ijk[2];
                     if (!face_fixed[d][q]) bnd_fixed = false;
                 }
-    h->lap_ok = bnd_fixed;
+    h->lap_ok = bnd_fixed && !gen;
     double cv = cell_vol ? cell_vol[0] : 1.0;
     Level& F = fine(h);
     F.vol = std::isnan(v) ? 0.0 : v;
@@ -1022,7 +1043,30 @@ int stg_set_boundary(stg_t* h, const double* cell_vol, const int32_t* cell_fixed
                                h->st));
         fi[d] = ist + h->ncell + d * h->nface;
     }
-    STG_TRY(mask_from_field(h->st, F.g, nullptr, fi[0], fi[1], fi[2], F.m));
+    const int* fc = nullptr;
+    if (gen && cell_fixed) {
+        STG_CK(cudaMemcpyAsync(ist, cell_fixed, sizeof(int) * h->ncell, cudaMemcpyHostToDevice, h->st));
+        fc = ist;
+    }
+    STG_TRY(mask_from_field(h->st, F.g, fc, fi[0], fi[1], fi[2], F.m));
+    h->gen = gen;
+    if (gen) {
+        // per-slot vols (0 on fixed unknowns, as the reference's finish() leaves them)
+        if (!F.V64 && dalloc(&F.V64, F.g.nslot)) return STG_E_CUDA;
+        const double* dc = nullptr;
+        const double* df[3] = {nullptr, nullptr, nullptr};
+        STG_TRY(upload_fields(h, cell_vol, face_vol, &dc, df));
+        STG_TRY(vol_from_field(h->st, F.g, dc, df[0], df[1], df[2], F.m, F.V64));
+        h->resid64 = gen_resid64;
+        h->precond = gen_precond;
+        h->apply32 = gen_apply32;
+        h->shift32 = gen_shift32;
+    } else {
+        h->resid64 = residual64;
+        h->precond = h->opts.method == STG_METHOD_LEARNED ? precond_learned : precond3;
+        h->apply32 = apply3;
+        h->shift32 = shift3;
+    }
     h->closed = closed != 0;
     h->have_boundary = true;
     h->updated = false;
@@ -1293,7 +1337,10 @@ int stg_apply_A_device(stg_t* h, int level, double* d_Ap, const double* d_p) {
     Level& L = h->lv[level];
     STG_TRY(ensure_adapter(L));
     STG_TRY(blocked_to_slots64(h->st, L.g, d_p, L.t0));
-    STG_TRY(op64(h->st, L.g, L.vol, L.t0, L.m, L.P64, nullptr, L.t1, 0, nullptr, nullptr));
+    if (h->gen)
+        STG_TRY(op64v(h->st, L.g, L.t0, L.m, L.P64, L.V64, nullptr, L.t1, 0, nullptr, nullptr));
+    else
+        STG_TRY(op64(h->st, L.g, L.vol, L.t0, L.m, L.P64, nullptr, L.t1, 0, nullptr, nullptr));
     // padding entries of the reference layout are fixed identity rows
     STG_TRY(slots_to_blocked64(h->st, L.g, L.t1, d_Ap, d_p));
     STG_CK(cudaStreamSynchronize(h->st));
@@ -1310,7 +1357,10 @@ int stg_apply_E_device(stg_t* h, double* d_Ap, const double* d_p) {
     Level& L = fine(h);
     STG_TRY(ensure_adapter(L));
     STG_TRY(blocked_to_slots64(h->st, L.g, d_p, L.t0));
-    STG_TRY(op64(h->st, L.g, L.vol, L.t0, L.m, L.P64, nullptr, L.t1, 2, nullptr, nullptr));
+    if (h->gen)
+        STG_TRY(op64v(h->st, L.g, L.t0, L.m, L.P64, L.V64, nullptr, L.t1, 2, nullptr, nullptr));
+    else
+        STG_TRY(op64(h->st, L.g, L.vol, L.t0, L.m, L.P64, nullptr, L.t1, 2, nullptr, nullptr));
     STG_TRY(slots_to_blocked64(h->st, L.g, L.t1, d_Ap, nullptr));
     STG_CK(cudaStreamSynchronize(h->st));
     return STG_OK;
@@ -1335,6 +1385,13 @@ int stg_vcycle_device(stg_t* h, double* d_out, const double* d_in) {
     Level& F = fine(h);
     STG_TRY(ensure_adapter(F));
     STG_TRY(blocked_to_slots64(h->st, F.g, d_in, F.t0));
+    if (h->gen) {
+        STG_CK(cudaMemcpyAsync(F.gr, F.t0, sizeof(d4) * F.g.nslot, cudaMemcpyDeviceToDevice, h->st));
+        STG_TRY(gen_vcycle(h));
+        STG_TRY(slots_to_blocked64(h->st, F.g, F.gx, d_out, nullptr));
+        STG_CK(cudaStreamSynchronize(h->st));
+        return STG_OK;
+    }
     PathGuard guard{h};
     STG_TRY(choose_path(h, F, F.t0));
     STG_TRY(f64_to_f32(h->st, F.g.nslot, F.t0, 1.0, h->w));
@@ -1386,6 +1443,15 @@ int stg_apply_op_device(stg_t* h, int op, int level, double* d_out, const double
         case STG_OP_VANKA_BLACK: {
             if (level == 0) break;
             STG_TRY(blocked_to_slots64(h->st, L.g, d_in, L.t0));
+            if (h->gen) {
+                if (op == STG_OP_SMOOTH_PRE || op == STG_OP_SMOOTH_POST)
+                    STG_TRY(gen_smooth(h, L, op == STG_OP_SMOOTH_POST, L.t0, L.t1));
+                else
+                    STG_TRY(gen_vanka(h, L, op == STG_OP_VANKA_BLACK ? 1 : 0, L.t0, L.t1));
+                STG_TRY(slots_to_blocked64(h->st, L.g, L.t1, d_out, nullptr));
+                STG_CK(cudaStreamSynchronize(h->st));
+                return STG_OK;
+            }
             PathGuard guard{h};
             STG_TRY(choose_path(h, L, L.t0));
             STG_TRY(f64_to_f32(h->st, L.g.nslot, L.t0, 1.0, L.r));
@@ -1434,8 +1500,12 @@ int stg_level_descr_device(stg_t* h, int level, double* d_vol, double* d_penalty
     if (d_penalty) STG_TRY(slots_to_blocked64(h->st, L.g, L.P64, d_penalty, nullptr));
     if (d_fixed) STG_TRY(mask_to_blocked(h->st, L.g, L.m, d_fixed));
     if (d_vol) {
-        STG_TRY(vol_slots(h->st, L.g, L.m, L.cell_vol, L.vol, L.t0));
-        STG_TRY(slots_to_blocked64(h->st, L.g, L.t0, d_vol, nullptr));
+        if (h->gen) {
+            STG_TRY(slots_to_blocked64(h->st, L.g, L.V64, d_vol, nullptr));
+        } else {
+            STG_TRY(vol_slots(h->st, L.g, L.m, L.cell_vol, L.vol, L.t0));
+            STG_TRY(slots_to_blocked64(h->st, L.g, L.t0, d_vol, nullptr));
+        }
     }
     STG_CK(cudaStreamSynchronize(h->st));
     return STG_OK;

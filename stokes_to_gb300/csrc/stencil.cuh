@@ -122,6 +122,102 @@ __device__ __forceinline__ void stencil_core(LD ld, T vol, uint8_t ms, T out[4])
     out[3] = (ms & MW) ? T(0) : gz;
 }
 
+// General-coefficient form: every face carries its own vol (V u per face, V at the
+// receiving face for the curl-curl and gradient terms), fixed faces carry vol 0 (as
+// StokeFlowDescriptor3D::finish leaves them), cells may be fixed. The same 13 slots as
+// stencil_core, each read with its three face vols.
+template <class T>
+struct NbV {
+    T p, ux, uy, uz;     // p and the masked face values fix_f u
+    T vux, vuy, vuz;     // V u of the three faces
+    bool mc;
+};
+
+template <class T, class VV>
+__device__ __forceinline__ NbV<T> nbv_load(const VV* x, const uint8_t* m, const VV* vol, int q) {
+    T p, u, v, w, c, a, b, e;
+    load4(x, q, p, u, v, w);
+    load4(vol, q, c, a, b, e);
+    uint8_t mm = __ldg(m + q);
+    NbV<T> r;
+    r.p = p;
+    r.ux = (mm & MU) ? T(0) : u;
+    r.uy = (mm & MV) ? T(0) : v;
+    r.uz = (mm & MW) ? T(0) : w;
+    r.vux = a * r.ux;
+    r.vuy = b * r.uy;
+    r.vuz = e * r.uz;
+    r.mc = !(mm & MP);
+    return r;
+}
+
+// A (or E) rows at slot s without the diagonal P x + F x terms; vx, vy, vz = the slot's face vols.
+template <class T, bool ENERGY, class LD>
+__device__ __forceinline__ void stencil_core_v(LD ld, T vx, T vy, T vz, uint8_t ms, T out[4]) {
+    NbV<T> c0 = ld(0, 0, 0);
+    NbV<T> xm = ld(-1, 0, 0), xp = ld(1, 0, 0);
+    NbV<T> ym = ld(0, -1, 0), yp = ld(0, 1, 0);
+    NbV<T> zm = ld(0, 0, -1), zp = ld(0, 0, 1);
+    NbV<T> xp_ym = ld(1, -1, 0), xm_yp = ld(-1, 1, 0);
+    NbV<T> xp_zm = ld(1, 0, -1), xm_zp = ld(-1, 0, 1);
+    NbV<T> yp_zm = ld(0, 1, -1), ym_zp = ld(0, -1, 1);
+    // fix_c D (V u) at the own cell and the three lower neighbours
+    T dv0 = c0.mc ? ((xp.vux - c0.vux) + (yp.vuy - c0.vuy) + (zp.vuz - c0.vuz)) : T(0);
+    T dvx = xm.mc ? ((c0.vux - xm.vux) + (xm_yp.vuy - xm.vuy) + (xm_zp.vuz - xm.vuz)) : T(0);
+    T dvy = ym.mc ? ((xp_ym.vux - ym.vux) + (c0.vuy - ym.vuy) + (ym_zp.vuz - ym.vuz)) : T(0);
+    T dvz = zm.mc ? ((xp_zm.vux - zm.vux) + (yp_zm.vuy - zm.vuy) + (c0.vuz - zm.vuz)) : T(0);
+    // curl-curl of fix_f u, as in stencil_core
+    T ex0 = c0.uy - zm.uy - c0.uz + ym.uz;
+    T exk = zp.uy - c0.uy - zp.uz + ym_zp.uz;
+    T exj = yp.uy - yp_zm.uy - yp.uz + c0.uz;
+    T ey0 = zm.ux - c0.ux + c0.uz - xm.uz;
+    T eyk = c0.ux - zp.ux + zp.uz - xm_zp.uz;
+    T eyi = xp_zm.ux - xp.ux + xp.uz - c0.uz;
+    T ez0 = c0.ux - ym.ux + xm.uy - c0.uy;
+    T ezj = yp.ux - c0.ux + xm_yp.uy - yp.uy;
+    T ezi = xp.ux - xp_ym.ux + c0.uy - xp.uy;
+    T ccx = (eyk - ey0) + (ez0 - ezj);
+    T ccy = (ex0 - exk) + (ezi - ez0);
+    T ccz = (exj - ex0) + (ey0 - eyi);
+    T gx = -(dv0 - dvx) + vx * ccx;
+    T gy = -(dv0 - dvy) + vy * ccy;
+    T gz = -(dv0 - dvz) + vz * ccz;
+    if (!ENERGY) {
+        gx -= vx * (c0.p - xm.p);
+        gy -= vy * (c0.p - ym.p);
+        gz -= vz * (c0.p - zm.p);
+    }
+    out[0] = ENERGY ? T(0) : dv0;
+    out[1] = (ms & MU) ? T(0) : gx;
+    out[2] = (ms & MV) ? T(0) : gy;
+    out[3] = (ms & MW) ? T(0) : gz;
+}
+
+// Full rows of A x (or E x) at slot s in the general-coefficient form.
+template <class T, bool ENERGY, class VV>
+__device__ __forceinline__ void apply_rows_v(const VV* __restrict__ x, const uint8_t* __restrict__ m, const VV* __restrict__ P,
+                                             const VV* __restrict__ vol, int s, int di, int dj, T out[4]) {
+    const uint8_t ms = __ldg(m + s);
+    T c, vx, vy, vz;
+    load4(vol, s, c, vx, vy, vz);
+    auto ld = [&](int a, int b, int e) { return nbv_load<T>(x, m, vol, s + a * di + b * dj + e); };
+    stencil_core_v<T, ENERGY>(ld, vx, vy, vz, ms, out);
+    T xp, xu, xv, xw, pp, pu, pv, pw;
+    load4(x, s, xp, xu, xv, xw);
+    load4(P, s, pp, pu, pv, pw);
+    if (ENERGY) {
+        out[0] += pp * xp;
+        out[1] += pu * xu;
+        out[2] += pv * xv;
+        out[3] += pw * xw;
+    } else {
+        out[0] += (pp + ((ms & MP) ? T(1) : T(0))) * xp;
+        out[1] += (pu + ((ms & MU) ? T(1) : T(0))) * xu;
+        out[2] += (pv + ((ms & MV) ? T(1) : T(0))) * xv;
+        out[3] += (pw + ((ms & MW) ? T(1) : T(0))) * xw;
+    }
+}
+
 template <class T, bool ENERGY, class V>
 __device__ __forceinline__ void stencil_rows(const V* __restrict__ x, const uint8_t* __restrict__ m, int s, int di, int dj,
                                              T vol, uint8_t ms, T out[4]) {

@@ -264,8 +264,14 @@ def test_errors_are_reported(stg):
     vol = [np.ones(stg.face_shape(n, d)) for d in range(3)]
     vol[0][3, 3, 3] = 2.0
     fixed = [np.zeros(stg.face_shape(n, d), dtype=np.int32) for d in range(3)]
+    # non-uniform vols run the general-coefficient form, which the learned method lacks
+    learned = stg.Solver(n, method=stg.STG_METHOD_LEARNED)
     with pytest.raises(stg.StgError) as e:
-        s.set_boundary(np.ones((n, n, n)), np.zeros((n, n, n), dtype=np.int32), vol, fixed)
+        learned.set_boundary(np.ones((n, n, n)), np.zeros((n, n, n), dtype=np.int32), vol, fixed)
+    assert e.value.code == stg.STG_E_UNSUPPORTED
+    s.set_boundary(np.ones((n, n, n)), np.zeros((n, n, n), dtype=np.int32), vol, fixed)
+    with pytest.raises(stg.StgError) as e:
+        s.set_method(stg.STG_METHOD_LEARNED)
     assert e.value.code == stg.STG_E_UNSUPPORTED
 
 
