@@ -18,7 +18,16 @@ Borrvall-Petersson alpha law (amax 1e4). Working set is ~27 GB, far above the 12
   roofline / vcycle_hbm  the dominant kernel class and the whole V-cycle: algorithmic bytes
          over CUDA-event time against the measured copy bandwidth; traffic from the
          committed ncu summary
-  --impl reference: the CPU reference restatement (oracle) on the host cores.
+  solve_batches  the configurations' batches of independent solves: 100 at 128^3 (plain)
+         and 50 at 256^3 (mixed), each on its own seeded density
+  cpu_baseline  a bounded sample of the 256^3 oracle solve on the host cores (its set-up
+         and two GMRES(V-cycle) iterations), scaled to the iteration count of the full
+         256^3 oracle solve recorded in profiles/oracle_solve_256cube.md
+  --impl reference: one full 256^3 oracle solve (the reference's FP64 GMRES(V-cycle) path
+         restated, pinned to the reference's own code) on all the host cores, measured.
+  --oracle-check: the GPU solutions against the FP64 oracle per field, J and dJ/drho.
+  --learned-config: the learned configuration (training on noise and OC trajectories,
+         then learned against plain on solves and the 40-iteration design loop).
 
 N>1 (torchrun): independent replicas, one per GPU, barrier + max over ranks.
 """
@@ -57,6 +66,11 @@ def parse():
     ap.add_argument("--n", type=int, default=N_DEFAULT)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-methods", action="store_true", help="skip the reference-smoother, mixed and learned legs")
+    ap.add_argument("--oracle-check", action="store_true",
+                    help="per-field error of the GPU solve against the full FP64 oracle solve (minutes on the host)")
+    ap.add_argument("--learned-config", action="store_true",
+                    help="train the network per the learned configuration and compare it with plain (minutes)")
+    ap.add_argument("--pairs", type=int, default=20000)
     return ap.parse_args()
 
 
@@ -225,53 +239,275 @@ def design_loop(driver, dim, n, frac, iters):
 
 
 # ------------------------------------------------------------------ reference (CPU) arm
-def cpu_reference_sample(sample_n=64):
-    """The reference algorithm restated on the CPU (GMRES with the reference V-cycle: Vanka
-    smoother, re-discretised coarse levels, dense coarsest solve), run to the same FP64
-    tolerance on the same problem family at sample_n^3, scaled by the cell count."""
+ORACLE_RECORD = os.path.join(ROOT, "profiles", "oracle_solve_256cube.md")
+
+
+def oracle_problem(n):
+    """The bench problem on the oracle: the same seeded density (seed 1, sigma 4), filter and
+    BP law as make_solver on rank 0."""
     from oracle import pyoracle as po
 
     po.build()
-    n = sample_n
     b = po.bc_parabolic(n)
     rho = po.density_noise(n, 1, 4.0)
-    fp = po.face_penalty(po.filt(rho, 1.5), 1, [1e4])
-    t0 = time.perf_counter()
+    phys = po.filt(rho, 1.5)
+    fp = po.face_penalty(phys, 1, [1e4])
     o = po.Steady3D(n)
     o.init_boundary(b)
     o.update_penalty(np.zeros((n, n, n)), fp)
     o.update_b(b.cell_b, b.face_b)
+    return po, o, b, phys
+
+
+def oracle_record():
+    """GMRES iterations and time of the full 256^3 oracle solve measured on this machine
+    (written by `bench.py --oracle-check`)."""
+    out = {}
+    if os.path.exists(ORACLE_RECORD):
+        for ln in open(ORACLE_RECORD):
+            p = ln.strip().split()
+            if len(p) == 3 and p[0] == "record":
+                out[p[1]] = float(p[2])
+    return out
+
+
+def oracle_full_solve(n, tol=TOL, max_iter=60, restarts=6):
+    """The reference algorithm on the host cores (the oracle: the reference's FP64 V-cycle -
+    Vanka smoother, re-discretised coarse levels, dense coarsest solve - as GMRES
+    preconditioner), solved to FP64 true relative residual `tol`. Returns the solution and
+    the timings of the set-up and of the Krylov solve."""
+    po, o, b, phys = oracle_problem(n)
+    t0 = time.perf_counter()
     o.setup()
-    x, st = o.solve(max_iter=60, abs_thr=0.0, rel_thr=1e-12, norm_thr=0.0, restarts=3, true_tol=TOL)
-    sec = time.perf_counter() - t0
+    t1 = time.perf_counter()
+    x, st = o.solve(max_iter=max_iter, abs_thr=0.0, rel_thr=1e-13, norm_thr=0.0, restarts=restarts, true_tol=tol)
+    t2 = time.perf_counter()
+    return po, o, b, phys, x, st, t1 - t0, t2 - t1
+
+
+def cpu_reference_sample(n=N_DEFAULT, iters=2):
+    """A bounded sample of the 256^3 oracle solve: its full set-up and `iters` GMRES(V-cycle)
+    iterations, measured on the host cores; scaled to a whole solve with the iteration count
+    of the full 256^3 oracle solve recorded in profiles/oracle_solve_256cube.md."""
+    po, o, b, phys = oracle_problem(n)
+    t0 = time.perf_counter()
+    o.setup()
+    t1 = time.perf_counter()
+    o.solve(max_iter=iters + 1, abs_thr=0.0, rel_thr=0.0, norm_thr=0.0)
+    t2 = time.perf_counter()
     o.close()
-    scale = (N_DEFAULT / n) ** 3
-    return sec * scale, sec, st
+    setup_s, per_iter = t1 - t0, (t2 - t1) / iters
+    rec = oracle_record() if n == 256 else {}
+    full_iters = rec.get("iterations", None)
+    value = setup_s + per_iter * (full_iters if full_iters else iters)
+    sample = (f"oracle at {n}^3 (the reference's FP64 GMRES(V-cycle) path restated): set-up {setup_s:.1f} s + "
+              f"{iters} GMRES iterations at {per_iter:.2f} s each, measured; scaled to the "
+              + (f"{int(full_iters)} iterations the full {n}^3 oracle solve to {TOL:g} needs "
+                 f"(profiles/oracle_solve_256cube.md: measured {rec.get('total_s', 0):.0f} s in full)"
+                 if full_iters else f"{iters} sampled iterations (no full-solve record)"))
+    return value, sample, setup_s + iters * per_iter
 
 
 def run_reference(args):
+    """--impl reference: one full 256^3 oracle solve to FP64 true residual 1e-8 on all the
+    host cores, measured end to end (set-up + GMRES). Steps and warm-ups are capped at 1
+    and 0: one solve takes minutes on the host cores."""
     world, rank, local = dist_env()
     if rank != 0:
         return
     cores = os.cpu_count() or 1
     os.environ.setdefault("OMP_NUM_THREADS", str(cores))
-    times = []
-    for i in range(args.warmup + args.steps):
-        v, sec, st = cpu_reference_sample()
-        if i >= args.warmup:
-            times.append(v)
-    value = statistics.mean(times)
-    sample = (f"oracle GMRES(V-cycle) solve of the 64^3 instance of the same problem to FP64 rel. residual "
-              f"{TOL:g} ({st['iters']} GMRES iterations, {sec:.2f} s), scaled x64 by cell count to 256^3")
+    n = args.n
+    po, o, b, phys, x, st, setup_s, solve_s = oracle_full_solve(n)
+    value = setup_s + solve_s
+    sample = (f"one full {n}^3 oracle solve (the reference's FP64 GMRES(V-cycle) path restated, its Vanka "
+              f"smoother and dense coarsest solve) to FP64 true rel. residual {TOL:g}: set-up {setup_s:.1f} s, "
+              f"{st['iters']} GMRES iterations ({st['restarts']} restarts) {solve_s:.1f} s, final {st['rel_true']:.2e}; "
+              f"steps/warm-ups capped at 1/0 (one solve takes minutes on the host cores)")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "s/solve", "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": value * 1e3, "higher_is_better": False,
+        "steps": 1, "warmup": 0, "ms_per_step": value * 1e3, "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "3D 256^3 Brinkman-Stokes solve to FP64 rel. residual 1e-8", "n": 256, "tol": TOL},
-        "cpu_baseline": {"value": value, "unit": "s/solve", "cores": cores, "kind": "port", "sample": sample},
+        "config": {"workload": f"3D {n}^3 Brinkman-Stokes solve to FP64 rel. residual {TOL:g}", "n": n, "tol": TOL},
+        "cpu_baseline": {"value": value, "unit": "s/solve", "cores": int(os.environ["OMP_NUM_THREADS"]), "kind": "port",
+                         "sample": sample},
         "e2e": {"value": value, "unit": "s/solve", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+def oracle_check(args):
+    """--oracle-check: the GPU solves of the bench problem (plain and mixed) against the FP64
+    oracle at n^3, per field (velocity components, pressure modulo a constant), the energy J
+    and the adjoint sensitivity dJ/drho; and the oracle's own timings, including its solve to
+    the bench tolerance. Writes one JSON line."""
+    import torch
+
+    from stokes_to_gb300 import build, capi
+
+    build.build()
+    n = args.n
+    cores = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
+    cell_vol, cell_fixed, cell_b, face_vol, face_fixed, face_b = parabolic_bc(n)
+    law = capi.alpha_bp(1e4)
+    out = {}
+    for method, name in ((capi.STG_METHOD_PLAIN, "plain"), (capi.STG_METHOD_MIXED, "mixed")):
+        s = capi.Solver(n, method=method, tol=1e-9)
+        s.set_boundary(cell_vol, cell_fixed, face_vol, face_fixed, True)
+        s.density_noise(1, 4.0, want=False)
+        s.filter(1.5, None, want=False)
+        s.set_density(None, law)
+        s.set_rhs(cell_b, face_b)
+        p, vel, st = s.solve()
+        J = s.energy()
+        g, ast = s.adjoint_sensitivity(law)
+        out[name] = {"p": p, "vel": vel, "J": J, "sens": g, "rel_residual": st["rel_residual"],
+                     "adjoint_rel_residual": ast["rel_residual"]}
+        s.close()
+    torch.cuda.empty_cache()
+    # the oracle's solve to the bench tolerance first (its timing is the CPU record), then
+    # a tighter one for the comparison
+    po8, o8, b8, phys8, x8, st8, setup8, solve8 = oracle_full_solve(n, TOL)
+    o8.close()
+    po, o, b, phys, x, st, setup_s, solve_s = oracle_full_solve(n, 1e-10)
+    t0 = time.perf_counter()
+    o.set_b_blocked(o.apply_E(x))
+    lam, ast = o.solve(max_iter=60, abs_thr=0.0, rel_thr=1e-13, norm_thr=0.0, restarts=6, true_tol=1e-10)
+    adj_s = time.perf_counter() - t0
+    p_ref, vel_ref = po.blocked_to_field(n, x)
+    _, lam_f = po.blocked_to_field(n, lam)
+    g_ref = po.sensitivity(phys, 1, [1e4], vel_ref, lam_f)
+    J_ref = o.energy(x)
+
+    def rel(a, b_):
+        return float(np.linalg.norm(np.asarray(a) - np.asarray(b_)) / np.linalg.norm(np.asarray(b_)))
+
+    res = {"workload": f"3D {n}^3 bench problem, GPU solves to 1e-9 against the FP64 oracle solves to 1e-10",
+           "oracle_to_bench_tol": {"setup_s": round(setup8, 2), "solve_s": round(solve8, 2), "iterations": st8["iters"],
+                                   "restarts": st8["restarts"], "rel_true": st8["rel_true"],
+                                   "total_s": round(setup8 + solve8, 2), "cores": int(os.environ["OMP_NUM_THREADS"])},
+           "oracle_to_1e-10": {"setup_s": round(setup_s, 2), "solve_s": round(solve_s, 2), "iterations": st["iters"],
+                               "restarts": st["restarts"], "rel_true": st["rel_true"], "adjoint_s": round(adj_s, 2),
+                               "adjoint_rel_true": ast["rel_true"]}}
+    for name in ("plain", "mixed"):
+        r = out[name]
+        res[name] = {"u": rel(r["vel"][0], vel_ref[0]), "v": rel(r["vel"][1], vel_ref[1]), "w": rel(r["vel"][2], vel_ref[2]),
+                     "p_mod_const": rel(r["p"] - r["p"].mean(), p_ref - p_ref.mean()),
+                     "J": abs(r["J"] - J_ref) / abs(J_ref), "sensitivity": rel(r["sens"], g_ref),
+                     "gpu_rel_residual": r["rel_residual"], "gpu_adjoint_rel_residual": r["adjoint_rel_residual"]}
+    print(json.dumps(res), flush=True)
+
+
+# ------------------------------------------------------------------ learned-preconditioner configuration
+def oc_loop(capi, s, n, frac, iters, law, on_iteration=None):
+    """The OC design loop of the fluid_topo driver (test 1: filter 1.5, move 0.2, uniform start
+    at the volume fraction) through the C ABI; on_iteration(it) runs after each iteration.
+    Returns per iteration (ms, V-cycles of both solves, objective, largest final residual)."""
+    import torch
+
+    x = np.full((n, n, n), frac)
+    out = []
+    for it in range(iters):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        phys = s.filter(1.5, x)
+        s.set_density(phys, law)
+        _, _, st = s.solve(want=False)
+        J = s.energy()
+        dc, ast = s.adjoint_sensitivity(law)
+        dc = s.filter(1.5, dc, transpose=True)
+        x, _ = s.oc_update(1.5, x, dc, frac)
+        torch.cuda.synchronize()
+        out.append(((time.perf_counter() - t0) * 1e3, st["inner_iters"] + ast["inner_iters"], J,
+                    max(st["rel_residual"], ast["rel_residual"])))
+        if on_iteration:
+            on_iteration(it)
+    return out
+
+
+def learned_config(args):
+    """--learned-config: the learned-preconditioner configuration as specified - the network
+    trained on the GPU by its own kernels at n^3 on residual/error pairs from the plain
+    solver's operators on seeded smoothed-noise densities (sigma 2..8) and on snapshots of
+    40-iteration OC runs at volume fractions 0.1..0.4 (Adam, lr 1e-3, --pairs in all) - then
+    applied inside FGMRES against the plain method: independent solves and the 40-iteration
+    design loop at fraction 0.15, every solve to FP64 rel. residual 1e-8. One JSON line."""
+    import torch
+
+    from stokes_to_gb300 import build, capi
+
+    build.build()
+    n = args.n
+    cell_vol, cell_fixed, cell_b, face_vol, face_fixed, face_b = parabolic_bc(n)
+    law = capi.alpha_bp(1e4)
+
+    def solver(method, **kw):
+        s = capi.Solver(n, method=method, tol=TOL, **kw)
+        s.set_boundary(cell_vol, cell_fixed, face_vol, face_fixed, True)
+        s.set_rhs(cell_b, face_b)
+        return s
+
+    tr = solver(capi.STG_METHOD_PLAIN, warm_start=1)
+    tr.net_init(7)
+    pairs, losses = 0, []
+    per_noise = max(1, args.pairs // 5 // 7)
+    t0 = time.perf_counter()
+    for q, sig in enumerate(range(2, 9)):
+        tr.density_noise(200 + q, float(sig), want=False)
+        tr.filter(1.5, None, want=False)
+        tr.set_density(None, law)
+        losses.extend(tr.net_train(per_noise, lr=1e-3, seed=11 + q).tolist())
+        pairs += per_noise
+    fracs = (0.1, 0.2, 0.3, 0.4)
+    per_snap = max(1, (args.pairs - pairs) // (len(fracs) * 20))
+
+    def snap(it):
+        nonlocal pairs
+        if it % 2 == 1:
+            losses.extend(tr.net_train(per_snap, lr=1e-3, seed=1000 + pairs).tolist())
+            pairs += per_snap
+
+    for f in fracs:
+        oc_loop(capi, tr, n, f, 40, law, snap)
+    torch.cuda.synchronize()
+    train_s = time.perf_counter() - t0
+    params = tr.net_params()
+    tr.close()
+
+    res = {"workload": f"3D {n}^3 learned-preconditioner configuration, every solve to FP64 rel. residual {TOL:g}",
+           "train": {"pairs": pairs, "s": round(train_s, 1), "noise_sigmas": "2..8",
+                     "trajectories": "OC runs of 40 iterations at fractions 0.1, 0.2, 0.3, 0.4; a training burst on "
+                                     "every second iteration's operator", "loss_first_100": round(float(np.mean(losses[:100])), 4),
+                     "loss_last_500": round(float(np.mean(losses[-500:])), 4)}}
+    for method, name in ((capi.STG_METHOD_PLAIN, "plain"), (capi.STG_METHOD_LEARNED, "learned")):
+        s = solver(method, warm_start=1)
+        if method == capi.STG_METHOD_LEARNED:
+            s.net_init(7)
+            s.net_set_params(params)
+        times, its, falls = [], [], []
+        for seed in range(11):
+            s.density_noise(3000 + seed, 4.0, want=False)
+            s.filter(1.5, None, want=False)
+            s.set_density(None, law)
+            torch.cuda.synchronize()
+            t1 = time.perf_counter()
+            _, _, st = s.solve(want=False)
+            torch.cuda.synchronize()
+            if seed > 0:  # the first solve warms the CUDA graphs
+                times.append(time.perf_counter() - t1)
+                its.append(st["inner_iters"])
+                falls.append(st["fallbacks"])
+        res[f"solves_{name}"] = {"s_per_solve": round(float(np.mean(times)), 5), "v_cycles_mean": float(np.mean(its)),
+                                 "fallbacks": int(sum(falls))}
+        loop = oc_loop(capi, s, n, 0.15, 40, law)
+        ms = np.array([q[0] for q in loop])
+        vc = np.array([q[1] for q in loop])
+        res[f"loop_{name}"] = {"total_s": round(float(ms.sum()) / 1e3, 3), "ms_per_iteration_median": round(float(np.median(ms)), 2),
+                               "v_cycles_per_iteration_median": float(np.median(vc)), "v_cycles_total": int(vc.sum()),
+                               "final_objective": float(loop[-1][2]), "rel_residual_max": float(max(q[3] for q in loop))}
+        s.close()
+    print(json.dumps(res), flush=True)
 
 
 # ------------------------------------------------------------------ replicas
@@ -458,6 +694,37 @@ def run_ours(args):
         methods["learned"] = r
         sv.close()
 
+    # ---- the batches of independent solves the benchmark configurations name: 100 solves at
+    # 128^3 (plain) and 50 at 256^3 (mixed), each on its own seeded density (sigma 4), every
+    # solve to FP64 rel. residual 1e-8; per solve: the density, filter and penalty set-up on
+    # the GPU and the solve, CUDA events around the whole batch
+    batches = None
+    if rank == 0 and world == 1 and not args.no_methods:
+        batches = {}
+        for nn, count, meth, name in ((128, 100, capi.STG_METHOD_PLAIN, "solves_128_plain"),
+                                      (n, 50, capi.STG_METHOD_MIXED, f"solves_{n}_mixed")):
+            sv = make_solver(meth, nn=nn)
+            sv.solve(want=False)
+            its, rels = [], []
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for seed in range(count):
+                sv.density_noise(1000 + seed, 4.0, want=False)
+                sv.filter(1.5, None, want=False)
+                sv.set_density(None, capi.alpha_bp(1e4))
+                _, _, st_ = sv.solve(want=False)
+                its.append(st_["inner_iters"])
+                rels.append(st_["rel_residual"])
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms_ = e0.elapsed_time(e1)
+            batches[name] = {"workload": f"{count} independent {nn}^3 solves ({'mixed' if meth else 'plain'}), seeded "
+                                         f"densities {1000}..{1000 + count - 1} (sigma 4), to FP64 rel. residual {TOL:g}",
+                             "s_total": round(ms_ / 1e3, 3), "s_per_solve": round(ms_ / 1e3 / count, 5),
+                             "v_cycles_mean": round(float(np.mean(its)), 2), "v_cycles_max": int(max(its)),
+                             "rel_residual_max": float(max(rels))}
+            sv.close()
+
     # ---- design loops through the fluid_topo driver: the 2D 64^2 one (uniform 0.3 start, solves
     # to 1e-10; latency-bound) and the 3D 128^3 one at fraction 0.15, 40 iterations (from
     # iteration 5 on high-contrast designs)
@@ -487,10 +754,9 @@ def run_ours(args):
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count() or 1))
-        cv, csec, cst = cpu_reference_sample()
+        cv, csample, csec = cpu_reference_sample(n)
         cpu = {"value": cv, "unit": "s/solve", "cores": int(os.environ["OMP_NUM_THREADS"]), "kind": "port",
-               "sample": f"oracle GMRES(V-cycle) solve of the 64^3 instance to FP64 rel. residual {TOL:g} "
-                         f"({cst['iters']} iterations, {csec:.2f} s on the host cores), scaled x64 by cell count"}
+               "sample": csample, "sample_s": round(csec, 2)}
 
     vc = statistics.mean(st["inner_iters"] for st in stats)
     if rank == 0:
@@ -514,6 +780,7 @@ def run_ours(args):
             "solver": {"v_cycles_per_solve": vc, "outer_per_solve": statistics.mean(st["outer_iters"] for st in stats),
                        "final_rel_residual_max": max(st["rel_residual"] for st in stats)},
             "methods": methods,
+            "solve_batches": batches,
             "design_loop_2d": loop2d,
             "design_loop_3d": loop3d,
             "kernels": kernel_table,
@@ -528,6 +795,10 @@ def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.oracle_check:
+        oracle_check(args)
+    elif args.learned_config:
+        learned_config(args)
     else:
         run_ours(args)
 
