@@ -21,10 +21,11 @@ Borrvall-Petersson alpha law (amax 1e4). Working set is ~27 GB, far above the 12
   solve_batches  the configurations' batches of independent solves: 100 at 128^3 (plain)
          and 50 at 256^3 (mixed), each on its own seeded density
   cpu_baseline  a bounded sample of the 256^3 oracle solve on the host cores (its set-up
-         and two GMRES(V-cycle) iterations), scaled to the iteration count of the full
+         and a two-iteration GMRES(V-cycle) run), scaled to the V-cycle count of the full
          256^3 oracle solve recorded in profiles/oracle_solve_256cube.md
-  --impl reference: one full 256^3 oracle solve (the reference's FP64 GMRES(V-cycle) path
-         restated, pinned to the reference's own code) on all the host cores, measured.
+  --impl reference: the same 256^3 oracle (the reference's FP64 GMRES(V-cycle) path
+         restated, pinned to the reference's own code) on all the host cores: set-up once,
+         a two-iteration GMRES run per step, scaled the same way.
   --oracle-check: the GPU solutions against the FP64 oracle per field, J and dJ/drho.
   --learned-config: the learned configuration (training on noise and OC trajectories,
          then learned against plain on solves and the 40-iteration design loop).
@@ -285,48 +286,71 @@ def oracle_full_solve(n, tol=TOL, max_iter=60, restarts=6):
     return po, o, b, phys, x, st, t1 - t0, t2 - t1
 
 
-def cpu_reference_sample(n=N_DEFAULT, iters=2):
-    """A bounded sample of the 256^3 oracle solve: its full set-up and `iters` GMRES(V-cycle)
-    iterations, measured on the host cores; scaled to a whole solve with the iteration count
-    of the full 256^3 oracle solve recorded in profiles/oracle_solve_256cube.md."""
+def oracle_sample(n):
+    """The oracle's 256^3 set-up and a bounded piece of its GMRES: returns (set-up s, the
+    oracle handle, a function that times one GMRES run of two iterations - three V-cycles
+    and two operator applications - and returns seconds per V-cycle)."""
     po, o, b, phys = oracle_problem(n)
     t0 = time.perf_counter()
     o.setup()
-    t1 = time.perf_counter()
-    o.solve(max_iter=iters + 1, abs_thr=0.0, rel_thr=0.0, norm_thr=0.0)
-    t2 = time.perf_counter()
-    o.close()
-    setup_s, per_iter = t1 - t0, (t2 - t1) / iters
+    setup_s = time.perf_counter() - t0
+
+    def step():
+        t1 = time.perf_counter()
+        o.solve(max_iter=3, abs_thr=0.0, rel_thr=0.0, norm_thr=0.0)
+        return (time.perf_counter() - t1) / 3.0
+
+    return setup_s, o, step
+
+
+def scale_to_solve(setup_s, per_vcycle, n):
+    """s per solve from a sample: the set-up plus the V-cycles of the full 256^3 oracle solve
+    to 1e-8 recorded in profiles/oracle_solve_256cube.md (measured there in full)."""
     rec = oracle_record() if n == 256 else {}
-    full_iters = rec.get("iterations", None)
-    value = setup_s + per_iter * (full_iters if full_iters else iters)
-    sample = (f"oracle at {n}^3 (the reference's FP64 GMRES(V-cycle) path restated): set-up {setup_s:.1f} s + "
-              f"{iters} GMRES iterations at {per_iter:.2f} s each, measured; scaled to the "
-              + (f"{int(full_iters)} iterations the full {n}^3 oracle solve to {TOL:g} needs "
-                 f"(profiles/oracle_solve_256cube.md: measured {rec.get('total_s', 0):.0f} s in full)"
-                 if full_iters else f"{iters} sampled iterations (no full-solve record)"))
-    return value, sample, setup_s + iters * per_iter
+    vc = rec.get("vcycles")
+    if vc:
+        return setup_s + per_vcycle * vc, (f"scaled to the {int(vc)} V-cycles of the full {n}^3 oracle solve to {TOL:g} "
+                                           f"(profiles/oracle_solve_256cube.md, measured there at {rec.get('total_s', 0):.0f} s)")
+    return setup_s + per_vcycle * 3, "not scaled (no full-solve record for this size)"
+
+
+def cpu_reference_sample(n=N_DEFAULT):
+    """cpu_baseline: the oracle's full 256^3 set-up and one GMRES run of two iterations,
+    measured on the host cores, scaled to a whole solve (scale_to_solve)."""
+    setup_s, o, step = oracle_sample(n)
+    per_vc = step()
+    o.close()
+    value, how = scale_to_solve(setup_s, per_vc, n)
+    sample = (f"oracle at {n}^3 (the reference's FP64 GMRES(V-cycle) path restated): set-up {setup_s:.1f} s and a "
+              f"GMRES run of 2 iterations ({per_vc:.2f} s per V-cycle), measured; {how}")
+    return value, sample, setup_s + 3 * per_vc
 
 
 def run_reference(args):
-    """--impl reference: one full 256^3 oracle solve to FP64 true residual 1e-8 on all the
-    host cores, measured end to end (set-up + GMRES). Steps and warm-ups are capped at 1
-    and 0: one solve takes minutes on the host cores."""
+    """--impl reference: the oracle (the reference's FP64 GMRES(V-cycle) path restated, pinned
+    to its own code) at 256^3 on all the host cores. Its set-up is measured once; every step
+    (warm-up or timed) is one GMRES run of two iterations at 256^3, so a step takes a few
+    seconds; the line's value is s per whole solve: set-up plus the mean V-cycle time times
+    the V-cycles of the full 256^3 oracle solve (recorded, measured in full, in
+    profiles/oracle_solve_256cube.md)."""
     world, rank, local = dist_env()
     if rank != 0:
         return
     cores = os.cpu_count() or 1
     os.environ.setdefault("OMP_NUM_THREADS", str(cores))
     n = args.n
-    po, o, b, phys, x, st, setup_s, solve_s = oracle_full_solve(n)
-    value = setup_s + solve_s
-    sample = (f"one full {n}^3 oracle solve (the reference's FP64 GMRES(V-cycle) path restated, its Vanka "
-              f"smoother and dense coarsest solve) to FP64 true rel. residual {TOL:g}: set-up {setup_s:.1f} s, "
-              f"{st['iters']} GMRES iterations ({st['restarts']} restarts) {solve_s:.1f} s, final {st['rel_true']:.2e}; "
-              f"steps/warm-ups capped at 1/0 (one solve takes minutes on the host cores)")
+    setup_s, o, step = oracle_sample(n)
+    for _ in range(args.warmup):
+        step()
+    per = [step() for _ in range(args.steps)]
+    o.close()
+    per_vc = statistics.mean(per)
+    value, how = scale_to_solve(setup_s, per_vc, n)
+    sample = (f"oracle at {n}^3 on {cores} host threads: set-up {setup_s:.1f} s (once), then per step a GMRES run of "
+              f"2 iterations (3 V-cycles, {per_vc:.2f} s each); value = set-up + V-cycle time x V-cycles, {how}")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "s/solve", "n_gpus": args.gpus,
-        "steps": 1, "warmup": 0, "ms_per_step": value * 1e3, "higher_is_better": False,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 3e3 * per_vc, "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": f"3D {n}^3 Brinkman-Stokes solve to FP64 rel. residual {TOL:g}", "n": n, "tol": TOL},
         "cpu_baseline": {"value": value, "unit": "s/solve", "cores": int(os.environ["OMP_NUM_THREADS"]), "kind": "port",
