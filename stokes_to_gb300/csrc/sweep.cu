@@ -946,27 +946,18 @@ __global__ void __launch_bounds__(NT, PB ? 4 : 3) k_sweep_tma(const __grid_const
     gm += 4 * plane;  // plane i0+3
     float4* gout = xout + (i0 + 1) * plane + out_jk;
 
-    // Two block barriers per plane: after the residual (the pressure phase reads neighbouring
-    // residuals) and after the pressure phase (the update reads neighbouring pressures).
-    // The loads of the next planes are issued after the first barrier of a plane - every
-    // thread has then finished the previous plane's update, the last reader of the ring
-    // slots they overwrite - and every thread waits for them on the mbarrier itself at the
-    // start of the next plane, so no third barrier is needed. The last plane issues none,
-    // so no copy is in flight when the block ends.
-    bool timed_out = false;
     for (int i = i0; i < i1; i++) {
-        if (i > i0 && !wait_loads()) timed_out = true;  // the loads issued during plane i-1
-        fetch_m(i + 3, gm);
-        residual(i + 1, x0, x1, x2, r1, p1, m1, rrm1);
-        if (__syncthreads_or(timed_out)) return fail(err);
         // stream x(i+3) into the slot of x(i-1), P(i+2) into P(i-1), r(i+2) into r(i)
-        if (tid == 0 && i + 1 < i1) {
+        if (tid == 0) {
             asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
             arm_tx(bar, (HAS_X ? XBYTES : 0) + PBYTES + RBYTES);
             if (HAS_X) tma_x(xm1, i + 3);
             tma_p(pm1, i + 2);
             tma_r(sr, r0, i + 2, &tmr);
         }
+        fetch_m(i + 3, gm);
+        residual(i + 1, x0, x1, x2, r1, p1, m1, rrm1);
+        __syncthreads();
         pressure(i, rr0, rrm1, p0, p1, m0, m1);
         __syncthreads();
         if (out_ok) {
@@ -999,6 +990,7 @@ __global__ void __launch_bounds__(NT, PB ? 4 : 3) k_sweep_tma(const __grid_const
             *gout = xo;
         }
         store_m(mm1);  // mask (i+3) into the slot of mask (i-1)
+        if (__syncthreads_or(!wait_loads())) return fail(err);
         S.dpp[tid] = S.dp[odi];
         // rotate the rings and advance the plane pointers
         {
