@@ -244,9 +244,7 @@ int stg_mma_reset(stg_t* h);
  * design d_x, the sensitivity d_dc and the result d_xnew (which may alias d_x); no
  * handle is needed and nothing is allocated.
  * The only scratch is a fixed 42 KB array inside this library's device image (every GPU
- * that loads the library holds it until exit). The first call on a device resolves that
- * array's device address (with the device current) - make it before any stream capture.
- * All calls share the array, so calls that overlap on the GPU (other streams, other host
+ * that loads the library holds it until exit). All calls share the array, so calls that overlap on the GPU (other streams, other host
  * threads on the same device) race; serialise them. N above 1024 and filter radii rmin
  * above 4 are rejected with STG_E_INVALID. Work is issued on cuda_stream (a cudaStream_t,
  * NULL = legacy default stream) and synchronised before return. Results equal
