@@ -70,6 +70,11 @@ typedef struct stg_opts {
                             along the face normal, 3/4 : 1/4 between the two nearest coarse
                             faces along each tangent - and pressures injected. The
                             LinearMapping adapters always inject. */
+    int basis16;         /* 1 (default): the 3D uniform-form FGMRES also keeps an FP16 copy
+                            of each basis vector (8 more bytes per slot and vector), from
+                            which its multi-dot pass reads; the projections and the
+                            solution update keep the FP32 basis. 0: FP32 only (e.g. to fit
+                            a 512^3 solve with a long basis in less memory). */
 } stg_opts;
 
 typedef struct stg_stats {
@@ -101,7 +106,7 @@ int stg_profile_read(stg_t* h, int cls, int64_t* launches, double* ms, double* b
 const char* stg_profile_name(int cls);
 
 /* Fills *o with the defaults (PLAIN, tol 1e-8, 20 outer, 30 inner, 1e-4, 1 sweep per colour,
-   no warm start). */
+   no warm start, injection, FP16 basis copies). */
 void stg_default_opts(stg_opts* o);
 
 /* Message of the last failure on this thread ("" if none). */

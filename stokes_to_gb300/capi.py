@@ -50,7 +50,8 @@ STG_PROF_NCLASS = 12
 class Opts(ctypes.Structure):
     _fields_ = [("method", ctypes.c_int), ("tol", ctypes.c_double), ("max_outer", ctypes.c_int),
                 ("inner_max", ctypes.c_int), ("inner_tol", ctypes.c_double), ("verbose", ctypes.c_int),
-                ("smooth_sweeps", ctypes.c_int), ("warm_start", ctypes.c_int), ("prolong", ctypes.c_int)]
+                ("smooth_sweeps", ctypes.c_int), ("warm_start", ctypes.c_int), ("prolong", ctypes.c_int),
+                ("basis16", ctypes.c_int)]
 
 
 class Stats(ctypes.Structure):

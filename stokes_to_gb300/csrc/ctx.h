@@ -105,11 +105,17 @@ struct stg_ctx {
     float* d_pscale = nullptr;
     unsigned* d_pmax = nullptr;
     const stg::d4 *df_x = nullptr, *df_b = nullptr;
+    // the last residual64 call left the residual in FP32 in w (double-float iterate)
+    bool r32_ok = false;
     // fine-level FP64
     stg::d4 *b64 = nullptr, *x64 = nullptr, *r64 = nullptr, *t64 = nullptr, *lam64 = nullptr;
     // Krylov (FP32)
     int m = 0;
     std::vector<float4*> V, Z;
+    // FP16 copies of the basis V (3D, opts.basis16) read by the multi-dot passes, and their
+    // scales (device)
+    std::vector<uint2*> V16;
+    float* dsc16 = nullptr;
     float4* w = nullptr;
     double *dscr = nullptr, *dh = nullptr, *dnrm = nullptr, *dy = nullptr, *dsig2 = nullptr;
     // host-order staging (cells + 3 face arrays)

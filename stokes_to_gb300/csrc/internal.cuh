@@ -31,13 +31,34 @@ struct Geom {
     int n = 0;
     int sx = 0, sy = 0, sz = 0;
     long long nslot = 0;
+    // division by m = n + 1 as a multiply-high and shift: with s = ceil(log2 m) and
+    // dmul = ceil(2^(31+s) / m) (below 2^32), floor(u dmul / 2^(31+s)) = floor(u / m) for
+    // every u < 2^31 (Granlund and Montgomery, "Division by invariant integers using
+    // multiplication", 1994, thm. 4.2: dmul m - 2^(31+s) < m <= 2^s). Box indices stay below
+    // 1025^3 < 2^31. dmul = 0 (a Geom not built by make) falls back to division.
+    unsigned dmul = 0;
+    int dsh = 0;  // s - 1
     __host__ __device__ int di() const { return sy * sz; }
     __host__ __device__ int dj() const { return sz; }
     __host__ __device__ int slot(int i, int j, int k) const { return ((i + 1) * sy + (j + 1)) * sz + (k + 1); }
     // slots of the logical box [0,n]^3 enumerated by a flat index t
     __host__ __device__ long long box() const { return (long long)(n + 1) * (n + 1) * (n + 1); }
+    __host__ __device__ unsigned div_m(unsigned u) const {
+#ifdef __CUDA_ARCH__
+        return __umulhi(u, dmul) >> dsh;
+#else
+        return (unsigned)(((unsigned long long)u * dmul) >> 32) >> dsh;
+#endif
+    }
     __host__ __device__ void box_ijk(long long t, int& i, int& j, int& k) const {
-        int m = n + 1;
+        const int m = n + 1;
+        if (dmul) {
+            const unsigned u = (unsigned)t, r = div_m(u), q = div_m(r);
+            k = (int)(u - r * (unsigned)m);
+            j = (int)(r - q * (unsigned)m);
+            i = (int)q;
+            return;
+        }
         k = (int)(t % m);
         long long r = t / m;
         j = (int)(r % m);
@@ -50,6 +71,13 @@ struct Geom {
         g.sy = n + 3;
         g.sz = n + 4;
         g.nslot = (long long)g.sx * g.sy * g.sz;
+        const unsigned long long m = (unsigned long long)n + 1;
+        if (n >= 1 && g.box() < (1ll << 31)) {
+            int s = 0;
+            while ((1ull << s) < m) s++;
+            g.dmul = (unsigned)(((1ull << (31 + s)) + m - 1) / m);
+            g.dsh = s - 1;
+        }
         return g;
     }
 };

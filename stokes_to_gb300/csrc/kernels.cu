@@ -4,6 +4,7 @@
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
+#include "fp64bits.cuh"
 #include "kernels.h"
 #include "stencil.cuh"
 
@@ -268,18 +269,23 @@ __global__ void k_to_f16(Geom g, const float4* __restrict__ x, const float* __re
 }
 
 // largest |x| over the box slots, as the bits of a non-negative float (atomicMax on them
-// orders as the values do)
+// orders as the values do): a grid-stride pass, one atomic per block
 __global__ void k_absmax(Geom g, const float4* __restrict__ x, unsigned* __restrict__ out) {
-    long long t = (long long)blockIdx.x * TPB + threadIdx.x;
+    __shared__ float sh[TPB / 32];
     float a = 0.f;
-    if (t < g.box()) {
+    for (long long t = (long long)blockIdx.x * TPB + threadIdx.x; t < g.box(); t += (long long)gridDim.x * TPB) {
         int i, j, k;
         g.box_ijk(t, i, j, k);
         const float4 v = __ldg(x + g.slot(i, j, k));
-        a = fmaxf(fmaxf(fabsf(v.x), fabsf(v.y)), fmaxf(fabsf(v.z), fabsf(v.w)));
+        a = fmaxf(a, fmaxf(fmaxf(fabsf(v.x), fabsf(v.y)), fmaxf(fabsf(v.z), fabsf(v.w))));
     }
     for (int o = 16; o > 0; o >>= 1) a = fmaxf(a, __shfl_xor_sync(0xffffffffu, a, o));
-    if ((threadIdx.x & 31) == 0) atomicMax(out, __float_as_uint(a));
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = a;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < TPB / 32; w++) a = fmaxf(a, sh[w]);
+        atomicMax(out, __float_as_uint(a));
+    }
 }
 
 // per-level FP16 scales: a power of two that brings the finest level's largest penalty to at
@@ -600,98 +606,157 @@ __device__ __forceinline__ F2 df_mul(F2 a, F2 b) {
     return F2{h, e - (h - p)};
 }
 
-// hi = fl32(a), lo = fl32(a - hi) componentwise
+// hi = fl32(a), lo = fl32(a - hi) componentwise (integer arithmetic, fp64bits.cuh); part
+// (optional): per-block partials of |a|^2 from the FP32 squares of the hi words, summed in
+// double-float arithmetic
+__device__ __forceinline__ F2 warp_sum_f2(F2 v) {
+    for (int o = 16; o > 0; o >>= 1) v = df_add(v, F2{__shfl_xor_sync(0xffffffffu, v.h, o), __shfl_xor_sync(0xffffffffu, v.l, o)});
+    return v;
+}
+
 __global__ void __launch_bounds__(TPB) k_split64(long long n4, const d4* __restrict__ a, float4* __restrict__ hi,
-                                                 float4* __restrict__ lo) {
+                                                 float4* __restrict__ lo, double* __restrict__ part) {
+    float acc = 0.f;
     for (long long t = (long long)blockIdx.x * TPB + threadIdx.x; t < n4; t += (long long)gridDim.x * TPB) {
         double v[4];
         load4(a, (int)t, v[0], v[1], v[2], v[3]);
         float h[4], l[4];
 #pragma unroll
-        for (int c = 0; c < 4; c++) {
-            h[c] = (float)v[c];
-            l[c] = (float)(v[c] - (double)h[c]);
-        }
+        for (int c = 0; c < 4; c++) split_bits(v[c], h[c], l[c]);
         if (hi) hi[t] = make_float4(h[0], h[1], h[2], h[3]);
         lo[t] = make_float4(l[0], l[1], l[2], l[3]);
+        acc += h[0] * h[0] + h[1] * h[1] + h[2] * h[2] + h[3] * h[3];
+    }
+    if (part) {
+        __shared__ F2 sh[TPB / 32];
+        const F2 v = warp_sum_f2(f2(acc, 0.f));
+        if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            F2 b = sh[0];
+            for (int w = 1; w < TPB / 32; w++) b = df_add(b, sh[w]);
+            part[blockIdx.x] = f2d_bits(b.h) + f2d_bits(b.l);
+        }
     }
 }
 
 // r = b - A x in the Laplacian form (rows of fixed unknowns 0, x zero on fixed unknowns),
-// double-float arithmetic, r in FP64, per-block partials of |r|^2
+// double-float arithmetic; HAS_X false: x = 0 (r = b). r in FP64 (r64), or rounded to FP32
+// (r32, what the Krylov basis is built from). Per-block partials of |r|^2, summed in
+// double-float arithmetic from the FP32 squares of the residual's high words.
+template <bool HAS_X>
 __global__ void __launch_bounds__(TPB) k_resid_df(Geom g, F2 vol, const float4* __restrict__ xh, const float4* __restrict__ xl,
                                                   const float4* __restrict__ bh, const float4* __restrict__ bl,
                                                   const float4* __restrict__ Ph, const float4* __restrict__ Pl,
-                                                  const uint8_t* __restrict__ m, d4* __restrict__ r, double* __restrict__ part) {
+                                                  const uint8_t* __restrict__ m, d4* __restrict__ r64, float4* __restrict__ r32,
+                                                  double* __restrict__ part) {
     const long long t = (long long)blockIdx.x * TPB + threadIdx.x;
     float acc = 0.f;
     if (t < g.box()) {
         int i, j, k;
         g.box_ijk(t, i, j, k);
         const int s = g.slot(i, j, k);
-        auto ld = [&](int q, F2 (&v)[4]) {
-            const float4 a = __ldg(xh + q), b = __ldg(xl + q);
-            v[0] = f2(a.x, b.x);
-            v[1] = f2(a.y, b.y);
-            v[2] = f2(a.z, b.z);
-            v[3] = f2(a.w, b.w);
-        };
-        F2 c[4], xm[4], xp[4], ym[4], yp[4], zm[4], zp[4];
-        ld(s, c);
-        ld(s - g.di(), xm);
-        ld(s + g.di(), xp);
-        ld(s - g.dj(), ym);
-        ld(s + g.dj(), yp);
-        ld(s - 1, zm);
-        ld(s + 1, zp);
-        const float4 ph = __ldg(Ph + s), pl = __ldg(Pl + s), b0 = __ldg(bh + s), b1 = __ldg(bl + s);
-        const F2 pen[4] = {f2(ph.x, pl.x), f2(ph.y, pl.y), f2(ph.z, pl.z), f2(ph.w, pl.w)};
+        const float4 b0 = __ldg(bh + s), b1 = __ldg(bl + s);
         const F2 bb[4] = {f2(b0.x, b1.x), f2(b0.y, b1.y), f2(b0.z, b1.z), f2(b0.w, b1.w)};
-        const F2 six = f2(6.f, 0.f);
-        // the rows of stencil.cuh lap_core
-        const F2 div = df_add(df_add(df_sub(xp[1], c[1]), df_sub(yp[2], c[2])), df_sub(zp[3], c[3]));
-        F2 o[4];
-        o[0] = df_add(df_mul(vol, div), df_mul(pen[0], c[0]));
-        const F2* lo_nb[3] = {xm, ym, zm};
+        F2 o[4] = {f2(0.f, 0.f), f2(0.f, 0.f), f2(0.f, 0.f), f2(0.f, 0.f)};
+        if (HAS_X) {
+            auto ld = [&](int q, F2 (&v)[4]) {
+                const float4 a = __ldg(xh + q), b = __ldg(xl + q);
+                v[0] = f2(a.x, b.x);
+                v[1] = f2(a.y, b.y);
+                v[2] = f2(a.z, b.z);
+                v[3] = f2(a.w, b.w);
+            };
+            F2 c[4], xm[4], xp[4], ym[4], yp[4], zm[4], zp[4];
+            ld(s, c);
+            ld(s - g.di(), xm);
+            ld(s + g.di(), xp);
+            ld(s - g.dj(), ym);
+            ld(s + g.dj(), yp);
+            ld(s - 1, zm);
+            ld(s + 1, zp);
+            const float4 ph = __ldg(Ph + s), pl = __ldg(Pl + s);
+            const F2 pen[4] = {f2(ph.x, pl.x), f2(ph.y, pl.y), f2(ph.z, pl.z), f2(ph.w, pl.w)};
+            const F2 six = f2(6.f, 0.f);
+            // the rows of stencil.cuh lap_core
+            const F2 div = df_add(df_add(df_sub(xp[1], c[1]), df_sub(yp[2], c[2])), df_sub(zp[3], c[3]));
+            o[0] = df_add(df_mul(vol, div), df_mul(pen[0], c[0]));
+            const F2* lo_nb[3] = {xm, ym, zm};
 #pragma unroll
-        for (int d = 1; d <= 3; d++) {
-            F2 l = df_mul(six, c[d]);
-            l = df_sub(l, df_add(xm[d], xp[d]));
-            l = df_sub(l, df_add(ym[d], yp[d]));
-            l = df_sub(l, df_add(zm[d], zp[d]));
-            const F2 gp = df_sub(c[0], lo_nb[d - 1][0]);
-            o[d] = df_add(df_mul(vol, df_sub(l, gp)), df_mul(pen[d], c[d]));
+            for (int d = 1; d <= 3; d++) {
+                F2 l = df_mul(six, c[d]);
+                l = df_sub(l, df_add(xm[d], xp[d]));
+                l = df_sub(l, df_add(ym[d], yp[d]));
+                l = df_sub(l, df_add(zm[d], zp[d]));
+                const F2 gp = df_sub(c[0], lo_nb[d - 1][0]);
+                o[d] = df_add(df_mul(vol, df_sub(l, gp)), df_mul(pen[d], c[d]));
+            }
         }
         const uint8_t ms = __ldg(m + s);
         const uint8_t bit[4] = {MP, MU, MV, MW};
-        double rv[4];
+        F2 rd[4];
 #pragma unroll
         for (int q = 0; q < 4; q++) {
-            const F2 d = df_sub(bb[q], o[q]);
-            rv[q] = (ms & bit[q]) ? 0.0 : (double)d.h + (double)d.l;
-            const float f = (ms & bit[q]) ? 0.f : d.h;
-            acc += f * f;
+            rd[q] = (ms & bit[q]) ? f2(0.f, 0.f) : df_sub(bb[q], o[q]);
+            acc += rd[q].h * rd[q].h;
         }
-        store4(r, s, rv[0], rv[1], rv[2], rv[3]);
+        if (r32) {
+            r32[s] = make_float4(rd[0].h, rd[1].h, rd[2].h, rd[3].h);
+        } else {
+            double rv[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) rv[q] = f2d_bits(rd[q].h) + f2d_bits(rd[q].l);
+            store4(r64, s, rv[0], rv[1], rv[2], rv[3]);
+        }
     }
     if (part) {
-        const double v = block_sum((double)acc);
-        if (threadIdx.x == 0) part[blockIdx.x] = v;
+        __shared__ F2 sh[TPB / 32];
+        const F2 v = warp_sum_f2(f2(acc, 0.f));
+        if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            F2 b = sh[0];
+            for (int w = 1; w < TPB / 32; w++) b = df_add(b, sh[w]);
+            part[blockIdx.x] = f2d_bits(b.h) + f2d_bits(b.l);
+        }
     }
 }
 
-int split64(cudaStream_t st, long long n4, const d4* a, float4* hi, float4* lo) {
-    k_split64<<<grid_for(n4, TPB) > 4096 ? 4096 : grid_for(n4, TPB), TPB, 0, st>>>(n4, a, hi, lo);
+// x = hi + lo in FP64 (one FP64 addition per element; the conversions by integer arithmetic)
+__global__ void __launch_bounds__(TPB) k_df_to_f64(long long n4, const float4* __restrict__ hi, const float4* __restrict__ lo,
+                                                   d4* __restrict__ x) {
+    for (long long t = (long long)blockIdx.x * TPB + threadIdx.x; t < n4; t += (long long)gridDim.x * TPB) {
+        const float4 h = __ldg(hi + t), l = __ldg(lo + t);
+        store4(x, (int)t, f2d_bits(h.x) + f2d_bits(l.x), f2d_bits(h.y) + f2d_bits(l.y), f2d_bits(h.z) + f2d_bits(l.z),
+               f2d_bits(h.w) + f2d_bits(l.w));
+    }
+}
+
+int split64(cudaStream_t st, long long n4, const d4* a, float4* hi, float4* lo, double* part, int* nblocks_out) {
+    const unsigned nb = grid_for(n4, TPB) > 4096 ? 4096 : grid_for(n4, TPB);
+    if (nblocks_out) *nblocks_out = (int)nb;
+    k_split64<<<nb, TPB, 0, st>>>(n4, a, hi, lo, part);
     STG_LAUNCH_CK();
     return STG_OK;
 }
 
 int resid64_df(cudaStream_t st, const Geom& g, double vol, const float4* xh, const float4* xl, const float4* bh, const float4* bl,
-               const float4* Ph, const float4* Pl, const uint8_t* m, d4* r, double* part, int* nblocks_out) {
+               const float4* Ph, const float4* Pl, const uint8_t* m, d4* r, float4* r32, double* part, int* nblocks_out) {
     const unsigned nb = grid_for(g.box(), TPB);
     if (nblocks_out) *nblocks_out = (int)nb;
     const float vh = (float)vol;
-    k_resid_df<<<nb, TPB, 0, st>>>(g, F2{vh, (float)(vol - (double)vh)}, xh, xl, bh, bl, Ph, Pl, m, r, part);
+    const F2 v2{vh, (float)(vol - (double)vh)};
+    if (xh)
+        k_resid_df<true><<<nb, TPB, 0, st>>>(g, v2, xh, xl, bh, bl, Ph, Pl, m, r, r32, part);
+    else
+        k_resid_df<false><<<nb, TPB, 0, st>>>(g, v2, xh, xl, bh, bl, Ph, Pl, m, r, r32, part);
+    STG_LAUNCH_CK();
+    return STG_OK;
+}
+
+int df_to_f64(cudaStream_t st, long long n4, const float4* hi, const float4* lo, d4* x) {
+    const unsigned nb = grid_for(n4, TPB);
+    k_df_to_f64<<<nb > 4096 ? 4096 : nb, TPB, 0, st>>>(n4, hi, lo, x);
     STG_LAUNCH_CK();
     return STG_OK;
 }
@@ -790,7 +855,8 @@ int to_f16(cudaStream_t st, const Geom& g, const float4* x, const float* scale, 
 
 int penalty_scales(cudaStream_t st, const Geom& fine, const float4* P, int nlev, unsigned* scratch, float* scale) {
     STG_CK(cudaMemsetAsync(scratch, 0, sizeof(unsigned), st));
-    k_absmax<<<grid_for(fine.box(), TPB), TPB, 0, st>>>(fine, P, scratch);
+    const unsigned nb = grid_for(fine.box(), TPB);
+    k_absmax<<<nb > 1216 ? 1216 : nb, TPB, 0, st>>>(fine, P, scratch);
     STG_LAUNCH_CK();
     k_pscale<<<1, 1, 0, st>>>(nlev, scratch, scale);
     STG_LAUNCH_CK();

@@ -35,11 +35,14 @@ int sweep_status(cudaStream_t st, int* timed_out);
 int restrict_resid32(cudaStream_t st, const Geom& gc, const Geom& gf, float volf, const float4* rf, const float4* xf,
                      const uint8_t* mf, const float4* Pf, const uint8_t* mc, float4* rc, bool lap = false);
 // Double-float (hi + lo FP32 words) copies of FP64 vectors and the FP64 residual from them:
-// hi = fl32(a), lo = fl32(a - hi) (hi may be null); r = b - A x in the Laplacian form with
-// per-block partials of |r|^2 (FP32 per slot, FP64 block sums)
-int split64(cudaStream_t st, long long n4, const d4* a, float4* hi, float4* lo);
+// hi = fl32(a), lo = fl32(a - hi) (hi may be null; part: block partials of |a|^2, 4096 at
+// most, their count to *nblocks_out); r = b - A x in the Laplacian form (xh
+// null: x = 0) into r (FP64) or, when r32 is non-null, rounded to FP32 into r32, with
+// per-block partials of |r|^2 (FP32 per slot, double-float block sums); x = hi + lo in FP64
+int split64(cudaStream_t st, long long n4, const d4* a, float4* hi, float4* lo, double* part = nullptr, int* nblocks_out = nullptr);
 int resid64_df(cudaStream_t st, const Geom& g, double vol, const float4* xh, const float4* xl, const float4* bh, const float4* bl,
-               const float4* Ph, const float4* Pl, const uint8_t* m, d4* r, double* part, int* nblocks_out);
+               const float4* Ph, const float4* Pl, const uint8_t* m, d4* r, float4* r32, double* part, int* nblocks_out);
+int df_to_f64(cudaStream_t st, long long n4, const float4* hi, const float4* lo, d4* x);
 // 1 in *flag (device) when x is nonzero on some fixed or absent unknown of the box, else 0
 int fixed_nonzero(cudaStream_t st, const Geom& g, const d4* x, const uint8_t* m, int* flag);
 // x_f = 0 on every fixed or absent unknown of the box
@@ -87,9 +90,13 @@ int half_square64(cudaStream_t st, long long n4, const d4* x, d4* out);
 // ---------------------------------------------------------------- vectors (blas.cu)
 int fill_bytes(cudaStream_t st, void* p, size_t bytes);
 int f64_to_f32(cudaStream_t st, long long n4, const d4* a, double scale, float4* out);
+// out = a * scale for an FP32 vector of norm 1 / scale, also writing out's FP16 copy (four
+// halves per slot: the vector times a scale) and that scale to *sc_out (device)
+int scale_h16(cudaStream_t st, long long n4, const float4* a, float scale, float4* out, uint2* out16, float* sc_out);
 int f32_to_f64(cudaStream_t st, long long n4, const float4* a, d4* out);
 // x64 += alpha * sum_j y[j] z[j]  (z FP32 vectors), y on device (nz entries); with xh / xl
-// non-null also writes the double-float copy of the new x there; with e non-null the FP32
+// non-null also writes the double-float copy of the new x there; with x null, (xh, xl) is
+// the iterate and takes the sum in double-float arithmetic; with e non-null the FP32
 // value of sum_j y[j] z[j] goes to e, which may be one of z[j] for j >= axpy_last_chunk(nz)
 int axpy_multi_32to64(cudaStream_t st, long long n4, const float4* const* z, const double* y, int nz, double alpha, d4* x,
                       float4* xh = nullptr, float4* xl = nullptr, float4* e = nullptr);
@@ -101,19 +108,24 @@ int axpy_last_chunk(int nz);
 int multidot32(cudaStream_t st, long long n4, const float4* const* v, int nv, const float4* w, double* h, double* scratch,
                double* ww);
 // w = v - A z (Laplacian form, slot layout of g) fused with h[q] = <V_q, w> (q < nv) and
-// <w, w> into *ww (device)
+// <w, w> into *ww (device). With V16 the first 16 dots read the vectors' FP16 copies
+// instead, scaled back by 1 / sc[q] (sc on the device).
 int shift_multidot32(cudaStream_t st, const Geom& g, float vol, const float4* v, const float4* z, const uint8_t* m, const float4* P,
-                     long long n4, const float4* const* V, int nv, float4* w, double* h, double* scratch, double* ww);
+                     long long n4, const float4* const* V, int nv, float4* w, double* h, double* scratch, double* ww,
+                     const uint2* const* V16 = nullptr, const float* sc = nullptr);
 // w -= sum_j h[j] v_j ; then returns ||w||^2 into nrm2 (device)
 int multiaxpy32_norm(cudaStream_t st, long long n4, const float4* const* v, int nv, const double* h, float4* w, double* nrm2,
                      double* scratch);
 // Classical Gram-Schmidt projection on unnormalised basis vectors in one pass:
 // out = w - sum_q sig2[q] d[q] v_q (d, sig2 on the device; out may alias w); ||out||^2
-// into *nrm2 and, when dots != nullptr, <v_q, out> into dots[0..nv) (device).
+// into *nrm2 and, when dots != nullptr, <v_q, out> into dots[0..nv) (device). With out16,
+// also the FP16 copy of out, scaled for an out of squared norm at most *nest, the scale to
+// *sc_out (nest, sc_out on the device).
 int project32(cudaStream_t st, long long n4, const float4* const* v, int nv, const double* d, const double* sig2, const float4* w,
-              float4* out, double* dots, double* nrm2, double* scratch);
-// out = x / sqrt(*nrm2)
-int scale32(cudaStream_t st, long long n4, float4* x, const double* nrm2, float4* out);
+              float4* out, double* dots, double* nrm2, double* scratch, uint2* out16 = nullptr, const double* nest = nullptr,
+              float* sc_out = nullptr);
+// out = x / sqrt(*nrm2); with sc, the scale of x's FP16 copy follows (*sc *= sqrt(*nrm2))
+int scale32(cudaStream_t st, long long n4, float4* x, const double* nrm2, float4* out, float* sc = nullptr);
 // deterministic sum of nparts partials -> *out
 int reduce_parts(cudaStream_t st, const double* parts, int nparts, double* out);
 int dot64(cudaStream_t st, long long n4, const d4* a, const d4* b, double* out, double* scratch);

@@ -359,11 +359,17 @@ int vcycle(stg_t* h, const float4* rhs) {
 int residual64(stg_t* h, const d4* b, const d4* x, d4* r, double* nrm2_host) {
     Level& F = fine(h);
     int nb = 0;
-    if (x && x == h->df_x && b == h->df_b && fast(h, F))
-        PROF(h, 5, 129.0 * F.g.box(),
-             resid64_df(h->st, F.g, F.vol, h->xh, h->xl, h->bh, h->bl, F.P32, h->Plo, F.m, r, h->d_parts, &nb));
-    else
+    h->r32_ok = false;
+    if ((!x || x == h->df_x) && b == h->df_b && fast(h, F)) {
+        // the solve's iterate is the double-float pair (xh, xl): the residual, rounded to
+        // FP32 (the Krylov basis is built from it), goes to h->w
+        PROF(h, 5, (x ? 113.0 : 49.0) * F.g.box(),
+             resid64_df(h->st, F.g, F.vol, x ? h->xh : nullptr, x ? h->xl : nullptr, h->bh, h->bl, F.P32, h->Plo, F.m, nullptr, h->w,
+                        h->d_parts, &nb));
+        h->r32_ok = true;
+    } else {
         PROF(h, 5, (x ? 129.0 : 65.0) * F.g.box(), op64(h->st, F.g, F.vol, x, F.m, F.P64, b, r, 1, h->d_parts, &nb, fast(h, F)));
+    }
     STG_TRY(reduce_parts(h->st, h->d_parts, nb, h->dnrm));
     STG_CK(cudaMemcpyAsync(nrm2_host, h->dnrm, sizeof(double), cudaMemcpyDeviceToHost, h->st));
     STG_CK(cudaStreamSynchronize(h->st));
@@ -438,10 +444,16 @@ int solve_core(stg_t* h, const d4* b, d4* x, stg_stats* stats) {
         S.setup_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     }
     STG_CK(cudaEventRecord(h->e0, h->st));
+    // 3D Laplacian form: the iterate is kept as a double-float pair (xh, xl) during the solve
+    // (FP32 arithmetic only: GB300's FP64 pipe is far slower than HBM for per-element work)
+    // and formed in FP64 once at the end; b is split the same way for the FP64 residual
+    const bool df = h->dim == 3 && fast(h, fine(h));
+    // the fused operator + multi-dot pass (3D uniform form) reads the basis's FP16 copies
+    const bool h16 = df && !h->V16.empty();
     // zero initial guess as the reference, or the previous solution of this equation
     if (h->opts.warm_start && h->has_x0(x)) {
-        if (h->dim == 3 && fast(h, fine(h))) STG_TRY(zero_fixed(h->st, fine(h).g, fine(h).m, x));
-    } else {
+        if (df) STG_TRY(zero_fixed(h->st, fine(h).g, fine(h).m, x));
+    } else if (!df) {
         STG_CK(cudaMemsetAsync(x, 0, sizeof(d4) * n4, h->st));
     }
     if (h->opts.method == STG_METHOD_LEARNED && !h->net) {
@@ -449,8 +461,25 @@ int solve_core(stg_t* h, const d4* b, d4* x, stg_stats* stats) {
         return STG_E_INVALID;
     }
     h->net_on = h->opts.method == STG_METHOD_LEARNED;
+    // a zero start makes the first residual b itself (fixed rows cleared in the Laplacian form)
+    bool x_zero = !(h->opts.warm_start && h->has_x0(x));
+    h->df_x = h->df_b = nullptr;
     double bn2 = 0;
-    STG_TRY(dot64(h->st, n4, b, b, h->dnrm, h->dscr));
+    if (df) {
+        if (x_zero) {
+            STG_CK(cudaMemsetAsync(h->xh, 0, sizeof(float4) * n4, h->st));
+            STG_CK(cudaMemsetAsync(h->xl, 0, sizeof(float4) * n4, h->st));
+        } else {
+            PROF(h, 6, 64.0 * n4, split64(h->st, n4, x, h->xh, h->xl));
+        }
+        int nbp = 0;  // ||b||^2 from the same pass
+        PROF(h, 6, 64.0 * n4, split64(h->st, n4, b, h->bh, h->bl, h->d_parts, &nbp));
+        STG_TRY(reduce_parts(h->st, h->d_parts, nbp, h->dnrm));
+        h->df_x = x;
+        h->df_b = b;
+    } else {
+        STG_TRY(dot64(h->st, n4, b, b, h->dnrm, h->dscr));
+    }
     STG_CK(cudaMemcpyAsync(&bn2, h->dnrm, sizeof(double), cudaMemcpyDeviceToHost, h->st));
     STG_CK(cudaStreamSynchronize(h->st));
     const double bn = std::sqrt(bn2);
@@ -476,22 +505,6 @@ int solve_core(stg_t* h, const d4* b, d4* x, stg_stats* stats) {
     std::vector<double> H((size_t)(m + 1) * m), cs(m), sn(m), g(m + 1), y(m), hcol(m + 2), sig(m + 1);
     double rel = 0, rn = 0;
     int status = STG_E_NOT_CONVERGED;
-    // a zero start makes the first residual b itself (fixed rows cleared in the Laplacian form)
-    bool x_zero = !(h->opts.warm_start && h->has_x0(x));
-    // double-float copies of x and b for the FP64 residual (3D Laplacian form)
-    const bool df = h->dim == 3 && fast(h, fine(h));
-    h->df_x = h->df_b = nullptr;
-    if (df) {
-        if (x_zero) {
-            STG_CK(cudaMemsetAsync(h->xh, 0, sizeof(float4) * n4, h->st));
-            STG_CK(cudaMemsetAsync(h->xl, 0, sizeof(float4) * n4, h->st));
-        } else {
-            PROF(h, 6, 64.0 * n4, split64(h->st, n4, x, h->xh, h->xl));
-        }
-        PROF(h, 6, 64.0 * n4, split64(h->st, n4, b, h->bh, h->bl));
-        h->df_x = x;
-        h->df_b = b;
-    }
     for (int outer = 0; outer <= h->opts.max_outer; outer++) {
         double rn2 = 0;
         STG_TRY(h->resid64(h, b, (outer == 0 && x_zero && h->dim == 3) ? nullptr : x, h->r64, &rn2));
@@ -501,7 +514,7 @@ int solve_core(stg_t* h, const d4* b, d4* x, stg_stats* stats) {
             // a lot, e.g. when it first turns into a channel): start from zero instead
             if (h->opts.verbose) fprintf(stderr, "[stg] warm start rejected (||b-Ax0||/||b|| = %.3e)\n", bn > 0 ? rn / bn : 0.0);
             x_zero = true;
-            STG_CK(cudaMemsetAsync(x, 0, sizeof(d4) * n4, h->st));
+            if (!df) STG_CK(cudaMemsetAsync(x, 0, sizeof(d4) * n4, h->st));
             if (df) {
                 STG_CK(cudaMemsetAsync(h->xh, 0, sizeof(float4) * n4, h->st));
                 STG_CK(cudaMemsetAsync(h->xl, 0, sizeof(float4) * n4, h->st));
@@ -523,7 +536,12 @@ int solve_core(stg_t* h, const d4* b, d4* x, stg_stats* stats) {
         if (outer == h->opts.max_outer) break;
         S.outer_iters++;
         // v0 = r / ||r|| in FP32
-        PROF(h, 6, 48.0 * n4, f64_to_f32(h->st, n4, h->r64, 1.0 / rn, h->V[0]));
+        if (h->r32_ok && h16)
+            PROF(h, 6, 40.0 * n4, scale_h16(h->st, n4, h->w, (float)(1.0 / rn), h->V[0], h->V16[0], h->dsc16));
+        else if (h->r32_ok)
+            PROF(h, 6, 32.0 * n4, scale32(h->st, n4, h->w, h->dnrm, h->V[0]));
+        else
+            PROF(h, 6, 48.0 * n4, f64_to_f32(h->st, n4, h->r64, 1.0 / rn, h->V[0]));
         double beta = 1.0;
         // ask this step for what the target still needs, within [inner_tol / 10, inner_tol]
         const double itol = std::min(h->opts.inner_tol, std::max(0.3 * h->opts.tol / rel, 0.1 * h->opts.inner_tol));
@@ -553,15 +571,19 @@ int solve_core(stg_t* h, const d4* b, d4* x, stg_stats* stats) {
             if (h->dim == 3 && fast(h, fine(h))) {
                 // one pass: the operator and the first multi-dot (w is not re-read)
                 Level& F = fine(h);
-                PROF(h, 6, (65.0 + 16.0 * (j + 1)) * F.g.box(),
+                const int nh = h16 ? std::min(j + 1, 16) : 0;  // dots read from the FP16 copies
+                PROF(h, 6, (65.0 + 16.0 * (j + 1) - 8.0 * nh) * F.g.box(),
                      shift_multidot32(h->st, F.g, (float)F.vol, h->V[j], h->Z[j], F.m, F.P32, n4, h->V.data(), j + 1, h->w, h->dh,
-                                      h->dscr, h->dnrm + 1));
+                                      h->dscr, h->dnrm + 1, h16 ? h->V16.data() : nullptr, h->dsc16));
             } else {
                 STG_TRY(h->shift32(h, h->V[j], h->Z[j], h->w));
                 PROF(h, 6, 16.0 * (j + 2) * n4, multidot32(h->st, n4, h->V.data(), j + 1, h->w, h->dh, h->dscr, h->dnrm + 1));
             }
-            PROF(h, 6, 16.0 * (j + 3) * n4,
-                 project32(h->st, n4, h->V.data(), j + 1, h->dh, h->dsig2, h->w, h->V[j + 1], h->dh + m + 2, h->dnrm, h->dscr));
+            // the new vector's FP16 copy is scaled for a norm up to ||w|| (the projection only
+            // shortens w); a second projection rewrites it for its own input's norm
+            PROF(h, 6, (16.0 * (j + 3) + (h16 ? 8.0 : 0.0)) * n4,
+                 project32(h->st, n4, h->V.data(), j + 1, h->dh, h->dsig2, h->w, h->V[j + 1], h->dh + m + 2, h->dnrm, h->dscr,
+                           h16 ? h->V16[j + 1] : nullptr, h->dnrm + 1, h->dsc16 + j + 1));
             std::vector<double> h1(j + 1), h2(j + 1, 0.0);
             double nrm[2] = {0, 0};
             STG_CK(cudaMemcpyAsync(h1.data(), h->dh, sizeof(double) * (j + 1), cudaMemcpyDeviceToHost, h->st));
@@ -570,9 +592,9 @@ int solve_core(stg_t* h, const d4* b, d4* x, stg_stats* stats) {
             STG_CK(cudaStreamSynchronize(h->st));
             double nw2 = nrm[0];
             if (nrm[0] < 0.01 * nrm[1]) {
-                PROF(h, 6, 16.0 * (j + 3) * n4,
+                PROF(h, 6, (16.0 * (j + 3) + (h16 ? 8.0 : 0.0)) * n4,
                      project32(h->st, n4, h->V.data(), j + 1, h->dh + m + 2, h->dsig2, h->V[j + 1], h->V[j + 1], nullptr, h->dnrm,
-                               h->dscr));
+                               h->dscr, h16 ? h->V16[j + 1] : nullptr, h->dnrm, h->dsc16 + j + 1));
                 STG_CK(cudaMemcpyAsync(&nw2, h->dnrm, sizeof(double), cudaMemcpyDeviceToHost, h->st));
                 STG_CK(cudaStreamSynchronize(h->st));
             } else {
@@ -592,7 +614,7 @@ int solve_core(stg_t* h, const d4* b, d4* x, stg_stats* stats) {
                 // the unnormalised basis drifts in scale by the gain of A M each step (large
                 // for a weak preconditioner on high-contrast designs): renormalise before FP32
                 // over- or underflows
-                PROF(h, 6, 32.0 * n4, scale32(h->st, n4, h->V[j + 1], h->dnrm, h->V[j + 1]));
+                PROF(h, 6, 32.0 * n4, scale32(h->st, n4, h->V[j + 1], h->dnrm, h->V[j + 1], h16 ? h->dsc16 + j + 1 : nullptr));
                 sig[j + 1] = 1.0;
                 const double one1 = 1.0;
                 STG_CK(cudaMemcpyAsync(h->dsig2 + j + 1, &one1, sizeof(double), cudaMemcpyHostToDevice, h->st));
@@ -651,12 +673,14 @@ int solve_core(stg_t* h, const d4* b, d4* x, stg_stats* stats) {
             have_aug = std::min(naug, have_aug + 1);
         }
         PROF(h, 6, (16.0 * k + 64.0 + (keep ? 16.0 : 0.0)) * n4,
-             axpy_multi_32to64(h->st, n4, h->Z.data(), h->dy, k, rn, x, df ? h->xh : nullptr, df ? h->xl : nullptr, keep));
+             axpy_multi_32to64(h->st, n4, h->Z.data(), h->dy, k, rn, df ? nullptr : x, df ? h->xh : nullptr, df ? h->xl : nullptr,
+                               keep));
         // a stalled step means the V-cycle is too weak for this design (high-contrast
         // optimised densities): the rest of the solve smooths twice per colour (about 1.5x
         // the V-cycle's cost for 1.5-2x fewer V-cycles there)
         if (h->dim == 3 && stalled) h->boost = stalled_any = true;
     }
+    if (df) PROF(h, 6, 64.0 * n4, df_to_f64(h->st, n4, h->xh, h->xl, x));  // the iterate in FP64
     h->df_x = h->df_b = nullptr;  // finish() changes x; adapters must not see the copies
     if (h->finish) STG_TRY(h->finish(h, b, x));
     int sweep_timeout = 0;
@@ -731,6 +755,7 @@ void stg_default_opts(stg_opts* o) {
     o->smooth_sweeps = 1;
     o->warm_start = 0;
     o->prolong = 0;
+    o->basis16 = 1;
 }
 
 const char* stg_last_error(void) { return g_err; }
@@ -876,6 +901,12 @@ int stg_create(int dim, int n, const stg_opts* opts, stg_t** out) {
         if ((rc = dalloc(&p, ns))) return fail(rc);
     for (auto& p : h->Z)
         if ((rc = dalloc(&p, ns))) return fail(rc);
+    if (dim == 3 && h->opts.basis16) {
+        h->V16.assign(h->m + 1, nullptr);
+        for (auto& p : h->V16)
+            if ((rc = dalloc(&p, ns))) return fail(rc);
+        if ((rc = dalloc(&h->dsc16, (size_t)h->m + 1))) return fail(rc);
+    }
     if ((rc = dalloc(&h->dscr, 1216 * 18)) || (rc = dalloc(&h->dh, 2 * (h->m + 2))) || (rc = dalloc(&h->dnrm, 8)) ||
         (rc = dalloc(&h->dsig2, h->m + 2)) ||
         (rc = dalloc(&h->dy, h->m + 1)) || (rc = dalloc(&h->d_parts, (size_t)nparts + 1216)) || (rc = dalloc(&h->dflag, 1)))
@@ -924,6 +955,8 @@ int stg_destroy(stg_t* h) {
     cudaFree(h->d_pscale);
     cudaFree(h->d_pmax);
     for (auto p : h->V) cudaFree(p);
+    for (auto p : h->V16) cudaFree(p);
+    cudaFree(h->dsc16);
     for (auto p : h->Z) cudaFree(p);
     for (double* p : {h->dscr, h->dh, h->dnrm, h->dy, h->dsig2, h->stage, h->d_design, h->d_phys, h->d_sens, h->d_sens_design, h->d_vw,
                       h->d_tmp, h->d_gauss, h->d_parts, h->d_wsum})

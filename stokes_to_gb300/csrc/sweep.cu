@@ -751,7 +751,7 @@ __global__ void __launch_bounds__(NT, PB ? 4 : 3) k_sweep_tma(const __grid_const
     const int n = g.n;
     const int tk = threadIdx.x, tj = threadIdx.y, tid = tj * SK + tk;
     const int k0 = blockIdx.x * SK, j0 = blockIdx.y * SJ, i0 = blockIdx.z * chunk;
-    const int i1 = min(i0 + chunk, n + 1);
+    const int i1 = i0 + chunk >= n ? n + 1 : i0 + chunk;  // the last chunk also takes plane n
     const int j = j0 + tj, k = k0 + tk;
     const float v6 = 6.f * vol;
 
@@ -782,9 +782,9 @@ __global__ void __launch_bounds__(NT, PB ? 4 : 3) k_sweep_tma(const __grid_const
     const bool out_ok = j <= n && k <= n;
     const long long out_jk = (long long)(j + 1) * g.sz + (k + 1);
     const int oxi = (tj + 2) * XK + (tk + 2), ori = (tj + 1) * RK + (tk + 1), odi = (tj + 1) * DK + (tk + 1);
-    const bool jk_cell = j < n && k < n;
-    const int opar = (j + k + flag) & 1;  // own colour is red when ((i & 1) ^ opar) == 0
-    const bool lo_j_ok = j >= 1 && k < n, lo_k_ok = k >= 1 && j < n;
+    // the grid's tiles cover [0, n) in j and k: where a tile ends at n, its last lane in k
+    // (last row in j) also writes the slot at k = n (j = n)
+    const bool ext_k = tk == SK - 1 && k + 1 == n && j <= n, ext_j = tj == SJ - 1 && j + 1 == n && k <= n;
 
     // plane p of x (region origin j0-2, k0-2) or of r / P (origin j0-1, k0-1) into a ring
     // slot by one TMA box load each; out-of-allocation parts of a box read as zero
@@ -878,6 +878,43 @@ __global__ void __launch_bounds__(NT, PB ? 4 : 3) k_sweep_tma(const __grid_const
     }
     int mm1 = 0 * XN, m0 = 1 * XN, m1 = 2 * XN, m2 = 3 * XN;  // masks of planes i-1 .. i+2
 
+    // new x of slot (i, jj, kk) of the current plane (x / mask index xi, rr / P index ri,
+    // dp index di of its own cell), written to dst: the pressure of an own red cell, and
+    // each face whose red block is the own cell (red) or the cell below it (the own cell
+    // black). dp is read only where that red cell exists, so the high-side slots (jj or
+    // kk = n) read nothing outside the dp region; dpp (the cell below in i) only for the
+    // thread's own (j, k).
+    auto update = [&](int i, int jj, int kk, int xi, int ri, int di, float4* dst) {
+        float4 xo = HAS_X ? S.x[x0 + xi] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float4 rv = RR[rr0 + ri], pv = ldv(S.P[p0 + ri], psc);
+        const uint8_t mo = S.m[m0 + xi];
+        const bool jkc = jj < n && kk < n;
+        const bool own_col = ((i + jj + kk + flag) & 1) == 0;
+        const bool own_red = jkc && i < n && own_col;
+        const float dpown = own_red ? S.dp[di] : 0.f;
+        if (own_red) xo.x += dpown;
+        // the lower cells have the other colour: red exactly when the own colour is black
+        const bool lo_ok[3] = {!own_col && i >= 1 && jkc, !own_col && jj >= 1 && kk < n && i < n,
+                               !own_col && kk >= 1 && jj < n && i < n};
+        const float dplo[3] = {lo_ok[0] ? S.dpp[tid] : 0.f, lo_ok[1] ? S.dp[di - DK] : 0.f, lo_ok[2] ? S.dp[di - 1] : 0.f};
+        const float rf[3] = {rv.y, rv.z, rv.w}, pf[3] = {pv.y, pv.z, pv.w};
+        const uint8_t bit[3] = {MU, MV, MW};
+        float upd[3];
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+            upd[d] = 0.f;
+            if (!own_red && !lo_ok[d]) continue;
+            const bool fix = mo & bit[d];
+            const float v = fix ? 0.f : vol;
+            const float D = fix ? 1.f : v6 + pf[d];
+            upd[d] = __fdividef(rf[d] - (own_red ? -v : v) * (own_red ? dpown : dplo[d]), D);
+        }
+        xo.y += upd[0];
+        xo.z += upd[1];
+        xo.w += upd[2];
+        *dst = xo;
+    };
+
     // prologue: planes i0-2 .. i0+1 of x, i0-1 .. i0+1 of P, i0-1 and i0 of r, masks i0-1 .. i0+2
     if (tid == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar) : "memory");
@@ -961,33 +998,12 @@ __global__ void __launch_bounds__(NT, PB ? 4 : 3) k_sweep_tma(const __grid_const
         pressure(i, rr0, rrm1, p0, p1, m0, m1);
         __syncthreads();
         if (out_ok) {
-            float4 xo = HAS_X ? S.x[x0 + oxi] : make_float4(0.f, 0.f, 0.f, 0.f);
-            const float4 rv = RR[rr0 + ori], pv = ldv(S.P[p0 + ori], psc);
-            const uint8_t mo = S.m[m0 + oxi];
-            const bool cell = jk_cell && i < n;
-            const bool own_col = ((i & 1) ^ opar) == 0;  // (i + j + k + flag) even
-            const bool own_red = cell && own_col;
-            const float dpown = S.dp[odi];
-            if (own_red) xo.x += dpown;
-            // the lower cells have the other colour: red exactly when the own colour is black
-            const bool lo_ok[3] = {!own_col && i >= 1 && jk_cell, !own_col && lo_j_ok && i < n, !own_col && lo_k_ok && i < n};
-            const float dplo[3] = {S.dpp[tid], S.dp[odi - DK], S.dp[odi - 1]};
-            const float rf[3] = {rv.y, rv.z, rv.w}, pf[3] = {pv.y, pv.z, pv.w};
-            const uint8_t bit[3] = {MU, MV, MW};
-            float upd[3];
-#pragma unroll
-            for (int d = 0; d < 3; d++) {
-                upd[d] = 0.f;
-                if (!own_red && !lo_ok[d]) continue;
-                const bool fix = mo & bit[d];
-                const float v = fix ? 0.f : vol;
-                const float D = fix ? 1.f : v6 + pf[d];
-                upd[d] = __fdividef(rf[d] - (own_red ? -v : v) * (own_red ? dpown : dplo[d]), D);
-            }
-            xo.y += upd[0];
-            xo.z += upd[1];
-            xo.w += upd[2];
-            *gout = xo;
+            update(i, j, k, oxi, ori, odi, gout);
+            // the last tile in k (j) also writes column k = n (row j = n): slots whose only
+            // unknowns are the faces on the box's high side, updated by the cells below them
+            if (ext_k) update(i, j, k + 1, oxi + 1, ori + 1, odi + 1, gout + 1);
+            if (ext_j) update(i, j + 1, k, oxi + XK, ori + RK, odi + DK, gout + g.sz);
+            if (ext_j && ext_k) update(i, j + 1, k + 1, oxi + XK + 1, ori + RK + 1, odi + DK + 1, gout + g.sz + 1);
         }
         store_m(mm1);  // mask (i+3) into the slot of mask (i-1)
         if (__syncthreads_or(!wait_loads())) return fail(err);
@@ -1104,6 +1120,9 @@ int sweep32(cudaStream_t st, const Geom& g, float vol, const float4* r, const fl
     // coarse levels, where the sequential march, not bandwidth, sets the time
     const int chunk = g.n >= 192 ? 32 : g.n >= 96 ? 8 : g.n >= 48 ? 4 : g.n >= 24 ? 2 : 1;
     dim3 grid((g.n + SK) / SK, (g.n + SJ) / SJ, (g.n + chunk) / chunk), block(SK, SJ);
+    // the TMA sweep's tiles and chunks cover [0, n) and take the high-side slots (k, j or
+    // i = n) with the last ones: at n = 256, 8 x 32 x 8 blocks instead of 9 x 33 x 9
+    const dim3 grid_t((g.n + SK - 1) / SK, (g.n + SJ - 1) / SJ, (g.n + chunk - 1) / chunk);
     if (lap && encoder()) {
         const int smem_t = (int)sizeof(SmemT<false>), smem_b = (int)sizeof(SmemT<true>);
         if (!g_tattr_set[dev]) {
@@ -1123,13 +1142,13 @@ int sweep32(cudaStream_t st, const Geom& g, float vol, const float4* r, const fl
         if (ok) {
             int* err = g_sweep_err[dev];
             if (P16 && xin)
-                k_sweep_tma<true, true><<<grid, block, smem_b, st>>>(mx, mr, mp, g, vol, xout, m, flag, chunk, err, p16_scale);
+                k_sweep_tma<true, true><<<grid_t, block, smem_b, st>>>(mx, mr, mp, g, vol, xout, m, flag, chunk, err, p16_scale);
             else if (P16)
-                k_sweep_tma<false, true><<<grid, block, smem_b, st>>>(mr, mr, mp, g, vol, xout, m, flag, chunk, err, p16_scale);
+                k_sweep_tma<false, true><<<grid_t, block, smem_b, st>>>(mr, mr, mp, g, vol, xout, m, flag, chunk, err, p16_scale);
             else if (xin)
-                k_sweep_tma<true, false><<<grid, block, smem_t, st>>>(mx, mr, mp, g, vol, xout, m, flag, chunk, err, nullptr);
+                k_sweep_tma<true, false><<<grid_t, block, smem_t, st>>>(mx, mr, mp, g, vol, xout, m, flag, chunk, err, nullptr);
             else
-                k_sweep_tma<false, false><<<grid, block, smem_t, st>>>(mr, mr, mp, g, vol, xout, m, flag, chunk, err, nullptr);
+                k_sweep_tma<false, false><<<grid_t, block, smem_t, st>>>(mr, mr, mp, g, vol, xout, m, flag, chunk, err, nullptr);
             STG_LAUNCH_CK();
             return STG_OK;
         }

@@ -23,7 +23,10 @@
 //   -tol t      FP64 relative residual of every solve (1e-8 in 3D, 1e-10 in 2D)
 //   -method plain|mixed   solver precision form (plain)
 //   -inner m    FGMRES basis size per refinement step (30); each step of the basis holds two
-//               FP32 vectors (V and Z), 32 bytes per cell in 3D: 4.4 GB at 512^3
+//               FP32 vectors (V and Z) and an FP16 copy of V, 40 bytes per cell in 3D:
+//               5.5 GB at 512^3
+//   -basis16 0|1  keep the FP16 basis copies the 3D multi-dots read (default 1; 0 saves 8
+//               bytes per cell and basis step: 32 bytes, 4.4 GB at 512^3)
 //   -maxouter k FP64 refinement steps per solve (20); a solve that ends without reaching
 //               -tol is logged with its residual and the loop goes on
 //   -warm 0|1   start each forward / adjoint solve from the previous one (default 1; the
@@ -71,7 +74,7 @@ struct Args {
 Args parse(int argc, char** argv) {
     static const char* known[] = {"-o",   "-s",    "-test", "-driver", "-lf",  "-frac",   "-rmin",  "-law",   "-amax",
                                   "-move", "-tol", "-method", "-init", "-seed", "-sigma", "-frames", "-verbose",
-                                  "-dump_boundary", "-opt", "-warm", "-inner", "-maxouter"};
+                                  "-dump_boundary", "-opt", "-warm", "-inner", "-maxouter", "-basis16"};
     Args a;
     for (int i = 1; i < argc; i++) {
         std::string k = argv[i];
@@ -128,6 +131,7 @@ int run(const Args& a) {
     opts.warm_start = a.geti("-warm", 1);
     opts.inner_max = a.geti("-inner", opts.inner_max);
     opts.max_outer = a.geti("-maxouter", opts.max_outer);
+    opts.basis16 = a.geti("-basis16", opts.basis16);
 
     stg_alpha law{};
     if (law_s == "ref") {
