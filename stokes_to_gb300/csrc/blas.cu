@@ -382,22 +382,19 @@ __global__ void k_reduce_cols(const double* __restrict__ part, int nparts, int s
     }
 }
 
-// Sums column q of a [nparts][stride] table of double-float partials in a fixed order.
-__global__ void k_reduce_cols_df(const float2* __restrict__ part, int nparts, int stride, int ncols, double* __restrict__ out) {
-    __shared__ float2 sh[TPB / 32];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    for (int q = 0; q < ncols; q++) {
-        float2 s = make_float2(0.f, 0.f);
-        for (int p = threadIdx.x; p < nparts; p += TPB) s = df_add(s, part[(long long)p * stride + q]);
-        s = warp_sum_df(s);
-        if (lane == 0) sh[wid] = s;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            float2 r = sh[0];
-            for (int w = 1; w < TPB / 32; w++) r = df_add(r, sh[w]);
-            out[q] = (double)r.x + (double)r.y;
-        }
-        __syncthreads();
+// Sums column q of a [nparts][stride] table of double-float partials in a fixed order, one
+// warp per column (no block barriers): columns 0 .. ncols-2 go to out[q], the last to
+// *out_last (or to out[ncols-1] when out_last is null).
+__global__ void k_reduce_cols_df(const float2* __restrict__ part, int nparts, int stride, int ncols, double* __restrict__ out,
+                                 double* __restrict__ out_last) {
+    const int q = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (q >= ncols) return;
+    float2 s = make_float2(0.f, 0.f);
+    for (int p = lane; p < nparts; p += 32) s = df_add(s, part[(long long)p * stride + q]);
+    s = warp_sum_df(s);
+    if (lane == 0) {
+        double* dst = (out_last && q == ncols - 1) ? out_last : out + q;
+        *dst = (double)s.x + (double)s.y;
     }
 }
 
@@ -442,8 +439,8 @@ int f32_to_f64(cudaStream_t st, long long n4, const float4* a, d4* out) {
 }
 
 // column sums of a table of double-float partials (the Krylov kernels' scratch, 8 bytes an entry)
-static void rcols_df(cudaStream_t st, const double* scratch, int nparts, int stride, int ncols, double* out) {
-    k_reduce_cols_df<<<1, TPB, 0, st>>>(reinterpret_cast<const float2*>(scratch), nparts, stride, ncols, out);
+static void rcols_df(cudaStream_t st, const double* scratch, int nparts, int stride, int ncols, double* out, double* out_last = nullptr) {
+    k_reduce_cols_df<<<1, 32 * ncols, 0, st>>>(reinterpret_cast<const float2*>(scratch), nparts, stride, ncols, out, out_last);
 }
 
 int reduce_parts(cudaStream_t st, const double* parts, int nparts, double* out) {
@@ -549,9 +546,7 @@ int shift_multidot32(cudaStream_t st, const Geom& g, float vol, const float4* v,
     }
     dispatch_nv<ShiftL>(nb, st, g, vol, v, z, m, P, t, th, V16 ? sc : nullptr, w, scratch);
     STG_LAUNCH_CK();
-    rcols_df(st, scratch, RGRID, MAXV + 1, nb, h);
-    STG_LAUNCH_CK();
-    rcols_df(st, scratch + nb, RGRID, MAXV + 1, 1, ww);
+    rcols_df(st, scratch, RGRID, MAXV + 1, nb + 1, h, ww);  // the dots, and <w, w> in column nb
     STG_LAUNCH_CK();
     // basis vectors past the first MAXV: a plain multi-dot pass over the written w
     if (nv > MAXV) STG_TRY(multidot32(st, n4, V + MAXV, nv - MAXV, w, h + MAXV, scratch, nullptr));
@@ -568,12 +563,8 @@ int multidot32(cudaStream_t st, long long n4, const float4* const* v, int nv, co
         for (int q = 0; q < nb; q++) t.p[q] = v[j0 + q];
         dispatch_nv<DotL>(nb, st, n4, t, w, scratch, want_ww);
         STG_LAUNCH_CK();
-        rcols_df(st, scratch, (int)g, MAXV + 1, nb, h + j0);
+        rcols_df(st, scratch, (int)g, MAXV + 1, want_ww ? nb + 1 : nb, h + j0, want_ww ? ww : nullptr);
         STG_LAUNCH_CK();
-        if (want_ww) {
-            rcols_df(st, scratch + nb, (int)g, MAXV + 1, 1, ww);
-            STG_LAUNCH_CK();
-        }
     }
     return STG_OK;
 }
@@ -617,11 +608,10 @@ int project32(cudaStream_t st, long long n4, const float4* const* v, int nv, con
         for (int q = 0; q < nv; q++) t.p[q] = v[q];
         dispatch_nv<ProjL>(nv, st, n4, t, d, sig2, w, out, scratch, dots != nullptr, out16, nest, sc_out);
         STG_LAUNCH_CK();
-        if (dots) {
-            rcols_df(st, scratch, (int)g, MAXV + 1, nv, dots);
-            STG_LAUNCH_CK();
-        }
-        rcols_df(st, scratch + nv, (int)g, MAXV + 1, 1, nrm2);
+        if (dots)
+            rcols_df(st, scratch, (int)g, MAXV + 1, nv + 1, dots, nrm2);  // the dots, and |out|^2 in column nv
+        else
+            rcols_df(st, scratch + nv, (int)g, MAXV + 1, 1, nrm2);
         STG_LAUNCH_CK();
         return STG_OK;
     }

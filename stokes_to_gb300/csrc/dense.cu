@@ -8,8 +8,11 @@
 // gets +1 everywhere (:605-608). Unknowns that exist only as padding in the reference
 // layout are identity rows decoupled from the rest, so the dense system here keeps the
 // unknowns that exist. It is inverted once per set-up by Gauss-Jordan elimination with
-// partial pivoting on [A | I] (one grid-wide kernel per pivot, double-buffered in L2), and
-// the inverse is applied as a GEMV inside each V-cycle.
+// partial pivoting on [A | I] (double-buffered in L2; all pivot steps in one cooperative
+// launch with a grid-wide barrier between them), and the inverse is applied as a GEMV
+// inside each V-cycle.
+#include <cooperative_groups.h>
+
 #include <vector>
 
 #include "kernels.h"
@@ -114,12 +117,10 @@ __global__ void k_aug_init(int nd, double* __restrict__ A) {
     A[t] = (col >= nd && col - nd == row) ? 1.0 : 0.0;
 }
 
-// One Gauss-Jordan pivot step on the row-major nd x 2nd matrix: every block finds the
-// pivot of column k among rows k..nd-1 (largest |a|, first on ties, as LAPACK), then
-// rewrites its rows into the other buffer: row k <- row p / a_pk, row p <- row k - a_kk
-// row k', other rows i <- row i - a_ik row k'. Block b handles row b.
-__global__ void __launch_bounds__(TPB) k_gj_step(int nd, int k, const double* __restrict__ in, double* __restrict__ out,
-                                                 int* __restrict__ info) {
+// Pivot of column k among rows k..nd-1 of the row-major nd x 2nd matrix (largest |a|, the
+// first on ties, as LAPACK), found by every block; loads through L2 (the cooperative
+// kernel rewrites the buffers during its launch).
+__device__ __forceinline__ int gj_pivot(int nd, int k, const double* in) {
     __shared__ double sv[TPB / 32];
     __shared__ int si[TPB / 32];
     __shared__ int sp;
@@ -127,15 +128,15 @@ __global__ void __launch_bounds__(TPB) k_gj_step(int nd, int k, const double* __
     double best = -1.0;
     int bi = nd;
     for (int r = k + threadIdx.x; r < nd; r += TPB) {
-        double a = fabs(in[(long long)r * W + k]);
+        const double a = fabs(__ldcg(in + (long long)r * W + k));
         if (a > best || (a == best && r < bi)) {
             best = a;
             bi = r;
         }
     }
     for (int o = 16; o > 0; o >>= 1) {
-        double ob = __shfl_xor_sync(0xffffffffu, best, o);
-        int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+        const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+        const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
         if (ob > best || (ob == best && oi < bi)) {
             best = ob;
             bi = oi;
@@ -157,20 +158,56 @@ __global__ void __launch_bounds__(TPB) k_gj_step(int nd, int k, const double* __
         sp = ii;
     }
     __syncthreads();
-    const int p = sp;
-    const int row = blockIdx.x;
-    const double piv = in[(long long)p * W + k];
-    if (piv == 0.0) {
-        if (row == 0 && threadIdx.x == 0 && *info == 0) *info = k + 1;
-        for (int c = threadIdx.x; c < W; c += TPB) out[(long long)row * W + c] = in[(long long)row * W + c];
-        return;
+    return sp;
+}
+
+// One Gauss-Jordan pivot step, rows row0, row0 + rstep, ... of the output: row k <- row
+// p / a_pk, row p <- row k - a_kk row k', other rows i <- row i - a_ik row k'. The
+// reciprocal of the pivot is formed once per block (an FP64 division per thread costs
+// more than the row on GB300's FP64 pipe).
+__device__ __forceinline__ void gj_rows(int nd, int k, int p, const double* in, double* out, int* info, int row0, int rstep) {
+    __shared__ double s_inv;
+    const int W = 2 * nd;
+    const double piv = __ldcg(in + (long long)p * W + k);
+    if (threadIdx.x == 0) s_inv = piv != 0.0 ? 1.0 / piv : 0.0;
+    __syncthreads();
+    const double inv = s_inv;
+    for (int row = row0; row < nd; row += rstep) {
+        if (piv == 0.0) {
+            if (row == 0 && threadIdx.x == 0 && *info == 0) *info = k + 1;
+            for (int c = threadIdx.x; c < W; c += TPB) out[(long long)row * W + c] = __ldcg(in + (long long)row * W + c);
+            continue;
+        }
+        const int src = row == k ? p : (row == p ? k : row);
+        const double f = row == k ? 0.0 : __ldcg(in + (long long)src * W + k);
+        for (int c = threadIdx.x; c < W; c += TPB) {
+            const double pr = __ldcg(in + (long long)p * W + c) * inv;
+            out[(long long)row * W + c] = row == k ? pr : __ldcg(in + (long long)src * W + c) - f * pr;
+        }
     }
-    const double inv = 1.0 / piv;
-    const int src = row == k ? p : (row == p ? k : row);
-    const double f = row == k ? 0.0 : in[(long long)src * W + k];
-    for (int c = threadIdx.x; c < W; c += TPB) {
-        double pr = in[(long long)p * W + c] * inv;
-        out[(long long)row * W + c] = row == k ? pr : in[(long long)src * W + c] - f * pr;
+    __syncthreads();  // s_inv and the pivot's shared words are rewritten by the next step
+}
+
+// One pivot step per launch (block b handles row b); the fallback where a cooperative
+// launch is unavailable.
+__global__ void __launch_bounds__(TPB) k_gj_step(int nd, int k, const double* in, double* out, int* info) {
+    const int p = gj_pivot(nd, k, in);
+    gj_rows(nd, k, p, in, out, info, blockIdx.x, nd);
+}
+
+// All nd pivot steps in one cooperative launch, a grid-wide barrier between them (the
+// launch gaps of nd dependent kernels were most of the set-up time): the operations of
+// k_gj_step in the same order, so the same inverse bit for bit. Step k reads buffer k mod
+// 2 and writes the other.
+__global__ void __launch_bounds__(TPB) k_gj_all(int nd, double* a, double* b, int* info) {
+    namespace cg = cooperative_groups;
+    cg::grid_group grid = cg::this_grid();
+    for (int k = 0; k < nd; k++) {
+        const double* in = (k & 1) ? b : a;
+        double* out = (k & 1) ? a : b;
+        const int p = gj_pivot(nd, k, in);
+        gj_rows(nd, k, p, in, out, info, blockIdx.x, gridDim.x);
+        grid.sync();
     }
 }
 
@@ -279,10 +316,11 @@ int dense_setup_v(cudaStream_t st, DenseCoarse& D, const Geom& g, const d4* V, c
         STG_LAUNCH_CK();
     }
     if (extra) STG_TRY(extra(D.A, nd));
-    return gj_invert(st, nd, D.A, D.Ainv, D.info, &D.inv);
+    return gj_invert(st, nd, D.A, D.Ainv, D.info, &D.inv, true);
 }
 
-int dense_setup(cudaStream_t st, DenseCoarse& D, const Geom& g, double vol, const uint8_t* m, const d4* P64, int closed) {
+int dense_setup(cudaStream_t st, DenseCoarse& D, const Geom& g, double vol, const uint8_t* m, const d4* P64, int closed,
+                bool invert) {
     const int nd = D.nd;
     k_aug_init<<<grid_for(2ll * nd * nd, TPB), TPB, 0, st>>>(nd, D.A);
     STG_LAUNCH_CK();
@@ -300,11 +338,27 @@ int dense_setup(cudaStream_t st, DenseCoarse& D, const Geom& g, double vol, cons
         k_closed<<<grid_for((long long)nd * nd, TPB), TPB, 0, st>>>(nd, D.comp_of, D.A);
         STG_LAUNCH_CK();
     }
-    return gj_invert(st, nd, D.A, D.Ainv, D.info, &D.inv);
+    return invert ? gj_invert(st, nd, D.A, D.Ainv, D.info, &D.inv) : STG_OK;
 }
 
-int gj_invert(cudaStream_t st, int nd, double* a, double* b, int* info, const double** inv) {
+int gj_invert(cudaStream_t st, int nd, double* a, double* b, int* info, const double** inv, bool coop) {
     STG_CK(cudaMemsetAsync(info, 0, sizeof(int), st));
+    if (coop) {
+        // one block per SM at most (fewer blocks, a cheaper grid barrier), within what can
+        // be co-resident
+        int dev = 0, sms = 0, per_sm = 0;
+        STG_CK(cudaGetDevice(&dev));
+        STG_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        STG_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gj_all, TPB, 0));
+        if (per_sm >= 1 && sms >= 1) {
+            const int g = nd < sms ? nd : sms;
+            void* args[] = {&nd, &a, &b, &info};
+            STG_CK(cudaLaunchCooperativeKernel((const void*)k_gj_all, dim3((unsigned)g), dim3(TPB), args, 0, st));
+            add_launches(1);
+            *inv = (nd & 1) ? b + nd : a + nd;  // step nd-1 wrote buffer nd mod 2
+            return STG_OK;
+        }
+    }
     for (int k = 0; k < nd; k++) {
         k_gj_step<<<nd, TPB, 0, st>>>(nd, k, a, b, info);
         STG_LAUNCH_CK();

@@ -147,16 +147,21 @@ struct DenseCoarse {
 };
 int dense_init(DenseCoarse& D, const Geom& g);
 void dense_free(DenseCoarse& D);
-// DirectSolve3D::update: probe assembly + (closed) all-ones p-block + inversion
-int dense_setup(cudaStream_t st, DenseCoarse& D, const Geom& g, double vol, const uint8_t* m, const d4* P64, int closed);
+// DirectSolve3D::update: probe assembly + (closed) all-ones p-block + inversion (invert
+// false: the assembly only, for a caller that captures it in a CUDA graph and then calls
+// gj_invert with a cooperative launch outside the capture)
+int dense_setup(cudaStream_t st, DenseCoarse& D, const Geom& g, double vol, const uint8_t* m, const d4* P64, int closed,
+                bool invert = true);
 // The same with per-slot face vols (general.cu op64v); extra(A, nd) may add entries to the
 // assembled matrix (row-major, row stride 2 nd) before the inversion
 int dense_setup_v(cudaStream_t st, DenseCoarse& D, const Geom& g, const d4* V, const uint8_t* m, const d4* P64, int closed,
                   const std::function<int(double*, int)>& extra);
 // In-place Gauss-Jordan inversion of the row-major nd x 2nd [A | I] held in a (b is the
 // second buffer of the same size); *inv receives the inverse (row stride 2 nd), which
-// lies in whichever buffer the last step wrote. *info = first zero pivot + 1, or 0.
-int gj_invert(cudaStream_t st, int nd, double* a, double* b, int* info, const double** inv);
+// lies in whichever buffer the last step wrote. *info = first zero pivot + 1, or 0. coop:
+// all steps in one cooperative launch (not capturable in a CUDA graph), else one launch
+// per pivot; the two give the same inverse bit for bit.
+int gj_invert(cudaStream_t st, int nd, double* a, double* b, int* info, const double** inv, bool coop = false);
 // x = A^-1 r on the slots (FP32 in/out, FP64 inside)
 int dense_apply32(cudaStream_t st, const DenseCoarse& D, const Geom& g, const float4* r, float4* x);
 int dense_apply64(cudaStream_t st, const DenseCoarse& D, const Geom& g, const d4* r, d4* x);

@@ -170,18 +170,17 @@ int update(stg_t* h) {
     for (int i = 0; i < h->L; i++) PROF(h, 8, 0.0, to_f16(h->st, h->lv[i].g, h->lv[i].P32, h->d_pscale + i, h->lv[i].P16));
     // low words of the finest penalty for the double-float residual (P32 holds the high)
     PROF(h, 8, 0.0, split64(h->st, fine(h).g.nslot, fine(h).P64, nullptr, h->Plo));
-    // the coarsest set-up (one launch per Gauss-Jordan pivot) reads and writes fixed buffers:
-    // replayed as a CUDA graph; the inverse's buffer pointer is host state
+    // the coarsest matrix's assembly (27 small launches) reads and writes fixed buffers:
+    // replayed as a CUDA graph; its Gauss-Jordan inversion is one cooperative launch
     GraphCache& G = h->sgraph;
     PROF(h, 8, 0.0,
          graphed(h, G, h->closed ? 2 : 1,
-                 [&] { return dense_setup(h->st, h->dense, h->lv[0].g, h->lv[0].vol, h->lv[0].m, h->lv[0].P64, h->closed ? 1 : 0); },
-                 [&](bool save) {
-                     if (save)
-                         G.saved = h->dense.inv;
-                     else
-                         h->dense.inv = static_cast<const double*>(G.saved);
-                 }));
+                 [&] {
+                     return dense_setup(h->st, h->dense, h->lv[0].g, h->lv[0].vol, h->lv[0].m, h->lv[0].P64, h->closed ? 1 : 0,
+                                        false);
+                 },
+                 [](bool) {}));
+    PROF(h, 8, 0.0, gj_invert(h->st, h->dense.nd, h->dense.A, h->dense.Ainv, h->dense.info, &h->dense.inv, true));
     h->updated = true;
     return STG_OK;
 }

@@ -600,8 +600,8 @@ int setup2(stg_t* h) {
         return STG_E_INVALID;
     }
     auto& lv = h->c2->lv;
-    // coarsening, the analytic coarsest matrix and its Gauss-Jordan inverse touch fixed
-    // buffers only: replayed as a CUDA graph; the inverse's buffer pointer is host state
+    // coarsening and the analytic coarsest matrix touch fixed buffers only: replayed as a
+    // CUDA graph; the Gauss-Jordan inverse follows as one cooperative launch
     auto body = [&]() -> int {
         for (int i = (int)lv.size() - 2; i >= 0; i--) {
             Level2 &c = lv[i], &f = lv[i + 1];
@@ -617,15 +617,12 @@ int setup2(stg_t* h) {
         const int nd = C.g.size();
         k2_calcA<<<g1((long long)nd * nd), TPB, 0, h->st>>>(C.g, C.vol, C.pen, C.fixed, C.lap, h->closed ? 1 : 0, h->c2->aug0);
         STG_LAUNCH_CK();
-        return gj_invert(h->st, nd, h->c2->aug0, h->c2->aug1, h->c2->info, &h->c2->inv);
+        return STG_OK;
     };
     GraphCache& G = h->sgraph;
-    STG_TRY(graphed(h, G, (h->closed ? 2 : 1) | (h->hier_flow ? 4 : 0), body, [&](bool save) {
-        if (save)
-            G.saved = h->c2->inv;
-        else
-            h->c2->inv = static_cast<const double*>(G.saved);
-    }));
+    STG_TRY(graphed(h, G, (h->closed ? 2 : 1) | (h->hier_flow ? 4 : 0), body, [](bool) {}));
+    // the inversion: one cooperative launch, outside the graph
+    STG_TRY(gj_invert(h->st, lv[0].g.size(), h->c2->aug0, h->c2->aug1, h->c2->info, &h->c2->inv, true));
     h->updated = true;
     return STG_OK;
 }
