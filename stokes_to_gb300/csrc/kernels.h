@@ -27,8 +27,13 @@ int apply32(cudaStream_t st, const Geom& g, float vol, const float4* x, const ui
             bool lap = false);
 // One colour of the box-Vanka block-Jacobi step on the residual equation, fused with the
 // residual: xout = xin + SHATTER(B^-1 GATHER(r - A xin)) (sweep.cu). xin == nullptr: xin = 0.
+// xc (coarse x on gc): xin is first corrected by the injected coarse value (the
+// prolongation fused into the sweep; needs xin, lap and P16, else STG_E_UNSUPPORTED).
 int sweep32(cudaStream_t st, const Geom& g, float vol, const float4* r, const float4* xin, float4* xout, const uint8_t* m,
-            const float4* P, int flag, bool lap = false, const __half* P16 = nullptr, const float* p16_scale = nullptr);
+            const float4* P, int flag, bool lap = false, const __half* P16 = nullptr, const float* p16_scale = nullptr,
+            const float4* xc = nullptr, const Geom* gc = nullptr);
+// whether the TMA-staged sweep (and with it the fused prolongation) can run here
+bool sweep_tma_available();
 // 1 in *timed_out when a sweep with TMA staging gave up waiting for its loads (sticky)
 int sweep_status(cudaStream_t st, int* timed_out);
 // rc = R (rf - A xf) with R the 8-child sum masked by the coarse mask (xf == nullptr: rc = R rf).

@@ -199,7 +199,7 @@ int ensure_setup(stg_t* h, bool reference) {
 // Smoother of StokeLike::GenerateJacobiPreconditioner(grid, A, 2) (stoke/StokeLike.cu:345-372):
 // DescentSmoother({red, black}, {2, 2}) before the coarse correction and {black, red} after
 // (common_cpx/DescentSmoother.cu:31-47), written in correction form x <- x + P_c(r - A x).
-int sweep(stg_t* h, Level& L, const float4* r, int flag, bool first) {
+int sweep(stg_t* h, Level& L, const float4* r, int flag, bool first, Level* C = nullptr) {
     float vol = (float)L.vol;
     // profile class 1: sweeps of the finest level; 10: of the coarser levels
     const int cls = &L == &fine(h) ? 1 : 10;
@@ -212,9 +212,22 @@ int sweep(stg_t* h, Level& L, const float4* r, int flag, bool first) {
         PROF(h, cls, 41.0 * L.g.box(), sweep32(h->st, L.g, vol, r, nullptr, L.x(), L.m, L.P32, flag, fast(h, L), P16, psc));
         return STG_OK;
     }
+    if (C) {  // with the coarse correction injected as x is staged: 2 B a slot more
+        PROF(h, cls, 59.0 * L.g.box(),
+             sweep32(h->st, L.g, vol, r, L.x(), L.other(), L.m, L.P32, flag, fast(h, L), P16, psc, C->x(), &C->g));
+        L.cur ^= 1;
+        return STG_OK;
+    }
     PROF(h, cls, 57.0 * L.g.box(), sweep32(h->st, L.g, vol, r, L.x(), L.other(), L.m, L.P32, flag, fast(h, L), P16, psc));
     L.cur ^= 1;
     return STG_OK;
+}
+
+// The prolongation (injection) can ride on the first post-smoothing sweep: FP32 coarse
+// correction, the solver's own uniform-form sweeps (TMA, FP16 penalty) with x present.
+bool fuse_prolong(const stg_t* h, const Level& F) {
+    return !h->reference_cycle && h->opts.method != STG_METHOD_MIXED && h->opts.prolong != 1 && fast(h, F) && F.P16 &&
+           sweep_tma_available();
 }
 
 // Sweeps per colour: the reference's 2 for the adapters, else the solver option, raised to
@@ -225,12 +238,13 @@ int sweeps_per_colour(const stg_t* h) {
     return h->boost ? std::max(s, 2) : s;
 }
 
-int smooth(stg_t* h, Level& L, const float4* r, bool post, bool x_is_zero) {
+// C: the coarse level whose correction the first sweep injects (fuse_prolong)
+int smooth(stg_t* h, Level& L, const float4* r, bool post, bool x_is_zero, Level* C = nullptr) {
     const int per = sweeps_per_colour(h);
     int s = 0;
     for (int c = 0; c < 2; c++) {
         const int flag = post ? 1 - c : c;
-        for (int q = 0; q < per; q++, s++) STG_TRY(sweep(h, L, r, flag, s == 0 && x_is_zero));
+        for (int q = 0; q < per; q++, s++) STG_TRY(sweep(h, L, r, flag, s == 0 && x_is_zero, s == 0 ? C : nullptr));
     }
     return STG_OK;
 }
@@ -257,6 +271,10 @@ int vcycle_levels(stg_t* h, int top, const float4* rhs) {
         Level& F = h->lv[i];
         Level& C = h->lv[i - 1];
         const float4* r = (i == L - 1) ? rhs : F.r;
+        if (fuse_prolong(h, F)) {
+            STG_TRY(smooth(h, F, r, true, false, &C));
+            continue;
+        }
         if (mixed) {
             PROF(h, 3, 24.0 * C.g.box(), to_bf16(h->st, C.g, C.x(), C.xbf));
             PROF(h, 3, 8.0 * C.g.box() + 33.0 * F.g.box(), prolong_add_bf16(h->st, F.g, C.g, C.xbf, F.m, F.x(), lin));
@@ -344,6 +362,7 @@ int vcycle(stg_t* h, const float4* rhs) {
     STG_TRY(smooth(h, F, rhs, false, true));
     PROF(h, 2, 49.0 * F.g.box() + 17.0 * C.g.box(), restrict_resid32(h->st, C.g, F.g, (float)F.vol, rhs, F.x(), F.m, F.P32, C.m, C.r, fast(h, F)));
     STG_TRY(coarse_cycle(h));
+    if (fuse_prolong(h, F)) return smooth(h, F, rhs, true, false, &C);
     const bool lin = h->opts.prolong == 1 && !h->reference_cycle;
     if (mixed) {
         PROF(h, 3, 24.0 * C.g.box(), to_bf16(h->st, C.g, C.x(), C.xbf));

@@ -731,12 +731,18 @@ __device__ __forceinline__ void fail(int* err) {
     if (threadIdx.x == 0 && threadIdx.y == 0) atomicExch(err, 1);
 }
 
-template <bool HAS_X, bool PB>
+// PRO (with HAS_X and PB): the sweep also applies the coarse-grid correction, x_in = x +
+// inject(xc) (k_prolong_add32's injection: each unmasked unknown of a box slot adds its
+// parent coarse slot's value), to every x plane as it lands in shared memory, so the
+// first post-smoothing sweep replaces the prolongation pass; xout = x_in + the update.
+template <bool HAS_X, bool PB, bool PRO = false>
 __global__ void __launch_bounds__(NT, PB ? 4 : 3) k_sweep_tma(const __grid_constant__ CUtensorMap tmx,
                                                              const __grid_constant__ CUtensorMap tmr,
                                                              const __grid_constant__ CUtensorMap tmp, Geom g, float vol,
                                                              float4* __restrict__ xout, const uint8_t* __restrict__ m, int flag,
-                                                             int chunk, int* __restrict__ err, const float* __restrict__ pscale) {
+                                                             int chunk, int* __restrict__ err, const float* __restrict__ pscale,
+                                                             const float4* __restrict__ xc, int c_plane, int c_sz) {
+    static_assert(!PRO || (HAS_X && PB), "the fused prolongation needs x and the FP16 penalty ring");
     extern __shared__ __align__(128) unsigned char smem_raw[];
     SmemT<PB>& S = *reinterpret_cast<SmemT<PB>*>(smem_raw);
     float4* RR;  // the residual ring: its own array, or the r ring itself
@@ -799,6 +805,35 @@ __global__ void __launch_bounds__(NT, PB ? 4 : 3) k_sweep_tma(const __grid_const
         const bool ok = wait_phase(bar, phase);
         phase ^= 1u;
         return ok;
+    };
+    // fused prolongation: the thread's two staged x elements, whether they lie in the
+    // box's (j, k) range, and their parents' offsets in a coarse plane
+    bool pin0 = false, pin1 = false;
+    int cofs0 = 0, cofs1 = 0;
+    if (PRO) {
+        auto setup = [&](const Stage& X, int e, bool& pin, int& cofs) {
+            const int jj = j0 - 2 + e / XK, kk = k0 - 2 + e % XK;
+            pin = X.s >= 0 && jj >= 0 && jj <= n && kk >= 0 && kk <= n;
+            cofs = pin ? ((jj >> 1) + 1) * c_sz + ((kk >> 1) + 1) : 0;
+        };
+        setup(X0, tid, pin0, cofs0);
+        setup(X1, tid + NT, pin1, cofs1);
+    }
+    // x plane p in ring slot xs += inject(xc), with the plane's masks ma, mb of the two elements
+    auto prolong = [&](int xs, int p, uint8_t ma, uint8_t mb) {
+        if (!PRO || p < 0 || p > n) return;
+        const float4* cp = xc + (long long)((p >> 1) + 1) * c_plane;
+        auto add = [&](int idx, int cofs, uint8_t mm) {
+            const float4 v = __ldg(cp + cofs);
+            float4 x = S.x[xs + idx];
+            if (!(mm & MP)) x.x += v.x;
+            if (!(mm & MU)) x.y += v.y;
+            if (!(mm & MV)) x.z += v.z;
+            if (!(mm & MW)) x.w += v.w;
+            S.x[xs + idx] = x;
+        };
+        if (pin0) add(X0.s, cofs0, ma);
+        if (pin1) add(X1.s, cofs1, mb);
     };
     uint8_t mr0 = MALL, mr1 = MALL;
     auto fetch_m = [&](int p, const uint8_t* src) {
@@ -946,6 +981,18 @@ __global__ void __launch_bounds__(NT, PB ? 4 : 3) k_sweep_tma(const __grid_const
     fetch_m(i0 + 2, gm + 3 * plane);
     store_m(m2);
     if (__syncthreads_or(!wait_loads())) return fail(err);
+    if (PRO) {
+        // planes i0-1 .. i0+1 take their masks from the ring (the thread's own entries), i0-2
+        // from memory
+        auto ms = [&](int slot, const Stage& X) { return X.s >= 0 ? S.m[slot + X.s] : (uint8_t)MALL; };
+        const uint8_t* g2 = m + (long long)(i0 - 1) * plane;  // plane i0-2
+        const bool ok2 = i0 - 2 >= 0;
+        prolong(xm1, i0 - 2, ok2 && X0.jk >= 0 ? __ldg(g2 + X0.jk) : (uint8_t)MALL, ok2 && X1.jk >= 0 ? __ldg(g2 + X1.jk) : (uint8_t)MALL);
+        prolong(x0, i0 - 1, ms(mm1, X0), ms(mm1, X1));
+        prolong(x1, i0, ms(m0, X0), ms(m0, X1));
+        prolong(x2, i0 + 1, ms(m1, X0), ms(m1, X1));
+        __syncthreads();
+    }
     // residual of i0-1: x(i0-2, i0-1, i0) = slots (xm1, x0, x1), r(i0-1) = r0, P(i0-1) = pm1, mask(i0-1) = mm1
     residual(i0 - 1, xm1, x0, x1, r0, pm1, mm1, rrm1);
     __syncthreads();
@@ -962,6 +1009,10 @@ __global__ void __launch_bounds__(NT, PB ? 4 : 3) k_sweep_tma(const __grid_const
     __syncthreads();
     S.dpp[tid] = S.dp[odi];
     if (__syncthreads_or(!wait_loads())) return fail(err);
+    if (PRO) {  // x(i0+2) landed in slot xm1; its masks are in ring slot m2
+        prolong(xm1, i0 + 2, X0.s >= 0 ? S.m[m2 + X0.s] : (uint8_t)MALL, X1.s >= 0 ? S.m[m2 + X1.s] : (uint8_t)MALL);
+        __syncthreads();
+    }
     // rotate to the loop's view at i = i0: x(i0-1..i0+2) = (x0, x1, x2, xm1), r(i0) = r1,
     // r(i0+1) = r0, rr(i0-1) = rrm1, rr(i0) = rr0, P(i0-1) = pm1, masks i0-1 .. i0+2 unchanged
     {
@@ -1008,6 +1059,10 @@ __global__ void __launch_bounds__(NT, PB ? 4 : 3) k_sweep_tma(const __grid_const
         store_m(mm1);  // mask (i+3) into the slot of mask (i-1)
         if (__syncthreads_or(!wait_loads())) return fail(err);
         S.dpp[tid] = S.dp[odi];
+        if (PRO) {  // x(i+3) landed in slot xm1; its masks are still in registers
+            prolong(xm1, i + 3, mr0, mr1);
+            __syncthreads();
+        }
         // rotate the rings and advance the plane pointers
         {
             int t = xm1;
@@ -1117,6 +1172,8 @@ int tma_chunk(int dev, int n, bool fp16_pen) {
 
 }  // namespace
 
+bool sweep_tma_available() { return encoder() != nullptr; }
+
 int sweep_status(cudaStream_t st, int* timed_out) {
     *timed_out = 0;
     const int dev = device_slot();
@@ -1127,7 +1184,7 @@ int sweep_status(cudaStream_t st, int* timed_out) {
 }
 
 int sweep32(cudaStream_t st, const Geom& g, float vol, const float4* r, const float4* xin, float4* xout, const uint8_t* m,
-            const float4* P, int flag, bool lap, const __half* P16, const float* p16_scale) {
+            const float4* P, int flag, bool lap, const __half* P16, const float* p16_scale, const float4* xc, const Geom* gc) {
     const int dev = device_slot();
     if (dev < 0) {
         set_error("sweep32: device ordinal beyond %d", MAX_DEVICES - 1);
@@ -1156,6 +1213,7 @@ int sweep32(cudaStream_t st, const Geom& g, float vol, const float4* r, const fl
             STG_CK(cudaFuncSetAttribute(k_sweep_tma<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_t));
             STG_CK(cudaFuncSetAttribute(k_sweep_tma<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_b));
             STG_CK(cudaFuncSetAttribute(k_sweep_tma<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_b));
+            STG_CK(cudaFuncSetAttribute(k_sweep_tma<true, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_b));
             STG_CK(cudaMalloc((void**)&g_sweep_err[dev], sizeof(int)));
             STG_CK(cudaMemset(g_sweep_err[dev], 0, sizeof(int)));
             g_tattr_set[dev] = true;
@@ -1167,17 +1225,31 @@ int sweep32(cudaStream_t st, const Geom& g, float vol, const float4* r, const fl
                         (P16 ? slot_map16(enc, &mp, P16, g, RK, RJ) : slot_map(enc, &mp, P, g, RK, RJ));
         if (ok) {
             int* err = g_sweep_err[dev];
+            if (xc && P16 && xin) {
+                k_sweep_tma<true, true, true><<<grid_t, block, smem_b, st>>>(mx, mr, mp, g, vol, xout, m, flag, chunk_t, err, p16_scale,
+                                                                             xc, gc->sy * gc->sz, gc->sz);
+                STG_LAUNCH_CK();
+                return STG_OK;
+            }
+            if (xc) {
+                set_error("sweep32: the fused prolongation needs x and the FP16 penalty");
+                return STG_E_UNSUPPORTED;
+            }
             if (P16 && xin)
-                k_sweep_tma<true, true><<<grid_t, block, smem_b, st>>>(mx, mr, mp, g, vol, xout, m, flag, chunk_t, err, p16_scale);
+                k_sweep_tma<true, true><<<grid_t, block, smem_b, st>>>(mx, mr, mp, g, vol, xout, m, flag, chunk_t, err, p16_scale, nullptr, 0, 0);
             else if (P16)
-                k_sweep_tma<false, true><<<grid_t, block, smem_b, st>>>(mr, mr, mp, g, vol, xout, m, flag, chunk_t, err, p16_scale);
+                k_sweep_tma<false, true><<<grid_t, block, smem_b, st>>>(mr, mr, mp, g, vol, xout, m, flag, chunk_t, err, p16_scale, nullptr, 0, 0);
             else if (xin)
-                k_sweep_tma<true, false><<<grid_t, block, smem_t, st>>>(mx, mr, mp, g, vol, xout, m, flag, chunk_t, err, nullptr);
+                k_sweep_tma<true, false><<<grid_t, block, smem_t, st>>>(mx, mr, mp, g, vol, xout, m, flag, chunk_t, err, nullptr, nullptr, 0, 0);
             else
-                k_sweep_tma<false, false><<<grid_t, block, smem_t, st>>>(mr, mr, mp, g, vol, xout, m, flag, chunk_t, err, nullptr);
+                k_sweep_tma<false, false><<<grid_t, block, smem_t, st>>>(mr, mr, mp, g, vol, xout, m, flag, chunk_t, err, nullptr, nullptr, 0, 0);
             STG_LAUNCH_CK();
             return STG_OK;
         }
+    }
+    if (xc) {
+        set_error("sweep32: the fused prolongation needs the TMA sweep");
+        return STG_E_UNSUPPORTED;
     }
     if (xin && lap)
         k_sweep_lap<true><<<grid, block, smem_l, st>>>(g, vol, r, xin, xout, m, P, flag, chunk);
