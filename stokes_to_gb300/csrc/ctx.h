@@ -76,6 +76,11 @@ struct stg_ctx {
     stg_opts opts{};
     cudaStream_t st = nullptr;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
+    // second stream and events for host copies that overlap the set-up (stg_set_rhs)
+    cudaStream_t cst = nullptr;
+    cudaEvent_t ec0 = nullptr, ec1 = nullptr;
+    // the set-up ran after the last penalty change, in stg_set_rhs: stg_solve skips its own
+    bool setup_fresh = false;
     std::vector<stg::Level> lv;  // lv[0] coarsest ... lv[L-1] finest (reference order)
     DenseCoarse dense;
     bool closed = true, have_boundary = false, have_penalty = false, have_rhs = false, updated = false, have_solution = false;

@@ -873,6 +873,10 @@ int stg_create(int dim, int n, const stg_opts* opts, stg_t** out) {
     h->st = h->own_st;
     cudaEventCreate(&h->e0);
     cudaEventCreate(&h->e1);
+    if (cudaStreamCreateWithFlags(&h->cst, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&h->ec0, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&h->ec1, cudaEventDisableTiming) != cudaSuccess)
+        return fail(cuda_fail(cudaGetLastError(), "create", __FILE__, __LINE__));
     if (dim == 2 && (rc = create2d(h))) return fail(rc);
     h->lv.resize(dim == 3 ? h->L : 0);
     for (int i = (int)h->lv.size() - 1, nn = n; i >= 0; i--, nn /= 2) {
@@ -985,6 +989,9 @@ int stg_destroy(stg_t* h) {
     if (h->e1) cudaEventDestroy(h->e1);
     for (auto e : h->prof.pool) cudaEventDestroy(e);
     if (h->own_st) cudaStreamDestroy(h->own_st);
+    if (h->cst) cudaStreamDestroy(h->cst);
+    if (h->ec0) cudaEventDestroy(h->ec0);
+    if (h->ec1) cudaEventDestroy(h->ec1);
     delete h;
     return STG_OK;
 }
@@ -1151,7 +1158,25 @@ int stg_set_rhs(stg_t* h, const double* cell_b, const double* const* face_b) {
     STG_TRY(check_handle(h));
     const double* dc = nullptr;
     const double* df[3] = {nullptr, nullptr, nullptr};
-    STG_TRY(upload_fields(h, cell_b, face_b, &dc, df));
+    // A pending 3D set-up (the penalty changed since the last one) reads only the penalty
+    // and the boundary: it runs on the handle's stream while b is copied on the copy
+    // stream, and the next stg_solve uses it instead of running its own.
+    const bool overlap = h->dim == 3 && h->have_boundary && h->have_penalty && (!h->updated || !h->hier_flow);
+    if (overlap) {
+        STG_CK(cudaEventRecord(h->ec0, h->st));  // earlier work on the staging buffer first
+        STG_CK(cudaStreamWaitEvent(h->cst, h->ec0, 0));
+        cudaStream_t keep = h->st;
+        h->st = h->cst;
+        const int urc = upload_fields(h, cell_b, face_b, &dc, df);
+        h->st = keep;
+        STG_TRY(urc);
+        STG_CK(cudaEventRecord(h->ec1, h->cst));
+        STG_TRY(ensure_setup(h, false));
+        h->setup_fresh = true;
+        STG_CK(cudaStreamWaitEvent(h->st, h->ec1, 0));
+    } else {
+        STG_TRY(upload_fields(h, cell_b, face_b, &dc, df));
+    }
     STG_TRY(fields_to_vec(h, dc, df, h->b64));
     h->have_rhs = true;
     STG_CK(cudaStreamSynchronize(h->st));
@@ -1164,7 +1189,10 @@ int stg_solve(stg_t* h, double* p_out, double* const* vel_out, stg_stats* stats)
         set_error("stg_set_rhs must come first");
         return STG_E_INVALID;
     }
-    h->updated = false;  // the reference re-runs the set-up on every solve
+    // the reference re-runs the set-up on every solve; one that stg_set_rhs ran after the
+    // last penalty change (overlapping the copy of b) counts as this solve's
+    if (!h->setup_fresh) h->updated = false;
+    h->setup_fresh = false;
     int rc = solve_core(h, h->b64, h->x64, stats);
     if (rc != STG_OK && rc != STG_E_NOT_CONVERGED) return rc;
     h->have_solution = true;
