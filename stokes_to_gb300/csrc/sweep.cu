@@ -819,12 +819,19 @@ __global__ void __launch_bounds__(NT, PB ? 4 : 3) k_sweep_tma(const __grid_const
         setup(X0, tid, pin0, cofs0);
         setup(X1, tid + NT, pin1, cofs1);
     }
-    // x plane p in ring slot xs += inject(xc), with the plane's masks ma, mb of the two elements
-    auto prolong = [&](int xs, int p, uint8_t ma, uint8_t mb) {
+    // the coarse values of plane p for the thread's two elements (zero outside the box)
+    auto coarse = [&](int p, float4& v0, float4& v1) {
+        const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+        v0 = v1 = z;
         if (!PRO || p < 0 || p > n) return;
         const float4* cp = xc + (long long)((p >> 1) + 1) * c_plane;
-        auto add = [&](int idx, int cofs, uint8_t mm) {
-            const float4 v = __ldg(cp + cofs);
+        if (pin0) v0 = __ldg(cp + cofs0);
+        if (pin1) v1 = __ldg(cp + cofs1);
+    };
+    // x plane p in ring slot xs += the coarse values v0, v1, with the masks ma, mb
+    auto inject = [&](int xs, int p, const float4& v0, const float4& v1, uint8_t ma, uint8_t mb) {
+        if (!PRO || p < 0 || p > n) return;
+        auto add = [&](int idx, const float4& v, uint8_t mm) {
             float4 x = S.x[xs + idx];
             if (!(mm & MP)) x.x += v.x;
             if (!(mm & MU)) x.y += v.y;
@@ -832,8 +839,13 @@ __global__ void __launch_bounds__(NT, PB ? 4 : 3) k_sweep_tma(const __grid_const
             if (!(mm & MW)) x.w += v.w;
             S.x[xs + idx] = x;
         };
-        if (pin0) add(X0.s, cofs0, ma);
-        if (pin1) add(X1.s, cofs1, mb);
+        if (pin0) add(X0.s, v0, ma);
+        if (pin1) add(X1.s, v1, mb);
+    };
+    auto prolong = [&](int xs, int p, uint8_t ma, uint8_t mb) {
+        float4 v0, v1;
+        coarse(p, v0, v1);
+        inject(xs, p, v0, v1, ma, mb);
     };
     uint8_t mr0 = MALL, mr1 = MALL;
     auto fetch_m = [&](int p, const uint8_t* src) {
@@ -1044,6 +1056,10 @@ __global__ void __launch_bounds__(NT, PB ? 4 : 3) k_sweep_tma(const __grid_const
             tma_r(sr, r0, i + 2, &tmr);
         }
         fetch_m(i + 3, gm);
+        // the coarse values for x(i+3) are loaded now and injected once it has landed, so
+        // their latency hides behind this plane's work
+        float4 pc0, pc1;
+        coarse(i + 3, pc0, pc1);
         residual(i + 1, x0, x1, x2, r1, p1, m1, rrm1);
         __syncthreads();
         pressure(i, rr0, rrm1, p0, p1, m0, m1);
@@ -1060,7 +1076,7 @@ __global__ void __launch_bounds__(NT, PB ? 4 : 3) k_sweep_tma(const __grid_const
         if (__syncthreads_or(!wait_loads())) return fail(err);
         S.dpp[tid] = S.dp[odi];
         if (PRO) {  // x(i+3) landed in slot xm1; its masks are still in registers
-            prolong(xm1, i + 3, mr0, mr1);
+            inject(xm1, i + 3, pc0, pc1, mr0, mr1);
             __syncthreads();
         }
         // rotate the rings and advance the plane pointers
