@@ -73,8 +73,10 @@ typedef struct stg_opts {
     int basis16;         /* 1 (default): the 3D uniform-form FGMRES also keeps an FP16 copy
                             of each basis vector (8 more bytes per slot and vector), from
                             which its multi-dot pass reads; the projections and the
-                            solution update keep the FP32 basis. 0: FP32 only (e.g. to fit
-                            a 512^3 solve with a long basis in less memory). */
+                            solution update keep the FP32 basis. Where the copies do not
+                            fit in device memory the handle runs without them. 0: FP32
+                            only (e.g. to fit a 512^3 solve with a long basis in a memory
+                            budget). */
 } stg_opts;
 
 typedef struct stg_stats {

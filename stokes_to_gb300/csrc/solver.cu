@@ -924,10 +924,19 @@ int stg_create(int dim, int n, const stg_opts* opts, stg_t** out) {
     for (auto& p : h->Z)
         if ((rc = dalloc(&p, ns))) return fail(rc);
     if (dim == 3 && h->opts.basis16) {
+        // the FP16 copies only speed up the multi-dot: without room for them the handle
+        // runs on the FP32 basis alone
         h->V16.assign(h->m + 1, nullptr);
-        for (auto& p : h->V16)
-            if ((rc = dalloc(&p, ns))) return fail(rc);
-        if ((rc = dalloc(&h->dsc16, (size_t)h->m + 1))) return fail(rc);
+        bool ok = dalloc(&h->dsc16, (size_t)h->m + 1) == STG_OK;
+        for (auto& p : h->V16) ok = ok && dalloc(&p, ns) == STG_OK;
+        if (!ok) {
+            for (auto p : h->V16) cudaFree(p);
+            cudaFree(h->dsc16);
+            h->V16.clear();
+            h->dsc16 = nullptr;
+            cudaGetLastError();
+            set_error("%s", "");
+        }
     }
     if ((rc = dalloc(&h->dscr, 1216 * 18)) || (rc = dalloc(&h->dh, 2 * (h->m + 2))) || (rc = dalloc(&h->dnrm, 8)) ||
         (rc = dalloc(&h->dsig2, h->m + 2)) ||
