@@ -216,7 +216,7 @@ __global__ void __launch_bounds__(TPB) k_axpy_multi_32to64(long long n4, Tab z, 
 }
 
 // Per-thread partial sums are FP32 (a thread covers a few hundred products; GB300's FP64
-// pipe cannot keep up with HBM for these streams); block and grid sums are FP64.
+// pipe cannot keep up with HBM for these streams); block and grid sums are double-float.
 // With WW the pass also returns <w, w> in column NV.
 template <int NV, bool WW>
 __global__ void __launch_bounds__(TPB) k_multidot32(long long n4, Tab v, const float4* __restrict__ w, float2* __restrict__ part) {

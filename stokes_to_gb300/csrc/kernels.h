@@ -107,7 +107,7 @@ int axpy_multi_32to64(cudaStream_t st, long long n4, const float4* const* z, con
                       float4* xh = nullptr, float4* xl = nullptr, float4* e = nullptr);
 // first index of the last group of vectors axpy_multi_32to64 sums in one pass
 int axpy_last_chunk(int nz);
-// h[j] = <v_j, w> for j < nv (FP32 per-thread partials, FP64 block and grid sums),
+// h[j] = <v_j, w> for j < nv (FP32 per-thread partials, double-float block and grid sums),
 // and <w, w> into *ww when ww != nullptr
 
 int multidot32(cudaStream_t st, long long n4, const float4* const* v, int nv, const float4* w, double* h, double* scratch,
