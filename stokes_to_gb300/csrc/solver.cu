@@ -1180,9 +1180,15 @@ int stg_set_rhs(stg_t* h, const double* cell_b, const double* const* face_b) {
         h->st = keep;
         STG_TRY(urc);
         STG_CK(cudaEventRecord(h->ec1, h->cst));
-        STG_TRY(ensure_setup(h, false));
-        h->setup_fresh = true;
+        const int src = ensure_setup(h, false);
+        // the handle's stream takes the copy over in every case, so no later call finds
+        // the staging buffer still being written
         STG_CK(cudaStreamWaitEvent(h->st, h->ec1, 0));
+        if (src != STG_OK) {
+            cudaStreamSynchronize(h->cst);
+            return src;
+        }
+        h->setup_fresh = true;
     } else {
         STG_TRY(upload_fields(h, cell_b, face_b, &dc, df));
     }
