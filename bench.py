@@ -28,7 +28,11 @@ Borrvall-Petersson alpha law (amax 1e4). Working set is ~27 GB, far above the 12
          a two-iteration GMRES run per step, scaled the same way.
   --oracle-check: the GPU solutions against the FP64 oracle per field, J and dJ/drho.
   --learned-config: the learned configuration (training on noise and OC trajectories,
-         then learned against plain on solves and the 40-iteration design loop).
+         then learned against plain on solves and the 40-iteration design loop, and the
+         learned warm start against the plain one on that loop).
+  --learned-warm: the learned warm start (warm_start 2, network trained at 64^3 on noise
+         as in the bench's learned leg) against the plain warm start on the n^3
+         40-iteration design loop.
 
 N>1 (torchrun): independent replicas, one per GPU, barrier + max over ranks.
 """
@@ -72,6 +76,8 @@ def parse():
     ap.add_argument("--learned-config", action="store_true",
                     help="train the network per the learned configuration and compare it with plain (minutes)")
     ap.add_argument("--pairs", type=int, default=20000)
+    ap.add_argument("--learned-warm", action="store_true",
+                    help="the learned warm start against the plain one on the 40-iteration design loop")
     return ap.parse_args()
 
 
@@ -524,12 +530,66 @@ def learned_config(args):
                 falls.append(st["fallbacks"])
         res[f"solves_{name}"] = {"s_per_solve": round(float(np.mean(times)), 5), "v_cycles_mean": float(np.mean(its)),
                                  "fallbacks": int(sum(falls))}
-        loop = oc_loop(capi, s, n, 0.15, 40, law)
-        ms = np.array([q[0] for q in loop])
-        vc = np.array([q[1] for q in loop])
-        res[f"loop_{name}"] = {"total_s": round(float(ms.sum()) / 1e3, 3), "ms_per_iteration_median": round(float(np.median(ms)), 2),
-                               "v_cycles_per_iteration_median": float(np.median(vc)), "v_cycles_total": int(vc.sum()),
-                               "final_objective": float(loop[-1][2]), "rel_residual_max": float(max(q[3] for q in loop))}
+        res[f"loop_{name}"] = loop_summary(oc_loop(capi, s, n, 0.15, 40, law))
+        s.close()
+    # the learned warm start: plain solves, each warm start corrected by one learned step
+    s = solver(capi.STG_METHOD_PLAIN, warm_start=2)
+    s.net_init(7)
+    s.net_set_params(params)
+    res["loop_plain_learned_warm_start"] = loop_summary(oc_loop(capi, s, n, 0.15, 40, law))
+    s.close()
+    print(json.dumps(res), flush=True)
+
+
+def loop_summary(loop):
+    ms = np.array([q[0] for q in loop])
+    vc = np.array([q[1] for q in loop])
+    return {"total_s": round(float(ms.sum()) / 1e3, 3), "ms_per_iteration_median": round(float(np.median(ms)), 2),
+            "v_cycles_per_iteration_median": float(np.median(vc)), "v_cycles_total": int(vc.sum()),
+            "final_objective": float(loop[-1][2]), "rel_residual_max": float(max(q[3] for q in loop))}
+
+
+def learned_warm(args):
+    """--learned-warm: the learned warm start (warm_start 2: the previous solution plus one
+    FGMRES step whose preconditioner is the network-corrected V-cycle) against the plain warm
+    start on the n^3 40-iteration OC loop at fraction 0.15, every solve to FP64 rel. residual
+    1e-8; the network trained at 64^3 on seeded noise densities as in the bench's learned
+    leg. One JSON line."""
+    import torch
+
+    from stokes_to_gb300 import build, capi
+
+    build.build()
+    n = args.n
+    law = capi.alpha_bp(1e4)
+
+    def solver(nn, **kw):
+        bc = parabolic_bc(nn)
+        s = capi.Solver(nn, method=capi.STG_METHOD_PLAIN, tol=TOL, **kw)
+        s.set_boundary(bc[0], bc[1], bc[3], bc[4], True)
+        s.set_rhs(bc[2], bc[5])
+        return s
+
+    tr = solver(NET_TRAIN_N)
+    tr.density_noise(1, 4.0, want=False)
+    tr.filter(1.5, None, want=False)
+    tr.set_density(None, law)
+    tr.net_init(7)
+    t0 = time.perf_counter()
+    losses = tr.net_train(NET_TRAIN_STEPS, lr=NET_LR, seed=3)
+    torch.cuda.synchronize()
+    res = {"workload": f"3D {n}^3 40-iteration OC loop at fraction 0.15, plain solves to FP64 rel. residual {TOL:g}: "
+                       "plain warm start against the learned warm start",
+           "train": {"s": round(time.perf_counter() - t0, 1), "steps": NET_TRAIN_STEPS, "n": NET_TRAIN_N,
+                     "final_loss": round(float(np.mean(losses[-100:])), 4)}}
+    params = tr.net_params()
+    tr.close()
+    for ws, name in ((1, "plain_warm_start"), (2, "learned_warm_start")):
+        s = solver(n, warm_start=ws)
+        if ws == 2:
+            s.net_init(7)
+            s.net_set_params(params)
+        res[name] = loop_summary(oc_loop(capi, s, n, 0.15, 40, law))
         s.close()
     print(json.dumps(res), flush=True)
 
@@ -823,6 +883,8 @@ def main():
         oracle_check(args)
     elif args.learned_config:
         learned_config(args)
+    elif args.learned_warm:
+        learned_warm(args)
     else:
         run_ours(args)
 

@@ -63,7 +63,11 @@ typedef struct stg_opts {
     int warm_start;      /* 1: start each solve from the previous solution of the same
                             equation (the forward one for stg_solve, the adjoint one for
                             stg_adjoint_sensitivity) instead of zero, unless its residual
-                            exceeds ||b|| (then zero); 0 (default): zero, as the reference */
+                            exceeds ||b|| (then zero); 2: the same, then a learned
+                            correction of that start (3D, needs a network: one FGMRES step
+                            whose preconditioner is the network-corrected V-cycle, its
+                            length minimising the residual); 0 (default): zero, as the
+                            reference */
     int prolong;         /* coarse-correction transfer of the 3D solver's uniform-form V-cycle:
                             0 the reference's piecewise-constant injection
                             (StokeFlowUpSample3D); 1 face velocities interpolated - linearly

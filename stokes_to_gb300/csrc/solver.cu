@@ -478,6 +478,10 @@ int solve_core(stg_t* h, const d4* b, d4* x, stg_stats* stats) {
         set_error("STG_METHOD_LEARNED needs a network (stg_net_init, then stg_net_train or stg_net_set_params)");
         return STG_E_INVALID;
     }
+    if (h->opts.warm_start == 2 && (!h->net || h->dim != 3)) {
+        set_error("the learned warm start (warm_start 2) needs a 3D handle with a network");
+        return STG_E_INVALID;
+    }
     h->net_on = h->opts.method == STG_METHOD_LEARNED;
     // a zero start makes the first residual b itself (fixed rows cleared in the Laplacian form)
     bool x_zero = !(h->opts.warm_start && h->has_x0(x));
@@ -577,9 +581,22 @@ int solve_core(stg_t* h, const d4* b, d4* x, stg_stats* stats) {
         const double one = 1.0;
         STG_CK(cudaMemcpyAsync(h->dsig2, &one, sizeof(double), cudaMemcpyHostToDevice, h->st));
         double prev_est = beta;
-        for (int j = 0; j < m; j++) {
+        // Learned warm start (warm_start 2): the first refinement step of a warm-started solve
+        // is one FGMRES step whose preconditioner is the learned correction, i.e. the
+        // previous solution plus the step along the network-corrected V-cycle of its
+        // residual that minimises the new residual (never worse than the plain warm start)
+        const bool predict = h->opts.warm_start == 2 && outer == 0 && !x_zero;
+        const int msteps = predict ? 1 : m;
+        for (int j = 0; j < msteps; j++) {
             const bool aug_step = j >= m - have_aug;  // Z[j] holds a stored correction
-            if (!aug_step) {
+            if (predict) {
+                S.learned_iters++;
+                const bool keep = h->net_on;
+                h->net_on = true;
+                const int prc = precond_learned(h, h->V[j], h->Z[j]);
+                h->net_on = keep;
+                STG_TRY(prc);
+            } else if (!aug_step) {
                 if (h->net_on) S.learned_iters++;
                 STG_TRY(h->precond(h, h->V[j], h->Z[j]));
             }

@@ -68,3 +68,38 @@ def test_setup_overlapped_with_rhs_copy(oracle, stg):
     assert sa2["inner_iters"] == sd["inner_iters"]
     for k in range(3):
         assert np.array_equal(va2[k], vd[k])
+
+
+def test_learned_warm_start(oracle, stg):
+    """warm_start 2: a warm-started solve first takes one FGMRES step whose preconditioner
+    is the learned correction of the V-cycle (the step length minimises the residual), then
+    continues as the plain warm start. It needs a network, counts as a learned iteration
+    and reaches the tolerance and solution of the plain warm start."""
+    n = 32
+    b, rho, phys, fp = problem(oracle, n, seed=2)
+    law = stg.alpha_bp(1e4)
+    runs = {}
+    for ws in (1, 2):
+        s = stg.Solver(n, tol=1e-10, warm_start=ws)
+        s.set_boundary_from(b)
+        s.set_density(phys, law)
+        s.set_rhs(b.cell_b, b.face_b)
+        if ws == 2:
+            with pytest.raises(stg.StgError):
+                s.solve()  # no network yet
+            s.net_init(7)
+            s.net_train(300, lr=3e-4, seed=3)
+        _, _, st = s.solve()
+        assert st["learned_iters"] == 0  # a cold start takes no prediction step
+        # the next design, close enough that the previous solution is kept as the start
+        # (the penalty terms of this problem exceed b by about three orders, so a change of
+        # 1e-3 in the density already leaves a residual above ||b|| and a zero start)
+        s.set_density(np.clip(phys * (1.0 + 1e-5), 0.0, 1.0), law)
+        runs[ws] = s.solve()
+        s.close()
+    (p1, v1, st1), (p2, v2, st2) = runs[1], runs[2]
+    assert st2["status"] == 0 and st2["rel_residual"] <= 1e-10 and st2["learned_iters"] == 1
+    assert st1["learned_iters"] == 0
+    for d in range(3):
+        assert relerr(v2[d], v1[d]) < 1e-8
+    assert relerr(pressure_free(p2), pressure_free(p1)) < 1e-8
