@@ -159,11 +159,14 @@ int stg_set_boundary(stg_t* h, const double* cell_vol, const int32_t* cell_fixed
  * FluidEnergy3D::update_penalty. cell_penalty may be NULL (zero). */
 int stg_set_penalty(stg_t* h, const double* cell_penalty, const double* const* face_penalty);
 
-/* FluidSteadyState3D::update_b(cell_b, face_b) (:116-127). */
+/* FluidSteadyState3D::update_b(cell_b, face_b) (:116-127). Returns once the host arrays
+ * have been read. In 3D, a set-up pending since the last penalty change runs while b is
+ * copied, and the next stg_solve uses it instead of repeating it. */
 int stg_set_rhs(stg_t* h, const double* cell_b, const double* const* face_b);
 
 /* FluidSteadyState3D::solve() (:152-170): coarse re-discretisation, smoother and
- * coarsest set-up, then the Krylov solve from a zero initial guess. The results go to
+ * coarsest set-up (unless stg_set_rhs ran it after the last penalty change), then the
+ * Krylov solve from a zero initial guess (or the previous solution, stg_opts.warm_start). The results go to
  * p_out (cells) and vel_out[dim] (faces), the public members p and vel of the
  * reference; either may be NULL to keep the solution on the device only.
  * The solver's own coarse levels differ from the reference's in one rule: a coarse
